@@ -1,0 +1,119 @@
+"""Seeded synthetic meshes for the buckling workloads.
+
+The reference drives its solver from BDF files (examples/cylinder-buckling/
+mech-cylinder.bdf through TACSMeshLoader); the workloads here are generated
+instead, with the same node-major / tensor-order conventions the reference
+assembler expects:
+
+* nodes are numbered ring by ring (axial index i slowest, circumferential
+  index j fastest);
+* element connectivity is in tensor order (xi fastest, then eta), the order
+  TACSMeshLoader produces after its CQUAD4 reorder
+  (src/io/TACSMeshLoader.cpp:932-937);
+* a Dirichlet condition is (node, 6-bit DOF mask, 6 values), the content of
+  one TACSAssembler::addBCs call (src/TACSAssembler.h:104).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+DEFAULT_SEED = 20261203
+
+# Gauss points/weights on [-1, 1] (3-point rule, used for consistent edge loads)
+_G3 = (np.array([-0.774596669241483, 0.0, 0.774596669241483]),
+       np.array([5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0]))
+
+
+@dataclass
+class ShellMesh:
+    """A shell mesh with loads: everything a buckling solve consumes."""
+    X: np.ndarray            # (nn, 3) float64 node coordinates
+    conn: np.ndarray         # (ne, npe) int32 tensor-order connectivity
+    bc_nodes: np.ndarray     # (nb,) int32
+    bc_mask: np.ndarray      # (nb,) int32, bit k set = DOF k fixed
+    bc_vals: np.ndarray      # (nb, 6) float64 prescribed values
+    rhs: np.ndarray          # (nn, 6) float64 consistent nodal loads
+    thickness: np.ndarray    # (ne,) float64 shell thickness per element
+    dv_group: np.ndarray     # (ne,) int32 thickness design group per element
+    E: float = 70e9
+    nu: float = 0.3
+    order: int = 2           # nodes per direction (2 = Quad4, 3 = Quad9)
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def num_nodes(self) -> int:
+        return int(self.X.shape[0])
+
+    @property
+    def num_elements(self) -> int:
+        return int(self.conn.shape[0])
+
+
+def _lagrange_lobatto(order: int, u: np.ndarray) -> np.ndarray:
+    if order == 2:
+        return np.stack([0.5 * (1.0 - u), 0.5 * (1.0 + u)], axis=-1)
+    return np.stack([-0.5 * u * (1.0 - u), (1.0 - u) * (1.0 + u), 0.5 * (1.0 + u) * u], axis=-1)
+
+
+def cylinder(nx: int, ny: int, order: int = 2, R: float = 1.0, L: float = 2.0,
+             t: float = 2e-3, E: float = 70e9, nu: float = 0.3, load: float = 1.0,
+             imperfection: float = 0.01, seed: int = DEFAULT_SEED) -> ShellMesh:
+    """Axially compressed cylinder, axis along x, clamped at x = 0.
+
+    nx, ny: elements along the axis and around the circumference.  The x = L
+    ring carries a uniform compressive axial edge load `load` [N/m] as
+    consistent nodal forces.  A radial imperfection
+    r = R + imperfection*t*sum_k sin(m_k pi x/L) sin(n_k theta + phi_k),
+    (m, n) in {(1, 8), (2, 12), (3, 16)}, phi_k ~ U[0, 2 pi) from `seed`.
+    """
+    p = order - 1
+    nxn, nyn = nx * p + 1, ny * p            # nodes along axis, around
+    rng = np.random.default_rng(seed)
+    phi = rng.uniform(0.0, 2.0 * np.pi, size=3)
+    xs = np.linspace(0.0, L, nxn)
+    th = 2.0 * np.pi * np.arange(nyn) / nyn
+    xx, tt = np.meshgrid(xs, th, indexing="ij")      # (nxn, nyn)
+    r = np.full_like(xx, R)
+    for (m, n), ph in zip(((1, 8), (2, 12), (3, 16)), phi):
+        r += imperfection * t * np.sin(m * np.pi * xx / L) * np.sin(n * tt + ph)
+    X = np.stack([xx, r * np.cos(tt), r * np.sin(tt)], axis=-1).reshape(-1, 3)
+
+    def nid(i, j):
+        return i * nyn + (j % nyn)
+
+    ei, ej = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    ei, ej = ei.ravel(), ej.ravel()
+    cols = []
+    for b in range(order):           # eta (circumferential) slowest
+        for a in range(order):       # xi (axial) fastest
+            cols.append(nid(ei * p + a, ej * p + b))
+    conn = np.stack(cols, axis=1).astype(np.int32)
+
+    bc_nodes = np.array([nid(0, j) for j in range(nyn)], dtype=np.int32)
+    bc_mask = np.full(bc_nodes.shape, 0b111111, dtype=np.int32)
+    bc_vals = np.zeros((bc_nodes.size, 6))
+
+    # Consistent nodal forces of a uniform line load -load*e_x along the
+    # x = L ring: integrate the 1-D shape functions of each element edge.
+    rhs = np.zeros((X.shape[0], 6))
+    gp, gw = _G3
+    N = _lagrange_lobatto(order, gp)              # (3, order)
+    seg = 2.0 * np.pi * R / ny                    # edge length per element
+    for e in range(ny):
+        for a in range(order):
+            node = nid(nx * p, e * p + a)
+            rhs[node, 0] -= load * 0.5 * seg * np.sum(gw * N[:, a])
+
+    ne = conn.shape[0]
+    return ShellMesh(X=X, conn=conn, bc_nodes=bc_nodes, bc_mask=bc_mask, bc_vals=bc_vals,
+                     rhs=rhs, thickness=np.full(ne, t), dv_group=np.zeros(ne, np.int32),
+                     E=E, nu=nu, order=order,
+                     meta=dict(kind="cylinder", nx=nx, ny=ny, R=R, L=L, t=t, load=load,
+                               imperfection=imperfection, seed=seed, phases=phi.tolist()))
+
+
+def classical_cylinder_load(E: float, nu: float, t: float, R: float) -> float:
+    """Classical axial buckling load per unit circumference, E t^2/(R sqrt(3(1-nu^2)))."""
+    return E * t * t / (R * np.sqrt(3.0 * (1.0 - nu * nu)))

@@ -1,0 +1,151 @@
+"""Regenerate the golden fixtures in this directory from the reference itself.
+
+Builds the reference's own C++ sources into oracle/_ref (oracle/ref/Makefile),
+runs its fixture generator (oracle/ref/golden_gen.cpp, real and complex-step
+builds) and packs inputs and outputs into small .npz files:
+
+  elements_<TYPE>.npz   per-element K, G (finite-difference and complex-step),
+                        residual and Jacobian for 6 seeded elements of each of
+                        TACSQuad4Shell, TACSQuad4NonlinearShell,
+                        TACSQuad9Shell, TACSQuad9NonlinearShell
+  <case>.npz            a seeded cylinder: mesh and loads (inputs), the
+                        reference's node CSR, AMD permutation, BCSR pattern,
+                        assembled K and G, ILU pattern and factor, load path
+                        and buckling eigenpairs
+
+Only this container has the reference sources; the fixtures are committed so
+the tests never need them.  Run:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "a2d-shells_gb300"))
+
+from a2ds import mesh as meshgen  # noqa: E402
+
+REF_OUT = os.path.join(REPO, "oracle", "_ref")
+ELEMENT_TYPES = ["TACSQuad4Shell", "TACSQuad4NonlinearShell",
+                 "TACSQuad9Shell", "TACSQuad9NonlinearShell"]
+
+
+def build_reference():
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(REPO, "oracle", "ref"),
+                    f"OUT={REF_OUT}", os.path.join(REF_OUT, "golden_gen"),
+                    os.path.join(REF_OUT, "golden_gen_cplx")], check=True)
+
+
+def load_dir(d):
+    return {f[:-4]: np.load(os.path.join(d, f)) for f in os.listdir(d) if f.endswith(".npy")}
+
+
+def make_elements():
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([os.path.join(REF_OUT, "golden_gen"), "element", d], check=True)
+        subprocess.run([os.path.join(REF_OUT, "golden_gen_cplx"), "element", d], check=True)
+        arrs = load_dir(d)
+    for name in ELEMENT_TYPES:
+        pre = name + "_"
+        out = {k[len(pre):]: v for k, v in arrs.items() if k.startswith(pre)}
+        np.savez_compressed(os.path.join(HERE, f"elements_{name}.npz"), **out)
+        print("wrote", f"elements_{name}.npz", sorted(out))
+
+
+def write_inputs(d, m: meshgen.ShellMesh, sigma, lev, gm_m, gm_restarts, lanczos, neig,
+                 nonlinear=0, gm_tol=1e-12, temperature=0.0, alpha_t=0.0):
+    np.save(os.path.join(d, "X.npy"), np.ascontiguousarray(m.X, dtype=np.float64))
+    np.save(os.path.join(d, "conn.npy"), np.ascontiguousarray(m.conn, dtype=np.int32))
+    np.save(os.path.join(d, "bc_nodes.npy"), m.bc_nodes.astype(np.int32))
+    np.save(os.path.join(d, "bc_mask.npy"), m.bc_mask.astype(np.int32))
+    np.save(os.path.join(d, "bc_vals.npy"), np.ascontiguousarray(m.bc_vals, dtype=np.float64))
+    np.save(os.path.join(d, "rhs.npy"), np.ascontiguousarray(m.rhs, dtype=np.float64))
+    np.save(os.path.join(d, "elem_thickness.npy"), m.thickness.astype(np.float64))
+    prm = np.array([m.E, m.nu, sigma, lev, gm_m, gm_restarts, lanczos, neig, nonlinear,
+                    gm_tol, temperature, alpha_t], dtype=np.float64)
+    np.save(os.path.join(d, "params.npy"), prm)
+
+
+def dense_eigs(fx, neig):
+    """Lowest buckling loads of K x + lam G x = 0 on the free DOFs (dense)."""
+    import scipy.linalg as sla
+    n = fx["bcsr_rowp"].size - 1
+    rowp, cols = fx["bcsr_rowp"], fx["bcsr_cols"]
+
+    def dense(vals):
+        A = np.zeros((6 * n, 6 * n))
+        for i in range(n):
+            for jp in range(rowp[i], rowp[i + 1]):
+                j = cols[jp]
+                A[6 * i:6 * i + 6, 6 * j:6 * j + 6] = vals[jp]
+        return A
+    K, G = dense(fx["K_after"]), dense(fx["G"])
+    perm = fx["amd_perm"]
+    bcdof = np.zeros(6 * n, bool)
+    inv = np.empty(n, np.int64)
+    inv[perm] = np.arange(n)
+    for node, mask in zip(fx["bc_nodes"], fx["bc_mask"]):
+        for k in range(6):
+            if mask >> k & 1:
+                bcdof[6 * inv[node] + k] = True
+    free = ~bcdof
+    Kf = 0.5 * (K[np.ix_(free, free)] + K[np.ix_(free, free)].T)
+    Gf = 0.5 * (G[np.ix_(free, free)] + G[np.ix_(free, free)].T)
+    mu = sla.eigh(-Gf, Kf, eigvals_only=True)      # mu = 1/lambda
+    lam = 1.0 / mu[mu > 0]
+    lam = np.sort(lam)
+    return lam[:neig]
+
+
+def run_case(name, m, lev, gm_m, gm_restarts, lanczos, neig, sigma=None, nonlinear=0):
+    with tempfile.TemporaryDirectory() as d:
+        ind, outd = os.path.join(d, "in"), os.path.join(d, "out")
+        os.makedirs(ind)
+        os.makedirs(outd)
+        s0 = sigma if sigma is not None else 1e4
+        write_inputs(ind, m, s0, lev, gm_m, gm_restarts, lanczos, neig, nonlinear)
+        subprocess.run([os.path.join(REF_OUT, "golden_gen"), "assembly", ind, outd], check=True)
+        fx = load_dir(outd)
+        fx.update(bc_nodes=m.bc_nodes, bc_mask=m.bc_mask)
+        lam_dense = dense_eigs(fx, neig)
+        if sigma is None:
+            # Second pass with the shift just below the lowest dense eigenvalue
+            sigma = 0.95 * lam_dense[0]
+            write_inputs(ind, m, sigma, lev, gm_m, gm_restarts, lanczos, neig, nonlinear)
+            subprocess.run([os.path.join(REF_OUT, "golden_gen"), "assembly", ind, outd],
+                           check=True)
+        subprocess.run([os.path.join(REF_OUT, "golden_gen_cplx"), "assembly", ind, outd],
+                       check=True)
+        fx = load_dir(outd)
+    out = dict(fx)
+    out.update(X=m.X, conn=m.conn, bc_nodes=m.bc_nodes, bc_mask=m.bc_mask, bc_vals=m.bc_vals,
+               rhs=m.rhs, thickness=m.thickness, E=np.float64(m.E), nu=np.float64(m.nu),
+               sigma=np.float64(sigma), lev=np.int32(lev), gm_m=np.int32(gm_m),
+               gm_restarts=np.int32(gm_restarts), lanczos=np.int32(lanczos),
+               neig=np.int32(neig), nonlinear=np.int32(nonlinear),
+               eigvals_dense=lam_dense)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    rel = np.abs(out["eigvals"][:3] - lam_dense[:3]) / lam_dense[:3]
+    print("wrote", f"{name}.npz", "nnzb", out["bcsr_cols"].size, "eig", out["eigvals"][:3],
+          "dense", lam_dense[:3], "rel", rel)
+
+
+def main():
+    build_reference()
+    make_elements()
+    run_case("cyl_q4_4x8_lu", meshgen.cylinder(4, 8, order=2), lev=1000000, gm_m=10,
+             gm_restarts=15, lanczos=100, neig=50)
+    run_case("cyl_q4_8x16_ilu1", meshgen.cylinder(8, 16, order=2), lev=1, gm_m=30,
+             gm_restarts=15, lanczos=100, neig=50)
+    run_case("cyl_q9_2x4_lu", meshgen.cylinder(2, 4, order=3), lev=1000000, gm_m=10,
+             gm_restarts=15, lanczos=100, neig=50)
+
+
+if __name__ == "__main__":
+    main()
