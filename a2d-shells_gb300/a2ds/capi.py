@@ -1,0 +1,296 @@
+"""ctypes binding of the C ABI in include/a2ds.h, plus thin Python classes
+that mirror the reference's call surface for this path:
+
+  Assembler        TACSAssembler (src/TACSAssembler.h:59): mesh, material,
+                   Dirichlet conditions, initialize, assembleMatType,
+                   assembleRes, assembleJacobian
+  BCSRMat          TACSSchurMat / BCSRMat (src/bpmat/BCSRMat.h:34): getArrays,
+                   mult, copyValues, axpy, applyBCs
+  SchurPc          TACSSchurPc (src/bpmat/TACSSchurMat.h:148): ILU(k) factor
+  LinearBuckling   TACSLinearBuckling (src/TACSBuckling.h:43)
+
+All arrays are numpy; every call goes to the GB300 library and raises
+A2dsError on a non-zero status.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "liba2ds_gpu.so")
+
+A2DS_STIFFNESS_MATRIX = 0
+A2DS_GEOMETRIC_STIFFNESS_MATRIX = 2
+A2DS_NATURAL_ORDER = 0
+A2DS_TACS_AMD_ORDER = 4
+A2DS_SCATTER_ATOMIC = 0
+A2DS_SCATTER_COLORED = 1
+
+ERRORS = {1: "A2DS_ERR_ARG", 2: "A2DS_ERR_STATE", 3: "A2DS_ERR_CUDA", 4: "A2DS_ERR_NOMEM",
+          5: "A2DS_ERR_SINGULAR", 6: "A2DS_ERR_NOCONV", 7: "A2DS_ERR_BREAKDOWN",
+          8: "A2DS_ERR_NUMERIC"}
+
+# Every entry point of include/a2ds.h
+EXPORTS = [
+    "a2ds_last_error", "a2ds_device_count", "a2ds_mesh_create", "a2ds_mesh_destroy",
+    "a2ds_mesh_set_material", "a2ds_mesh_set_thickness", "a2ds_mesh_add_bcs",
+    "a2ds_mesh_plan", "a2ds_mesh_get_pattern", "a2ds_mesh_ilu_pattern",
+    "a2ds_mesh_initialize", "a2ds_mesh_get_ordering", "a2ds_mesh_node_csr",
+    "a2ds_bcsr_create", "a2ds_bcsr_destroy", "a2ds_bcsr_get", "a2ds_bcsr_set_values",
+    "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
+    "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
+    "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
+    "a2ds_pc_apply", "a2ds_pc_get", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
+    "a2ds_buckling_stats", "a2ds_eig_sens_thickness",
+]
+
+
+class A2dsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class BucklingOpts(ctypes.Structure):
+    """a2ds_buckling_opts"""
+    _fields_ = [("sigma", ctypes.c_double), ("max_lanczos", ctypes.c_int),
+                ("num_eigvals", ctypes.c_int), ("eig_tol", ctypes.c_double),
+                ("lev_fill", ctypes.c_int), ("gmres_m", ctypes.c_int),
+                ("gmres_restarts", ctypes.c_int), ("gmres_rtol", ctypes.c_double),
+                ("gmres_atol", ctypes.c_double), ("precision", ctypes.c_int),
+                ("seed", ctypes.c_int)]
+
+
+_lib = None
+
+P_D = ctypes.POINTER(ctypes.c_double)
+P_I = ctypes.POINTER(ctypes.c_int)
+VP = ctypes.c_void_p
+
+
+def load(build: bool = False):
+    """Load liba2ds_gpu.so (building it first when asked or when missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build or not os.path.exists(LIB_PATH):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("a2ds_build", os.path.join(PKG, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.a2ds_last_error.restype = ctypes.c_char_p
+    lib.a2ds_device_count.restype = ctypes.c_int
+    lib.a2ds_mesh_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P_I, P_D,
+                                     ctypes.c_int, ctypes.POINTER(VP)]
+    lib.a2ds_mesh_destroy.argtypes = [VP]
+    lib.a2ds_mesh_set_material.argtypes = [VP, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double]
+    lib.a2ds_mesh_set_thickness.argtypes = [VP, ctypes.c_int, P_D, P_I]
+    lib.a2ds_mesh_add_bcs.argtypes = [VP, ctypes.c_int, P_I, P_I, P_D]
+    lib.a2ds_mesh_initialize.argtypes = [VP, ctypes.c_int]
+    lib.a2ds_mesh_plan.argtypes = [VP, ctypes.c_int]
+    lib.a2ds_mesh_get_pattern.argtypes = [VP, P_I, P_I, P_I]
+    lib.a2ds_mesh_ilu_pattern.argtypes = [VP, ctypes.c_int, P_I, P_I, P_I]
+    lib.a2ds_mesh_get_ordering.argtypes = [VP, P_I]
+    lib.a2ds_mesh_node_csr.argtypes = [VP, ctypes.c_int, P_I, P_I, P_I]
+    lib.a2ds_bcsr_create.argtypes = [VP, ctypes.POINTER(VP)]
+    lib.a2ds_bcsr_destroy.argtypes = [VP]
+    lib.a2ds_bcsr_get.argtypes = [VP, P_I, P_I, P_I, P_I, P_D]
+    lib.a2ds_bcsr_set_values.argtypes = [VP, P_D]
+    lib.a2ds_assemble_mat.argtypes = [VP, ctypes.c_int, P_D, VP]
+    lib.a2ds_assemble_mat_ex.argtypes = [VP, ctypes.c_int, P_D, VP, ctypes.c_int]
+    lib.a2ds_assemble_res.argtypes = [VP, P_D, P_D]
+    lib.a2ds_assemble_jacobian.argtypes = [VP, P_D, P_D, VP]
+    lib.a2ds_bcsr_mult.argtypes = [VP, P_D, P_D]
+    lib.a2ds_bcsr_mult_rows.argtypes = [VP, P_D, P_D]
+    lib.a2ds_bcsr_copy.argtypes = [VP, VP]
+    lib.a2ds_bcsr_axpy.argtypes = [VP, ctypes.c_double, VP]
+    lib.a2ds_bcsr_apply_bcs.argtypes = [VP]
+    lib.a2ds_pc_create.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(VP)]
+    lib.a2ds_pc_destroy.argtypes = [VP]
+    lib.a2ds_pc_factor.argtypes = [VP, VP]
+    lib.a2ds_pc_apply.argtypes = [VP, P_D, P_D]
+    lib.a2ds_pc_get.argtypes = [VP, P_I, P_I, P_I, P_I, P_D]
+    lib.a2ds_buckling_default_opts.argtypes = [ctypes.POINTER(BucklingOpts)]
+    lib.a2ds_buckling_default_opts.restype = None
+    lib.a2ds_buckling_solve.argtypes = [VP, ctypes.POINTER(BucklingOpts), P_D, P_D, P_D, P_D, P_D]
+    lib.a2ds_buckling_stats.argtypes = [VP, ctypes.c_int, P_D]
+    lib.a2ds_eig_sens_thickness.argtypes = [VP, ctypes.c_int, P_D]
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise A2dsError(rc, _lib.a2ds_last_error().decode())
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(P_D)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(P_I)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Assembler:
+    """TACSAssembler for one shell element type (Quad4 / Quad9, linear or
+    nonlinear strain), one GPU."""
+
+    def __init__(self, X, conn, nonlinear=False):
+        self.lib = load()
+        X = _f64(X).reshape(-1, 3)
+        conn = _i32(conn)
+        self.num_nodes, self.num_elements = X.shape[0], conn.shape[0]
+        self.nodes_per_elem = conn.shape[1]
+        h = VP()
+        _check(self.lib.a2ds_mesh_create(self.num_nodes, self.num_elements,
+                                         self.nodes_per_elem, _i(conn), _d(X),
+                                         int(bool(nonlinear)), ctypes.byref(h)))
+        self.h = h
+        self._keep = (X, conn)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.a2ds_mesh_destroy(self.h)
+            self.h = None
+
+    def set_material(self, E, nu, alpha=0.0, temperature=0.0):
+        _check(self.lib.a2ds_mesh_set_material(self.h, E, nu, alpha, temperature))
+
+    def set_thickness(self, t, elem_group=None):
+        t = _f64(np.atleast_1d(t))
+        g = _i32(elem_group)
+        _check(self.lib.a2ds_mesh_set_thickness(self.h, t.size, _d(t), _i(g)))
+
+    def add_bcs(self, nodes, masks, vals=None):
+        nodes, masks = _i32(nodes), _i32(masks)
+        vals = _f64(vals)
+        _check(self.lib.a2ds_mesh_add_bcs(self.h, nodes.size, _i(nodes), _i(masks), _d(vals)))
+
+    def plan(self, order=A2DS_NATURAL_ORDER):
+        """Host-only pattern and ordering (no GPU needed)."""
+        _check(self.lib.a2ds_mesh_plan(self.h, order))
+
+    def initialize(self, order=A2DS_NATURAL_ORDER):
+        _check(self.lib.a2ds_mesh_initialize(self.h, order))
+
+    def get_pattern(self):
+        nz = ctypes.c_int()
+        _check(self.lib.a2ds_mesh_get_pattern(self.h, ctypes.byref(nz), None, None))
+        rowp = np.zeros(self.num_nodes + 1, np.int32)
+        cols = np.zeros(nz.value, np.int32)
+        _check(self.lib.a2ds_mesh_get_pattern(self.h, None, _i(rowp), _i(cols)))
+        return rowp, cols
+
+    def ilu_pattern(self, lev_fill):
+        nz = ctypes.c_int()
+        _check(self.lib.a2ds_mesh_ilu_pattern(self.h, lev_fill, ctypes.byref(nz), None, None))
+        rowp = np.zeros(self.num_nodes + 1, np.int32)
+        cols = np.zeros(nz.value, np.int32)
+        _check(self.lib.a2ds_mesh_ilu_pattern(self.h, lev_fill, None, _i(rowp), _i(cols)))
+        return rowp, cols
+
+    def get_ordering(self):
+        p = np.zeros(self.num_nodes, np.int32)
+        _check(self.lib.a2ds_mesh_get_ordering(self.h, _i(p)))
+        return p
+
+    def node_csr(self, nodiag=False):
+        nnz = ctypes.c_int()
+        _check(self.lib.a2ds_mesh_node_csr(self.h, int(nodiag), ctypes.byref(nnz), None, None))
+        rowp = np.zeros(self.num_nodes + 1, np.int32)
+        cols = np.zeros(nnz.value, np.int32)
+        _check(self.lib.a2ds_mesh_node_csr(self.h, int(nodiag), None, _i(rowp), _i(cols)))
+        return rowp, cols
+
+    def create_mat(self):
+        return BCSRMat(self)
+
+    def assemble_mat_type(self, mat_type, A, vars_=None, scatter=A2DS_SCATTER_ATOMIC):
+        v = _f64(vars_)
+        _check(self.lib.a2ds_assemble_mat_ex(self.h, mat_type, _d(v), A.h, scatter))
+
+    def assemble_res(self, vars_=None):
+        v = _f64(vars_)
+        res = np.zeros((self.num_nodes, 6))
+        _check(self.lib.a2ds_assemble_res(self.h, _d(v), _d(res)))
+        return res
+
+    def assemble_jacobian(self, A, vars_=None, want_res=True):
+        v = _f64(vars_)
+        res = np.zeros((self.num_nodes, 6)) if want_res else None
+        _check(self.lib.a2ds_assemble_jacobian(self.h, _d(v), _d(res), A.h))
+        return res
+
+
+class BCSRMat:
+    """Device BCSR matrix in the assembler's ordering."""
+
+    def __init__(self, assembler: Assembler):
+        self.a = assembler
+        self.lib = assembler.lib
+        h = VP()
+        _check(self.lib.a2ds_bcsr_create(assembler.h, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.a2ds_bcsr_destroy(self.h)
+            self.h = None
+
+    def get_arrays(self):
+        nr, nz = ctypes.c_int(), ctypes.c_int()
+        _check(self.lib.a2ds_bcsr_get(self.h, ctypes.byref(nr), ctypes.byref(nz), None, None,
+                                      None))
+        rowp = np.zeros(nr.value + 1, np.int32)
+        cols = np.zeros(nz.value, np.int32)
+        vals = np.zeros((nz.value, 6, 6))
+        _check(self.lib.a2ds_bcsr_get(self.h, None, None, _i(rowp), _i(cols), _d(vals)))
+        return rowp, cols, vals
+
+    def set_values(self, vals):
+        v = _f64(vals)
+        _check(self.lib.a2ds_bcsr_set_values(self.h, _d(v)))
+
+    def mult(self, x):
+        x = _f64(x).reshape(-1, 6)
+        y = np.zeros_like(x)
+        _check(self.lib.a2ds_bcsr_mult(self.h, _d(x), _d(y)))
+        return y
+
+    def copy_values(self, other):
+        _check(self.lib.a2ds_bcsr_copy(self.h, other.h))
+
+    def axpy(self, alpha, other):
+        _check(self.lib.a2ds_bcsr_axpy(self.h, float(alpha), other.h))
+
+    def apply_bcs(self):
+        _check(self.lib.a2ds_bcsr_apply_bcs(self.h))
+
+    def to_dense_nodes(self):
+        """Dense (6n x 6n) matrix in the caller's node numbering."""
+        rowp, cols, vals = self.get_arrays()
+        perm = self.a.get_ordering()
+        n = rowp.size - 1
+        A = np.zeros((6 * n, 6 * n))
+        for i in range(n):
+            r = perm[i]
+            for jp in range(rowp[i], rowp[i + 1]):
+                c = perm[cols[jp]]
+                A[6 * r:6 * r + 6, 6 * c:6 * c + 6] = vals[jp]
+        return A

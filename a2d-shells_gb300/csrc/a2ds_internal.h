@@ -1,0 +1,97 @@
+// Internal declarations shared by the a2ds translation units (host C++ and
+// CUDA).  Not part of the public ABI (include/a2ds.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "a2ds.h"
+
+namespace a2ds {
+
+// ------------------------------------------------------------------ errors
+struct Error {
+  int code;
+  std::string msg;
+};
+void set_error(int code, const std::string &msg);
+int fail(int code, const std::string &msg);  // sets and returns code
+const char *last_error_cstr();
+
+#define A2DS_CUDA_TRY(expr)                                                  \
+  do {                                                                       \
+    cudaError_t _e = (expr);                                                 \
+    if (_e != cudaSuccess)                                                   \
+      return ::a2ds::fail(A2DS_ERR_CUDA, std::string(#expr) + ": " +         \
+                                             cudaGetErrorString(_e));        \
+  } while (0)
+
+// ----------------------------------------------------------- device buffer
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  int alloc(size_t count) {
+    if (count == n && p) return 0;
+    release();
+    if (count == 0) return 0;
+    cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(A2DS_ERR_NOMEM, std::string("cudaMalloc of ") +
+                                      std::to_string(count * sizeof(T)) + " bytes: " +
+                                      cudaGetErrorString(e));
+    }
+    n = count;
+    return 0;
+  }
+  int upload(const T *h, size_t count, cudaStream_t s) {
+    int rc = alloc(count);
+    if (rc) return rc;
+    if (count) A2DS_CUDA_TRY(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+};
+
+// --------------------------------------------------------- element kernel
+enum ElemMode { MODE_K = 0, MODE_G = 1, MODE_R = 2, MODE_KR = 3 };
+
+struct ElemLaunch {
+  int order;             // 2 or 3
+  int nonlinear;         // model: 0 linear, 1 nonlinear
+  int mode;              // ElemMode
+  int num_elements;      // elements in this launch (subset via elem_list)
+  const int *elem_list;  // element ids for this launch (NULL = 0..num_elements-1)
+  const int *conn;       // Ne x NN, node rows in matrix ordering
+  const int *slots;      // Ne x NN*NN block indices
+  const double *X;       // Nn x 3, matrix ordering
+  const double *state;   // Nn x 6, matrix ordering (NULL = zero)
+  const double *tvals;   // thickness per group
+  const int *tgroup;     // group per element
+  double E, nu, alpha, temperature;
+  double *vals;          // BCSR values (36 per block) or NULL
+  double *res;           // residual (Nn x 6) or NULL
+  int atomic_scatter;    // 1 atomics, 0 plain adds (colour-ordered launch)
+};
+
+int launch_element_kernel(const ElemLaunch &L, cudaStream_t s);
+int upload_shell_tables();
+
+// ---------------------------------------------------------- BCSR helpers
+int launch_apply_bc_rows(double *vals, const int *rowp, const int *cols,
+                         const int *bc_rows, const int *bc_masks, int nbc,
+                         cudaStream_t s);
+
+}  // namespace a2ds

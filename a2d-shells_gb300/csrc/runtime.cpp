@@ -1,0 +1,215 @@
+// Host runtime behind the C ABI: mesh handles (the TACSAssembler role),
+// BCSR matrix handles (TACSSchurMat / BCSRMat role), the node-to-node
+// pattern, the matrix ordering, element-slot maps and element colours.
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "a2ds_internal.h"
+#include "host_graph.h"
+#include "kernels.h"
+#include "runtime.h"
+
+namespace a2ds {
+
+static thread_local std::string g_last_error;
+
+void set_error(int code, const std::string &msg) {
+  (void)code;
+  g_last_error = msg;
+}
+const char *last_error_cstr() { return g_last_error.c_str(); }
+
+int fail(int code, const std::string &msg) {
+  set_error(code, msg);
+  return code;
+}
+
+int ensure_device() {
+  static std::once_flag once;
+  static int status = 0;
+  static std::string msg;
+  std::call_once(once, [] {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+      status = A2DS_ERR_CUDA;
+      msg = std::string("no usable CUDA device: ") +
+            (e != cudaSuccess ? cudaGetErrorString(e) : "device count is 0");
+      return;
+    }
+    int rc = upload_shell_tables();
+    if (rc) {
+      status = rc;
+      msg = g_last_error;
+    }
+  });
+  if (status) return fail(status, msg);
+  return 0;
+}
+
+// ------------------------------------------------------------ mesh setup
+int Mesh::build_pattern() {
+  // node -> node pattern with the diagonal, sorted and unique per row
+  // (TACSAssembler::computeLocalNodeToNodeCSR + TacsSortAndUniquifyCSR)
+  node_csr(nn, ne, npe, conn.data(), 0, node_rowp, node_cols);
+
+  perm.resize(nn);
+  if (order_type == A2DS_TACS_AMD_ORDER) {
+    std::vector<int> rp, cl;
+    node_csr(nn, ne, npe, conn.data(), 1, rp, cl);
+    amd_order(nn, rp, cl, perm);
+  } else {
+    std::iota(perm.begin(), perm.end(), 0);
+  }
+  iperm.assign(nn, -1);
+  for (int i = 0; i < nn; i++) iperm[perm[i]] = i;
+
+  // BCSR pattern in the row ordering: row i <-> node perm[i]
+  rowp.assign(nn + 1, 0);
+  for (int i = 0; i < nn; i++) {
+    int node = perm[i];
+    rowp[i + 1] = rowp[i] + (node_rowp[node + 1] - node_rowp[node]);
+  }
+  cols.resize(rowp[nn]);
+  for (int i = 0; i < nn; i++) {
+    int node = perm[i];
+    int *c = &cols[rowp[i]];
+    int k = 0;
+    for (int jp = node_rowp[node]; jp < node_rowp[node + 1]; jp++) c[k++] = iperm[node_cols[jp]];
+    std::sort(c, c + k);
+  }
+  nnzb = rowp[nn];
+
+  // element connectivity in rows, and the element-slot map
+  const int nn2 = npe * npe;
+  conn_rows.resize((size_t)ne * npe);
+  slots.resize((size_t)ne * nn2);
+  for (int e = 0; e < ne; e++) {
+    for (int a = 0; a < npe; a++) conn_rows[(size_t)e * npe + a] = iperm[conn[(size_t)e * npe + a]];
+    for (int a = 0; a < npe; a++) {
+      int r = conn_rows[(size_t)e * npe + a];
+      const int *c0 = &cols[rowp[r]], *c1 = &cols[rowp[r + 1]];
+      for (int b = 0; b < npe; b++) {
+        int c = conn_rows[(size_t)e * npe + b];
+        const int *f = std::lower_bound(c0, c1, c);
+        if (f == c1 || *f != c)
+          return fail(A2DS_ERR_STATE, "internal: element block missing from the pattern");
+        slots[(size_t)e * nn2 + a * npe + b] = (int)(rowp[r] + (f - c0));
+      }
+    }
+  }
+
+  // element colours (no two elements of one colour share a node)
+  greedy_element_colors(nn, ne, npe, conn.data(), color_ptr, color_elems);
+
+  // Dirichlet rows
+  bc_rows.resize(bc_nodes.size());
+  for (size_t b = 0; b < bc_nodes.size(); b++) bc_rows[b] = iperm[bc_nodes[b]];
+  return 0;
+}
+
+int Mesh::upload() {
+  int rc;
+  std::vector<double> Xr((size_t)nn * 3);
+  for (int i = 0; i < nn; i++)
+    for (int c = 0; c < 3; c++) Xr[(size_t)i * 3 + c] = X[(size_t)perm[i] * 3 + c];
+  if ((rc = d_X.upload(Xr.data(), Xr.size(), stream))) return rc;
+  if ((rc = d_conn.upload(conn_rows.data(), conn_rows.size(), stream))) return rc;
+  if ((rc = d_slots.upload(slots.data(), slots.size(), stream))) return rc;
+  if ((rc = d_rowp.upload(rowp.data(), rowp.size(), stream))) return rc;
+  if ((rc = d_cols.upload(cols.data(), cols.size(), stream))) return rc;
+  if ((rc = d_tvals.upload(tvals.data(), tvals.size(), stream))) return rc;
+  if ((rc = d_tgroup.upload(tgroup.data(), tgroup.size(), stream))) return rc;
+  if ((rc = d_bc_rows.upload(bc_rows.data(), bc_rows.size(), stream))) return rc;
+  if ((rc = d_bc_masks.upload(bc_masks.data(), bc_masks.size(), stream))) return rc;
+  if ((rc = d_color_elems.upload(color_elems.data(), color_elems.size(), stream))) return rc;
+  if ((rc = d_state.alloc((size_t)nn * 6))) return rc;
+  if ((rc = d_res.alloc((size_t)nn * 6))) return rc;
+  A2DS_CUDA_TRY(cudaStreamSynchronize(stream));
+  return 0;
+}
+
+// Node-ordered host vector -> row-ordered device vector
+int Mesh::to_rows(const double *h, DBuf<double> &d) {
+  int rc = d.alloc((size_t)nn * 6);
+  if (rc) return rc;
+  h_tmp.resize((size_t)nn * 6);
+  if (h) {
+    for (int i = 0; i < nn; i++) memcpy(&h_tmp[(size_t)i * 6], &h[(size_t)perm[i] * 6], 6 * sizeof(double));
+  } else {
+    std::fill(h_tmp.begin(), h_tmp.end(), 0.0);
+  }
+  A2DS_CUDA_TRY(cudaMemcpyAsync(d.p, h_tmp.data(), h_tmp.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(stream));
+  return 0;
+}
+
+// Row-ordered device vector -> node-ordered host vector
+int Mesh::from_rows(const double *d, double *h) {
+  h_tmp.resize((size_t)nn * 6);
+  A2DS_CUDA_TRY(cudaMemcpyAsync(h_tmp.data(), d, h_tmp.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(stream));
+  for (int i = 0; i < nn; i++) memcpy(&h[(size_t)perm[i] * 6], &h_tmp[(size_t)i * 6], 6 * sizeof(double));
+  return 0;
+}
+
+ElemLaunch Mesh::launch_params(int mode, const double *d_st, double *vals, double *res) const {
+  ElemLaunch L;
+  memset(&L, 0, sizeof(L));
+  L.order = order;
+  L.nonlinear = nonlinear;
+  L.mode = mode;
+  L.num_elements = ne;
+  L.elem_list = nullptr;
+  L.conn = d_conn.p;
+  L.slots = d_slots.p;
+  L.X = d_X.p;
+  L.state = d_st;
+  L.tvals = d_tvals.p;
+  L.tgroup = d_tgroup.p;
+  L.E = E;
+  L.nu = nu;
+  L.alpha = alpha;
+  L.temperature = temperature;
+  L.vals = vals;
+  L.res = res;
+  L.atomic_scatter = 1;
+  return L;
+}
+
+// Element assembly into vals (zeroed first) and/or res, device state
+int Mesh::assemble_device(int mode, const double *d_st, double *vals, double *res, int scatter) {
+  int rc;
+  if (vals) A2DS_CUDA_TRY(cudaMemsetAsync(vals, 0, (size_t)nnzb * 36 * sizeof(double), stream));
+  if (res) A2DS_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)nn * 6 * sizeof(double), stream));
+  ElemLaunch L = launch_params(mode, d_st, vals, res);
+  if (scatter == A2DS_SCATTER_COLORED) {
+    L.atomic_scatter = 0;
+    const int ncol = (int)color_ptr.size() - 1;
+    for (int c = 0; c < ncol; c++) {
+      L.elem_list = d_color_elems.p + color_ptr[c];
+      L.num_elements = color_ptr[c + 1] - color_ptr[c];
+      if ((rc = launch_element_kernel(L, stream))) return rc;
+      launches++;
+    }
+  } else {
+    if ((rc = launch_element_kernel(L, stream))) return rc;
+    launches++;
+  }
+  if (vals) {
+    if ((rc = launch_apply_bc_rows(vals, d_rowp.p, d_cols.p, d_bc_rows.p, d_bc_masks.p,
+                                   (int)bc_rows.size(), stream)))
+      return rc;
+    launches++;
+  }
+  return 0;
+}
+
+}  // namespace a2ds

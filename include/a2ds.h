@@ -1,0 +1,246 @@
+/*
+  a2ds -- GB300 (sm_103a) buckling hot path of the a2d-shells director-MITC
+  shell code, behind a plain C ABI.
+
+  Every entry point returns 0 on success or a positive A2DS_ERR_* code; the
+  message of the last failure on the calling thread is a2ds_last_error().
+  All pointers are caller-owned HOST buffers (copied in or out during the
+  call; nothing is retained).  Device memory is owned by the handles.  Calls
+  on one handle must not overlap; distinct handles may be used from
+  different threads.  There is no CPU fallback: without a usable CUDA device
+  every call that needs one fails with A2DS_ERR_CUDA.
+
+  Vectors are node-major with 6 DOF per node (u, v, w, q1, q2, q3) in the
+  caller's node numbering, as TACSBVec stores them (src/bpmat/TACSBVec.h:67).
+  Element connectivity is in tensor order (xi fastest), as TACSAssembler
+  expects after TACSMeshLoader's CQUAD4 reorder (src/io/TACSMeshLoader.cpp:
+  932-937).  Block-CSR arrays use the reference layout BCSRMatData
+  (src/bpmat/BCSRMatImpl.h:27-45): row-major 6x6 blocks, rows in the matrix
+  ordering (see a2ds_mesh_get_ordering), sorted column indices.
+*/
+#ifndef A2DS_H
+#define A2DS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define A2DS_OK 0
+#define A2DS_ERR_ARG 1        /* invalid argument or size */
+#define A2DS_ERR_STATE 2      /* call out of order (e.g. before initialize) */
+#define A2DS_ERR_CUDA 3       /* CUDA runtime error / no device */
+#define A2DS_ERR_NOMEM 4      /* device or host allocation failed */
+#define A2DS_ERR_SINGULAR 5   /* zero pivot block in a factorization */
+#define A2DS_ERR_NOCONV 6     /* iterative solve did not reach its tolerance */
+#define A2DS_ERR_BREAKDOWN 7  /* Lanczos breakdown (beta ~ 0) */
+#define A2DS_ERR_NUMERIC 8    /* NaN/Inf detected on the device */
+
+/* Element matrix kinds, numbered as ElementMatrixType
+   (src/elements/TACSElementTypes.h:101-107). */
+#define A2DS_STIFFNESS_MATRIX 0
+#define A2DS_GEOMETRIC_STIFFNESS_MATRIX 2
+
+/* Node orderings for the matrix, numbered as TACSAssembler::OrderingType
+   (src/TACSAssembler.h:64-71). */
+#define A2DS_NATURAL_ORDER 0
+#define A2DS_TACS_AMD_ORDER 4
+
+/* Scatter strategies for element-to-BCSR assembly. */
+#define A2DS_SCATTER_ATOMIC 0   /* FP64 atomic adds (fastest, order-dependent rounding) */
+#define A2DS_SCATTER_COLORED 1  /* element colours, plain adds (bitwise reproducible) */
+
+typedef struct a2ds_mesh_s *a2ds_mesh;
+typedef struct a2ds_bcsr_s *a2ds_bcsr;
+typedef struct a2ds_pc_s *a2ds_pc;
+
+/* Message for the last failed call on this thread ("" if none). */
+const char *a2ds_last_error(void);
+
+/* Number of CUDA devices visible (0 if none); never fails. */
+int a2ds_device_count(void);
+
+/* ------------------------------------------------------------------ mesh
+   Replaces: TACSAssembler(comm, 6, numOwnedNodes, numElements)
+   (src/TACSAssembler.h:81), setElementConnectivity (:88), setElements (:90)
+   with one TACSQuad{4,9}[Nonlinear]Shell type for all elements
+   (src/elements/shell/TACSShellElementDefs.h:12-33), and setNodes (:156).
+   nodes_per_elem is 4 (Quad4) or 9 (Quad9); conn is num_elements x
+   nodes_per_elem; X is num_nodes x 3. */
+int a2ds_mesh_create(int num_nodes, int num_elements, int nodes_per_elem,
+                     const int *conn, const double *X, int nonlinear,
+                     a2ds_mesh *out);
+int a2ds_mesh_destroy(a2ds_mesh mesh);
+
+/* Isotropic material (TACSMaterialProperties iso ctor,
+   src/constitutive/TACSMaterialProperties.cpp:24-63) shared by all
+   elements, plus the element temperature (TACSShellElement::setTemperature,
+   src/elements/shell/TACSShellElement.h:76).  Shear correction 5/6 and
+   drilling regularisation 10 as in TACSIsoShellConstitutive /
+   TACSShellConstitutive (src/constitutive/TACSShellConstitutive.cpp:59). */
+int a2ds_mesh_set_material(a2ds_mesh mesh, double E, double nu, double alpha,
+                           double temperature);
+
+/* Thickness design variables: one TACSIsoShellConstitutive per group
+   (src/constitutive/TACSIsoShellConstitutive.cpp:28-43, design variable
+   tNum); elem_group[e] in [0, num_groups).  Default: one group, t = 1e-2. */
+int a2ds_mesh_set_thickness(a2ds_mesh mesh, int num_groups, const double *t,
+                            const int *elem_group);
+
+/* Dirichlet conditions: TACSAssembler::addBCs(1, &node, nbcs, vars, vals)
+   per entry (src/TACSAssembler.h:104); mask bit k fixes DOF k; vals is
+   num_bcs x 6 (entries whose bit is clear are ignored).  May be NULL. */
+int a2ds_mesh_add_bcs(a2ds_mesh mesh, int num_bcs, const int *nodes,
+                      const int *masks, const double *vals);
+
+/* Host-only half of a2ds_mesh_initialize (no GPU needed): the node-to-node
+   pattern, the matrix ordering of createSchurMat(order_type), the BCSR
+   pattern, the element-slot map and element colours.  After it,
+   a2ds_mesh_get_ordering / get_pattern / ilu_pattern can be queried. */
+int a2ds_mesh_plan(a2ds_mesh mesh, int order_type);
+
+/* The BCSR pattern of every matrix of this mesh (rows in the matrix
+   ordering): sizes first with rowp = cols = NULL. */
+int a2ds_mesh_get_pattern(a2ds_mesh mesh, int *nnzb, int *rowp, int *cols);
+
+/* The ILU(lev_fill) pattern of that matrix, as BCSRMat(comm, mat, levFill,
+   fill) builds it (BCSRMat::computeILUk, src/bpmat/BCSRMat.cpp:625-754). */
+int a2ds_mesh_ilu_pattern(a2ds_mesh mesh, int lev_fill, int *nnzb, int *rowp, int *cols);
+
+/* TACSAssembler::initialize (src/TACSAssembler.cpp:2459) plus the matrix
+   ordering of createSchurMat(order_type) (src/TACSAssembler.cpp:3453):
+   builds the node-to-node pattern, the ordering, the element-slot map and
+   uploads everything.  order_type: A2DS_NATURAL_ORDER or
+   A2DS_TACS_AMD_ORDER. */
+int a2ds_mesh_initialize(a2ds_mesh mesh, int order_type);
+
+/* perm[i] = node in row i of every matrix of this mesh (the reference's
+   schurBIndices / b_map, src/TACSAssembler.cpp:3593-3600). */
+int a2ds_mesh_get_ordering(a2ds_mesh mesh, int *perm);
+
+/* TACSAssembler::computeLocalNodeToNodeCSR(&rowp, &cols, nodiag)
+   (src/TACSAssembler.cpp:1839): rowp[num_nodes+1]; pass cols = NULL to get
+   the size in *nnz first. */
+int a2ds_mesh_node_csr(a2ds_mesh mesh, int nodiag, int *nnz, int *rowp, int *cols);
+
+/* ------------------------------------------------------------ matrices
+   Replaces TACSAssembler::createSchurMat (src/TACSAssembler.cpp:3453) with a
+   single-GPU BCSR matrix in the mesh ordering. */
+int a2ds_bcsr_create(a2ds_mesh mesh, a2ds_bcsr *out);
+int a2ds_bcsr_destroy(a2ds_bcsr mat);
+
+/* BCSRMat::getArrays (src/bpmat/BCSRMat.h:82): sizes first (pointers may be
+   NULL), then rowp[nrows+1], cols[nnzb], vals[36*nnzb]. */
+int a2ds_bcsr_get(a2ds_bcsr mat, int *nrows, int *nnzb, int *rowp, int *cols,
+                  double *vals);
+
+/* Overwrite the values (36*nnzb, the layout a2ds_bcsr_get returns). */
+int a2ds_bcsr_set_values(a2ds_bcsr mat, const double *vals);
+
+/* TACSAssembler::assembleMatType(matType, A) (src/TACSAssembler.cpp:4186)
+   at the element state vars (num_nodes x 6, NULL = zero), including the
+   row-only Dirichlet treatment of TACSSchurMat::applyBCs
+   (src/bpmat/TACSSchurMat.cpp:662).  For the geometric stiffness vars is the
+   load path (TACSShellElement::getMatType, TACSShellElement.h:675-771). */
+int a2ds_assemble_mat(a2ds_mesh mesh, int mat_type, const double *vars,
+                      a2ds_bcsr A);
+
+/* Same, selecting the scatter strategy (A2DS_SCATTER_*). */
+int a2ds_assemble_mat_ex(a2ds_mesh mesh, int mat_type, const double *vars,
+                         a2ds_bcsr A, int scatter);
+
+/* TACSAssembler::assembleRes (src/TACSAssembler.cpp:4000) at vars (NULL =
+   zero); res is num_nodes x 6, BC DOFs set to vars - bcval as in
+   TACSBVec::applyBCs / the assembler's BC residual. */
+int a2ds_assemble_res(a2ds_mesh mesh, const double *vars, double *res);
+
+/* TACSAssembler::assembleJacobian(1, 0, 0, res, A) (src/TACSAssembler.cpp:
+   4084): the tangent and residual at vars in one pass (res may be NULL). */
+int a2ds_assemble_jacobian(a2ds_mesh mesh, const double *vars, double *res,
+                           a2ds_bcsr A);
+
+/* BCSRMat::mult / TACSSchurMat::mult (src/bpmat/BCSRMat.cpp:1212,
+   TACSSchurMat.cpp:866): y = A x, x and y num_nodes x 6 in node order. */
+int a2ds_bcsr_mult(a2ds_bcsr A, const double *x, double *y);
+
+/* y = A x with both vectors already in the matrix (row) ordering. */
+int a2ds_bcsr_mult_rows(a2ds_bcsr A, const double *x, double *y);
+
+/* BCSRMat::copyValues (src/bpmat/BCSRMat.cpp:2375): Y <- X;
+   BCSRMat::axpy (:2430): Y <- Y + alpha X; same pattern required. */
+int a2ds_bcsr_copy(a2ds_bcsr Y, a2ds_bcsr X);
+int a2ds_bcsr_axpy(a2ds_bcsr Y, double alpha, a2ds_bcsr X);
+
+/* TACSSchurMat::applyBCs (src/bpmat/TACSSchurMat.cpp:662-700) with the
+   mesh's Dirichlet set: zero BC rows, identity on the diagonal. */
+int a2ds_bcsr_apply_bcs(a2ds_bcsr A);
+
+/* ------------------------------------------------ factorization (ILU(k))
+   Replaces TACSSchurPc(kmat, levFill, fill, 1) (src/bpmat/TACSSchurMat.cpp:
+   944): symbolic ILU(levFill) of A's pattern (BCSRMat::computeILUk,
+   src/bpmat/BCSRMat.cpp:625); levFill >= num_nodes gives the complete LU.
+   precision: 64 (FP64 factor) or 32 (FP32 factor). */
+int a2ds_pc_create(a2ds_bcsr A, int lev_fill, int precision, a2ds_pc *out);
+int a2ds_pc_destroy(a2ds_pc pc);
+
+/* TACSSchurPc::factor (src/bpmat/TACSSchurMat.cpp:1430) of the current
+   values of the matrix given at creation (or of `from`, same pattern, when
+   not NULL). */
+int a2ds_pc_factor(a2ds_pc pc, a2ds_bcsr from);
+
+/* TACSSchurPc::applyFactor (src/bpmat/TACSSchurMat.cpp:1549): y = (LU)^-1 x,
+   node-ordered num_nodes x 6 host vectors. */
+int a2ds_pc_apply(a2ds_pc pc, const double *x, double *y);
+
+/* BCSRMat::getArrays on the factor: the ILU(k) pattern (bit-exact with the
+   reference's) and the factored values (diagonal blocks stored inverted,
+   as BCSRMatFactor6 leaves them). */
+int a2ds_pc_get(a2ds_pc pc, int *nrows, int *nnzb, int *rowp, int *cols,
+                double *vals);
+
+/* --------------------------------------------------------- buckling solve */
+typedef struct {
+  double sigma;          /* spectral shift (TACSLinearBuckling ctor) */
+  int max_lanczos;       /* maximum Lanczos vectors */
+  int num_eigvals;       /* eigenvalues wanted (lowest magnitude) */
+  double eig_tol;        /* relative eigenvalue residual tolerance */
+  int lev_fill;          /* ILU level of fill for the preconditioner */
+  int gmres_m;           /* GMRES subspace size */
+  int gmres_restarts;    /* GMRES restarts */
+  double gmres_rtol;     /* GMRES relative tolerance */
+  double gmres_atol;     /* GMRES absolute tolerance */
+  int precision;         /* 64: all-FP64; 32: FP32 factor + FP64 GMRES-IR */
+  int seed;              /* Lanczos start vector seed */
+} a2ds_buckling_opts;
+
+/* Fills opts with the defaults (sigma = 0, 100 vectors, 10 eigenvalues,
+   tol 1e-10, complete LU, GMRES(30, 15) at 1e-12, FP64). */
+void a2ds_buckling_default_opts(a2ds_buckling_opts *opts);
+
+/* TACSLinearBuckling::solve(rhs, NULL) (src/TACSBuckling.cpp:197-278) and
+   extractEigenvector (:288): K at zero state, load path K u = rhs,
+   G at u, shift-invert Lanczos for the num_eigvals buckling loads lambda of
+   K x + lambda G x = 0 with the smallest magnitude.  Outputs (host):
+   eigvals[num_eigvals], errors[num_eigvals] (||K x + lambda G x|| / ||K x||),
+   eigvecs (num_eigvals x num_nodes x 6, may be NULL), path (num_nodes x 6,
+   may be NULL). */
+int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts,
+                        const double *rhs, double *eigvals, double *errors,
+                        double *eigvecs, double *path);
+
+/* Timings and counters of the last a2ds_buckling_solve on this mesh:
+   fills up to n doubles {total_s, assemble_k_s, assemble_g_s, factor_s,
+   path_s, lanczos_s, lanczos_iters, inner_iters, kernel_launches}. */
+int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out);
+
+/* ---------------------------------------------- eigenvalue sensitivities
+   The derivative of buckling load lambda_n with respect to each thickness
+   group, dlambda/dt_g = -phi^T (dK/dt_g + lambda dG/dt_g) phi / (phi^T G phi)
+   plus the load-path adjoint term (the formula documented at
+   src/TACSBuckling.cpp:359-382; the reference's evalEigenDVSens body is
+   commented out).  Needs a preceding a2ds_buckling_solve on this mesh. */
+int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,72 @@
+"""Host-side integer artefacts against the reference's own arrays (bit-exact).
+
+No GPU is needed: a2ds_mesh_plan builds the node-to-node pattern, the AMD
+ordering, the BCSR pattern and the ILU(k) pattern on the host.  The expected
+arrays come from the reference (tests/golden/cyl_*.npz):
+computeLocalNodeToNodeCSR, amd_order_interface, the TACSSchurMat B pattern
+and BCSRMat(comm, B, levFill, fill).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from a2ds import capi
+
+CASES = ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu"]
+
+
+def test_library_exports_every_declared_symbol():
+    lib = capi.load()
+    header = open(os.path.join(os.path.dirname(GOLDEN), "..", "include", "a2ds.h")).read()
+    import re
+    declared = set(re.findall(r"\b(a2ds_[a-z_0-9]+)\s*\(", header))
+    assert declared, "no declarations found"
+    for name in sorted(declared):
+        assert hasattr(lib, name), f"{name} declared in include/a2ds.h but not exported"
+    assert set(capi.EXPORTS) == declared
+
+
+def _planned(f, order):
+    a = capi.Assembler(f["X"], f["conn"])
+    a.add_bcs(f["bc_nodes"], f["bc_mask"], f["bc_vals"])
+    a.plan(order)
+    return a
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_node_csr_matches_reference(case):
+    f = np.load(os.path.join(GOLDEN, case + ".npz"))
+    a = capi.Assembler(f["X"], f["conn"])
+    rowp, cols = a.node_csr(nodiag=False)
+    assert np.array_equal(rowp, f["csr_rowp"])
+    assert np.array_equal(cols, f["csr_cols"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_amd_ordering_and_patterns_match_reference(case):
+    f = np.load(os.path.join(GOLDEN, case + ".npz"))
+    a = _planned(f, capi.A2DS_TACS_AMD_ORDER)
+    assert np.array_equal(a.get_ordering(), f["amd_perm"])
+    rowp, cols = a.get_pattern()
+    assert np.array_equal(rowp, f["bcsr_rowp"])
+    assert np.array_equal(cols, f["bcsr_cols"])
+    frowp, fcols = a.ilu_pattern(int(f["lev"]))
+    assert np.array_equal(frowp, f["ilu_rowp"])
+    assert np.array_equal(fcols, f["ilu_cols"])
+
+
+def test_natural_ordering_is_identity():
+    f = np.load(os.path.join(GOLDEN, CASES[0] + ".npz"))
+    a = _planned(f, capi.A2DS_NATURAL_ORDER)
+    assert np.array_equal(a.get_ordering(), np.arange(f["X"].shape[0]))
+
+
+def test_bad_inputs_are_rejected():
+    X = np.zeros((4, 3))
+    with pytest.raises(capi.A2dsError):
+        capi.Assembler(X, np.array([[0, 1, 2, 7]]))      # node out of range
+    with pytest.raises(capi.A2dsError):
+        capi.Assembler(X, np.array([[0, 1, 2]]))         # 3-node element
