@@ -294,3 +294,85 @@ class BCSRMat:
                 c = perm[cols[jp]]
                 A[6 * r:6 * r + 6, 6 * c:6 * c + 6] = vals[jp]
         return A
+
+
+class SchurPc:
+    """TACSSchurPc(mat, levFill, fill) on one GPU: block ILU(levFill)
+    (levFill >= num_nodes gives the complete LU), FP64 or FP32 factor."""
+
+    def __init__(self, A: BCSRMat, lev_fill: int, precision: int = 64):
+        self.A = A
+        self.lib = A.lib
+        h = VP()
+        _check(self.lib.a2ds_pc_create(A.h, int(lev_fill), int(precision), ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.a2ds_pc_destroy(self.h)
+            self.h = None
+
+    def factor(self, other: BCSRMat = None):
+        _check(self.lib.a2ds_pc_factor(self.h, other.h if other is not None else None))
+
+    def apply_factor(self, x):
+        x = _f64(x).reshape(-1, 6)
+        y = np.zeros_like(x)
+        _check(self.lib.a2ds_pc_apply(self.h, _d(x), _d(y)))
+        return y
+
+    def get_arrays(self):
+        nr, nz = ctypes.c_int(), ctypes.c_int()
+        _check(self.lib.a2ds_pc_get(self.h, ctypes.byref(nr), ctypes.byref(nz), None, None, None))
+        rowp = np.zeros(nr.value + 1, np.int32)
+        cols = np.zeros(nz.value, np.int32)
+        vals = np.zeros((nz.value, 6, 6))
+        _check(self.lib.a2ds_pc_get(self.h, None, None, _i(rowp), _i(cols), _d(vals)))
+        return rowp, cols, vals
+
+
+STAT_NAMES = ["total_s", "assemble_k_s", "assemble_g_s", "factor_s", "path_s", "lanczos_s",
+              "lanczos_iters", "inner_iters", "kernel_launches"]
+
+
+class LinearBuckling:
+    """TACSLinearBuckling(assembler, sigma, ..., max_lanczos, num_eigvals,
+    eig_tol): solve(rhs) then extract_eigenvalue / extract_eigenvector."""
+
+    def __init__(self, assembler: Assembler, sigma, max_lanczos=100, num_eigvals=10,
+                 eig_tol=1e-10, lev_fill=1000000, precision=64, seed=0):
+        self.a = assembler
+        self.lib = assembler.lib
+        o = BucklingOpts()
+        self.lib.a2ds_buckling_default_opts(ctypes.byref(o))
+        o.sigma, o.max_lanczos, o.num_eigvals, o.eig_tol = sigma, max_lanczos, num_eigvals, eig_tol
+        o.lev_fill, o.precision, o.seed = lev_fill, precision, seed
+        self.opts = o
+        self.eigvals = self.errors = self.eigvecs = self.path = None
+
+    def solve(self, rhs=None, want_vectors=True):
+        n, k = self.a.num_nodes, self.opts.num_eigvals
+        rhs = _f64(rhs)
+        lam, err = np.zeros(k), np.zeros(k)
+        vecs = np.zeros((k, n, 6)) if want_vectors else None
+        path = np.zeros((n, 6))
+        _check(self.lib.a2ds_buckling_solve(self.a.h, ctypes.byref(self.opts), _d(rhs), _d(lam),
+                                            _d(err), _d(vecs), _d(path)))
+        self.eigvals, self.errors, self.eigvecs, self.path = lam, err, vecs, path
+        return lam
+
+    def stats(self):
+        out = np.zeros(len(STAT_NAMES))
+        _check(self.lib.a2ds_buckling_stats(self.a.h, out.size, _d(out)))
+        return dict(zip(STAT_NAMES, out.tolist()))
+
+    def extract_eigenvalue(self, n):
+        return self.eigvals[n], self.errors[n]
+
+    def extract_eigenvector(self, n):
+        return self.eigvals[n], self.eigvecs[n], self.errors[n]
+
+    def eig_sens_thickness(self, n, num_groups):
+        out = np.zeros(num_groups)
+        _check(self.lib.a2ds_eig_sens_thickness(self.a.h, int(n), _d(out)))
+        return out
