@@ -332,7 +332,9 @@ class SchurPc:
 
 
 STAT_NAMES = ["total_s", "assemble_k_s", "assemble_g_s", "factor_s", "path_s", "lanczos_s",
-              "lanczos_iters", "inner_iters", "kernel_launches"]
+              "lanczos_iters", "inner_iters", "kernel_launches", "solve_event_ms",
+              "factor_a_event_ms", "factor_k_event_ms", "factor_nnzb", "factor_levels",
+              "factor_flops"]
 
 
 class LinearBuckling:
@@ -356,9 +358,11 @@ class LinearBuckling:
         lam, err = np.zeros(k), np.zeros(k)
         vecs = np.zeros((k, n, 6)) if want_vectors else None
         path = np.zeros((n, 6))
-        _check(self.lib.a2ds_buckling_solve(self.a.h, ctypes.byref(self.opts), _d(rhs), _d(lam),
-                                            _d(err), _d(vecs), _d(path)))
+        rc = self.lib.a2ds_buckling_solve(self.a.h, ctypes.byref(self.opts), _d(rhs), _d(lam),
+                                          _d(err), _d(vecs), _d(path))
+        # on A2DS_ERR_NOCONV the current Ritz pairs are still returned
         self.eigvals, self.errors, self.eigvecs, self.path = lam, err, vecs, path
+        _check(rc)
         return lam
 
     def stats(self):

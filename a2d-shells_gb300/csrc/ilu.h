@@ -14,27 +14,6 @@ struct LevelSchedule {
   DBuf<int> d_rows;
 };
 
-void build_levels(int n, const std::vector<int> &frowp, const std::vector<int> &fcols,
-                  const std::vector<int> &fdiag, bool upper, LevelSchedule &L);
-
-// F <- pattern-embedded copy of A (+ alpha2 * A2 when A2 != NULL), as T.
-template <typename T>
-int factor_scatter(int n, const int *rowp, const int *cols, const double *A, const double *A2,
-                   double alpha2, const int *frowp, const int *fcols, T *F, cudaStream_t s);
-
-// In-place numeric factorization of F (levels of the L pattern).  *status
-// receives max(row+1) of any singular diagonal block (0 = none).
-template <typename T>
-int factor_levels(const LevelSchedule &L, const int *frowp, const int *fcols, const int *fdiag,
-                  T *F, int *status, cudaStream_t s, long long *launches);
-
-// y = (LU)^{-1} x for nrhs right-hand sides, layout (row, dof, rhs); y may
-// alias x.
-template <typename T, typename TV>
-int solve_levels(const LevelSchedule &Lo, const LevelSchedule &Up, const int *frowp,
-                 const int *fcols, const int *fdiag, const T *F, const TV *x, TV *y, int nrhs,
-                 cudaStream_t s, long long *launches);
-
 // A factorization handle (the TACSSchurPc role on one GPU).
 struct Factor {
   int n = 0, lev_fill = 0, precision = 64;
@@ -42,9 +21,46 @@ struct Factor {
   DBuf<int> d_frowp, d_fcols, d_fdiag, d_status;
   DBuf<double> F64;
   DBuf<float> F32;
-  LevelSchedule lower, upper;
+  LevelSchedule flv;           // dependency levels of all rows (factorization)
+  LevelSchedule lower, upper;  // head rows [0, tail_s): row-oriented solves
+  // right-looking update tasks, grouped by level
+  std::vector<int> task_level_ptr, task_row, task_ptr, task_jp;
+  DBuf<int> d_task_row, d_task_ptr, d_task_jp;
+  // dense tail rows [tail_s, n): head pull split and column push lists
+  int tail_s = 0;
+  std::vector<int> lsplit, tl_ptr, tl_row, tl_pos, tl_col, tu_ptr, tu_row, tu_pos, tu_col;
+  DBuf<int> d_lsplit, d_tl_row, d_tl_pos, d_tl_col, d_tu_row, d_tu_pos, d_tu_col;
+  // algorithmic FP operations of one numeric factorization: 432 per L block
+  // (L_ij = A_ij D_j^{-1}), 432 per block update, 432 per diagonal inverse
+  double flop_count = 0.0;
   long long nnzb() const { return frowp.empty() ? 0 : frowp.back(); }
+  double flops() const { return flop_count; }
 };
+
+void build_levels(int n, const std::vector<int> &frowp, const std::vector<int> &fcols,
+                  const std::vector<int> &fdiag, bool upper, LevelSchedule &L,
+                  std::vector<int> *level_of = nullptr);
+void build_update_tasks(Factor &f, const std::vector<int> &lev);
+// Split rows into the head (row-oriented level solves) and the dense tail
+// (column-oriented pushes) and build both schedules; lev = factor levels.
+void build_solve_schedule(Factor &f, const std::vector<int> &lev, int narrow);
+int upload_schedules(Factor &f, cudaStream_t s);
+
+// F <- pattern-embedded copy of A (+ alpha2 * A2 when A2 != NULL), as T.
+template <typename T>
+int factor_scatter(int n, const int *rowp, const int *cols, const double *A, const double *A2,
+                   double alpha2, const int *frowp, const int *fcols, T *F, cudaStream_t s);
+
+// In-place numeric factorization of F.  *status receives max(row+1) of any
+// singular diagonal block (0 = none).
+template <typename T>
+int factor_levels(const Factor &f, T *F, int *status, cudaStream_t s, long long *launches);
+
+// y = (LU)^{-1} x for nrhs right-hand sides, layout (row, dof, rhs); y may
+// alias x.
+template <typename T, typename TV>
+int solve_levels(const Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
+                 long long *launches);
 
 struct Mesh;
 int factor_setup(Mesh &m, int lev_fill, int precision, Factor &f);

@@ -152,13 +152,14 @@ int factor_setup(Mesh &m, int lev_fill, int precision, Factor &f) {
   f.precision = precision;
   if ((rc = ilu_symbolic(m.nn, m.rowp, m.cols, lev_fill, f.frowp, f.fcols, f.fdiag)))
     return fail(A2DS_ERR_STATE, "symbolic factorization failed");
-  build_levels(m.nn, f.frowp, f.fcols, f.fdiag, false, f.lower);
-  build_levels(m.nn, f.frowp, f.fcols, f.fdiag, true, f.upper);
+  std::vector<int> lev;
+  build_levels(m.nn, f.frowp, f.fcols, f.fdiag, false, f.flv, &lev);
+  build_update_tasks(f, lev);
+  build_solve_schedule(f, lev, 48);
+  if ((rc = upload_schedules(f, m.stream))) return rc;
   if ((rc = f.d_frowp.upload(f.frowp.data(), f.frowp.size(), m.stream))) return rc;
   if ((rc = f.d_fcols.upload(f.fcols.data(), f.fcols.size(), m.stream))) return rc;
   if ((rc = f.d_fdiag.upload(f.fdiag.data(), f.fdiag.size(), m.stream))) return rc;
-  if ((rc = f.lower.d_rows.upload(f.lower.rows.data(), f.lower.rows.size(), m.stream))) return rc;
-  if ((rc = f.upper.d_rows.upload(f.upper.rows.data(), f.upper.rows.size(), m.stream))) return rc;
   if ((rc = f.d_status.alloc(1))) return rc;
   if (precision == 32) {
     if ((rc = f.F32.alloc((size_t)f.nnzb() * 36))) return rc;
@@ -177,15 +178,13 @@ int factor_numeric(Mesh &m, Factor &f, const double *A, const double *A2, double
                                     f.d_fcols.p, f.F32.p, m.stream)))
       return rc;
     m.launches++;
-    return factor_levels<float>(f.lower, f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, f.F32.p,
-                                f.d_status.p, m.stream, &m.launches);
+    return factor_levels<float>(f, f.F32.p, f.d_status.p, m.stream, &m.launches);
   }
   if ((rc = factor_scatter<double>(m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, f.d_frowp.p,
                                    f.d_fcols.p, f.F64.p, m.stream)))
     return rc;
   m.launches++;
-  return factor_levels<double>(f.lower, f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, f.F64.p,
-                               f.d_status.p, m.stream, &m.launches);
+  return factor_levels<double>(f, f.F64.p, f.d_status.p, m.stream, &m.launches);
 }
 
 int factor_check(Mesh &m, Factor &f) {
@@ -206,16 +205,14 @@ static int factor_apply(Mesh &m, Factor &f, const double *x, double *y, DBuf<flo
     if ((rc = w32.alloc(n6))) return rc;
     k_f64_to_f32<<<grid_for(n6), 256, 0, m.stream>>>(w32.p, x, n6);
     m.launches++;
-    if ((rc = solve_levels<float, float>(f.lower, f.upper, f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p,
-                                         f.F32.p, w32.p, w32.p, 1, m.stream, &m.launches)))
+    if ((rc = solve_levels<float, float>(f, f.F32.p, w32.p, w32.p, 1, m.stream, &m.launches)))
       return rc;
     A2DS_CUDA_TRY(cudaMemsetAsync(y, 0, n6 * sizeof(double), m.stream));
     k_add_f32<<<grid_for(n6), 256, 0, m.stream>>>(y, w32.p, n6);
     m.launches++;
     return 0;
   }
-  return solve_levels<double, double>(f.lower, f.upper, f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p,
-                                      f.F64.p, x, y, 1, m.stream, &m.launches);
+  return solve_levels<double, double>(f, f.F64.p, x, y, 1, m.stream, &m.launches);
 }
 
 // ------------------------------------------------- small dense eigensolver
@@ -274,6 +271,14 @@ struct BucklingState {
   int niters = 0, nconv = 0;
   double sigma = 0.0;
   int lev_fill = -1, precision = 0;
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  BucklingState() {
+    for (auto &e : ev) cudaEventCreate(&e);
+  }
+  ~BucklingState() {
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
 };
 
 void release_solver(Mesh &m) {
@@ -441,6 +446,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   B.launches = &m.launches;
 
   // 1. K at the zero state
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[0], m.stream));
   double ta = now();
   if ((rc = m.assemble_device(MODE_K, nullptr, S.K.p, nullptr, A2DS_SCATTER_ATOMIC))) return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
@@ -448,7 +454,9 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
 
   // 2. load path: res = R(0) - f (BC rows: 0 - bcval), path = -K^{-1} res
   ta = now();
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[4], m.stream));
   if ((rc = factor_numeric(m, S.fk, S.K.p, nullptr, 0.0))) return rc;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[5], m.stream));
   if ((rc = factor_check(m, S.fk))) return rc;
   double t_fk = now() - ta;
   ta = now();
@@ -489,7 +497,9 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
                                  (int)m.bc_rows.size(), m.stream)))
     return rc;
   m.launches += 2;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[2], m.stream));
   if ((rc = factor_numeric(m, S.fa, S.Aux.p, nullptr, 0.0))) return rc;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[3], m.stream));
   if ((rc = factor_check(m, S.fa))) return rc;
   double t_fa = now() - ta;
 
@@ -534,7 +544,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     double *qi = S.Q.p + (size_t)i * n6, *kqi = S.KQ.p + (size_t)i * n6;
     double *w = S.Q.p + (size_t)(i + 1) * n6, *kw = S.KQ.p + (size_t)(i + 1) * n6;
     // w = A^{-1} K q_i
-    if ((rc = refined_solve(m, S.fa, S.Aux.p, nullptr, 0.0, kqi, w, S, B, 1e-12, 3, &inner)))
+    if ((rc = refined_solve(m, S.fa, S.Aux.p, nullptr, 0.0, kqi, w, S, B, 1e-10, 2, &inner)))
       return rc;
     zero_bc(w);
     // full K-orthogonalisation, two classical Gram-Schmidt passes using K q_j
@@ -619,11 +629,17 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   }
   if (path_out && (rc = m.from_rows(S.path.p, path_out))) return rc;
   S.niters = m_iter;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[1], m.stream));
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   double total = now() - t0;
+  float ms_solve = 0.f, ms_fa = 0.f, ms_fk = 0.f;
+  cudaEventElapsedTime(&ms_solve, S.ev[0], S.ev[1]);
+  cudaEventElapsedTime(&ms_fa, S.ev[2], S.ev[3]);
+  cudaEventElapsedTime(&ms_fk, S.ev[4], S.ev[5]);
   m.stats = {total, t_k, t_g, t_fk + t_fa, t_path, t_lan, (double)m_iter, (double)inner,
-             (double)(m.launches - launches0)};
-  if (!converged) return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos");
+             (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
+             (double)S.fa.nnzb(), (double)S.fa.flv.nlevels, (double)S.fa.flops()};
+  if (!converged) return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
   return 0;
 }
 

@@ -113,3 +113,147 @@ def element_jacobian(order, nonlinear, mat: Material, X, vars_, alpha=1.0):
     lib.orc_add_jacobian(order, int(nonlinear), ctypes.byref(mat), alpha, _p(X), _p(v),
                          _p(res), _p(J))
     return res, J
+
+
+# ------------------------------------------------------------- solve path
+def _declare_solver(lib):
+    lib.orc_assemble.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 ctypes.POINTER(Material), ctypes.c_int, ctypes.c_int, PI, PI,
+                                 P, P, P, PI, PI, PI, P]
+    lib.orc_apply_bcs.argtypes = [PI, PI, P, ctypes.c_int, PI, PI]
+    lib.orc_spmv.argtypes = [ctypes.c_int, PI, PI, P, P, P]
+    lib.orc_factor_fill.argtypes = [ctypes.c_int, PI, PI, P, PI, PI, P]
+    lib.orc_factor.argtypes = [ctypes.c_int, PI, PI, PI, P]
+    lib.orc_factor.restype = ctypes.c_int
+    lib.orc_apply_factor.argtypes = [ctypes.c_int, PI, PI, PI, P, P, P]
+    lib.orc_gmres.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                              ctypes.c_double, P, P]
+    lib.orc_gmres.restype = ctypes.c_int
+    lib.orc_lanczos.argtypes = [ctypes.c_void_p, ctypes.c_int, PI, PI, P, ctypes.c_double,
+                                ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                ctypes.c_int, PI, PI, ctypes.c_uint, ctypes.c_int, P]
+    lib.orc_lanczos.restype = ctypes.c_int
+
+
+class _System(ctypes.Structure):
+    """orc_system (oracle/c/solver_oracle.c)"""
+    _fields_ = [("n", ctypes.c_int), ("rowp", PI), ("cols", PI), ("A", P),
+                ("frowp", PI), ("fcols", PI), ("fdiag", PI), ("F", P)]
+
+
+def _pi(a):
+    return a.ctypes.data_as(PI)
+
+
+def assemble(mesh, kind, perm, rowp, cols, vars_=None, nonlinear=False, bc_rows=None,
+             bc_masks=None):
+    """TACSAssembler::assembleMatType on the CPU: BCSR values in the matrix
+    ordering given by perm (row i <-> node perm[i]) and pattern rowp/cols."""
+    lib = load()
+    _declare_solver(lib)
+    n = perm.size
+    iperm = np.empty(n, np.int32)
+    iperm[perm] = np.arange(n, dtype=np.int32)
+    conn = np.ascontiguousarray(mesh.conn, np.int32)
+    conn_rows = np.ascontiguousarray(iperm[conn], np.int32)
+    X = np.ascontiguousarray(mesh.X, np.float64)
+    v = None if vars_ is None else np.ascontiguousarray(vars_, np.float64)
+    tv = np.ascontiguousarray(np.unique(mesh.thickness) if False else mesh.thickness, np.float64)
+    tg = np.arange(mesh.num_elements, dtype=np.int32)
+    rowp = np.ascontiguousarray(rowp, np.int32)
+    cols = np.ascontiguousarray(cols, np.int32)
+    vals = np.zeros((cols.size, 6, 6))
+    m = Material.iso(mesh.E, mesh.nu, 1.0)
+    lib.orc_assemble(mesh.order, int(nonlinear), kind, ctypes.byref(m), n, mesh.num_elements,
+                     _pi(conn), _pi(conn_rows), _p(X), None if v is None else _p(v), _p(tv),
+                     _pi(tg), _pi(rowp), _pi(cols), _p(vals))
+    if bc_rows is not None and len(bc_rows):
+        br = np.ascontiguousarray(bc_rows, np.int32)
+        bm = np.ascontiguousarray(bc_masks, np.int32)
+        lib.orc_apply_bcs(_pi(rowp), _pi(cols), _p(vals), br.size, _pi(br), _pi(bm))
+    return vals
+
+
+def factor(rowp, cols, vals, frowp, fcols, fdiag):
+    """BCSRMatFactor6 on the CPU (diagonal blocks inverted in place)."""
+    lib = load()
+    _declare_solver(lib)
+    n = rowp.size - 1
+    F = np.zeros((fcols.size, 6, 6))
+    args = [np.ascontiguousarray(a, np.int32) for a in (rowp, cols, frowp, fcols, fdiag)]
+    lib.orc_factor_fill(n, _pi(args[0]), _pi(args[1]), _p(np.ascontiguousarray(vals)),
+                        _pi(args[2]), _pi(args[3]), _p(F))
+    rc = lib.orc_factor(n, _pi(args[2]), _pi(args[3]), _pi(args[4]), _p(F))
+    if rc:
+        raise RuntimeError(f"singular diagonal block in row {rc - 1}")
+    return F
+
+
+class CpuBuckling:
+    """The reference's buckling path on the CPU (TACSLinearBuckling::solve
+    with a TACSSchurPc factor of K and GMRES on K + sigma G), timed phase by
+    phase.  Pattern, ordering and factor pattern are inputs (integer host
+    work, checked bit-exact against the reference separately)."""
+
+    def __init__(self, mesh, perm, rowp, cols, frowp, fcols, fdiag, bc_rows, bc_masks):
+        self.mesh, self.perm = mesh, np.ascontiguousarray(perm, np.int32)
+        self.rowp, self.cols = np.ascontiguousarray(rowp, np.int32), np.ascontiguousarray(cols, np.int32)
+        self.frowp, self.fcols = np.ascontiguousarray(frowp, np.int32), np.ascontiguousarray(fcols, np.int32)
+        self.fdiag = np.ascontiguousarray(fdiag, np.int32)
+        self.bc_rows = np.ascontiguousarray(bc_rows, np.int32)
+        self.bc_masks = np.ascontiguousarray(bc_masks, np.int32)
+        self.times = {}
+
+    def _to_rows(self, v):
+        return np.ascontiguousarray(np.asarray(v).reshape(-1, 6)[self.perm]).ravel()
+
+    def _from_rows(self, v):
+        out = np.empty_like(v.reshape(-1, 6))
+        out[self.perm] = v.reshape(-1, 6)
+        return out
+
+    def solve(self, sigma, rhs, lanczos_iters=10, num_eig=10, gm_m=10, gm_restarts=15,
+              gm_tol=1e-12, seed=0):
+        import time
+        lib = load()
+        _declare_solver(lib)
+        n = self.rowp.size - 1
+        t = self.times
+        t0 = time.perf_counter()
+        K = assemble(self.mesh, STIFFNESS, self.perm, self.rowp, self.cols, None, False,
+                     self.bc_rows, self.bc_masks)
+        t["assemble_k"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        F = factor(self.rowp, self.cols, K, self.frowp, self.fcols, self.fdiag)
+        t["factor"] = time.perf_counter() - t0
+        # load path: GMRES on K (aux = K at this point), pc = factor of K
+        t0 = time.perf_counter()
+        b = self._to_rows(rhs)
+        for r, mk in zip(self.bc_rows, self.bc_masks):
+            for k in range(6):
+                if mk >> k & 1:
+                    b[6 * r + k] = 0.0
+        path = np.zeros_like(b)
+        sysK = _System(n, _pi(self.rowp), _pi(self.cols), _p(K), _pi(self.frowp),
+                       _pi(self.fcols), _pi(self.fdiag), _p(F))
+        lib.orc_gmres(ctypes.byref(sysK), gm_m, gm_restarts, gm_tol, gm_tol, _p(b), _p(path))
+        t["path"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        G = assemble(self.mesh, GEOMETRIC, self.perm, self.rowp, self.cols,
+                     self._from_rows(path), False, self.bc_rows, self.bc_masks)
+        t["assemble_g"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        A = np.ascontiguousarray(K + sigma * G)
+        lib.orc_apply_bcs(_pi(self.rowp), _pi(self.cols), _p(A), self.bc_rows.size,
+                          _pi(self.bc_rows), _pi(self.bc_masks))
+        sysA = _System(n, _pi(self.rowp), _pi(self.cols), _p(A), _pi(self.frowp),
+                       _pi(self.fcols), _pi(self.fdiag), _p(F))
+        lam = np.zeros(num_eig)
+        gm = lib.orc_lanczos(ctypes.byref(sysA), n, _pi(self.rowp), _pi(self.cols), _p(K),
+                             sigma, lanczos_iters, gm_m, gm_restarts, gm_tol, self.bc_rows.size,
+                             _pi(self.bc_rows), _pi(self.bc_masks), seed, num_eig, _p(lam))
+        t["lanczos"] = time.perf_counter() - t0
+        t["gmres_iters"] = gm
+        self.path = self._from_rows(path)
+        self.eigvals = lam
+        return lam

@@ -92,3 +92,30 @@ def dense_buckling(K, G, bc_nodes, bc_mask):
     mu = sla.eigh(-Gf, Kf, eigvals_only=True)
     lam = 1.0 / mu[mu != 0]
     return lam[np.argsort(np.abs(lam))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64])
+def test_factor_solve_residual_mid_size(precision):
+    """A 24x48 cylinder: wide head levels (row-oriented solves) and a dense
+    tail (column pushes) are both exercised; K y = x to the factor's
+    precision.  (An FP32 factor of this K is not a usable solve on its own:
+    K's condition number, ~1e11 with the unit Dirichlet rows, is far beyond
+    1/eps_32; FP32 factors are only used inside FP64 refinement.)"""
+    from a2ds import mesh as meshgen
+    m = meshgen.cylinder(24, 48)
+    a = capi.Assembler(m.X, m.conn)
+    a.set_material(m.E, m.nu)
+    a.set_thickness([m.meta["t"]])
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    K = a.create_mat()
+    a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
+    pc = capi.SchurPc(K, 1000000, precision)
+    pc.factor()
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((m.num_nodes, 6))
+    y = pc.apply_factor(x)
+    r = K.mult(y) - x
+    tol = 1e-6 if precision == 64 else 5e-1
+    assert np.linalg.norm(r) / np.linalg.norm(x) < tol
