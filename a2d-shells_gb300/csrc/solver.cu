@@ -170,6 +170,54 @@ int factor_setup(Mesh &m, int lev_fill, int precision, Factor &f) {
   return 0;
 }
 
+// A second factor with the same symbolic pattern (no second symbolic
+// factorization), values in the given precision.
+static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
+  int rc;
+  f.n = src.n;
+  f.lev_fill = src.lev_fill;
+  f.precision = precision;
+  f.frowp = src.frowp;
+  f.fcols = src.fcols;
+  f.fdiag = src.fdiag;
+  f.flv.nlevels = src.flv.nlevels;
+  f.flv.ptr = src.flv.ptr;
+  f.flv.rows = src.flv.rows;
+  f.lower.nlevels = src.lower.nlevels;
+  f.lower.ptr = src.lower.ptr;
+  f.lower.rows = src.lower.rows;
+  f.upper.nlevels = src.upper.nlevels;
+  f.upper.ptr = src.upper.ptr;
+  f.upper.rows = src.upper.rows;
+  f.task_level_ptr = src.task_level_ptr;
+  f.task_row = src.task_row;
+  f.task_ptr = src.task_ptr;
+  f.task_jp = src.task_jp;
+  f.tail_s = src.tail_s;
+  f.lsplit = src.lsplit;
+  f.tl_ptr = src.tl_ptr;
+  f.tl_row = src.tl_row;
+  f.tl_pos = src.tl_pos;
+  f.tl_col = src.tl_col;
+  f.tu_ptr = src.tu_ptr;
+  f.tu_row = src.tu_row;
+  f.tu_pos = src.tu_pos;
+  f.tu_col = src.tu_col;
+  f.flop_count = src.flop_count;
+  if ((rc = upload_schedules(f, m.stream))) return rc;
+  if ((rc = f.d_frowp.upload(f.frowp.data(), f.frowp.size(), m.stream))) return rc;
+  if ((rc = f.d_fcols.upload(f.fcols.data(), f.fcols.size(), m.stream))) return rc;
+  if ((rc = f.d_fdiag.upload(f.fdiag.data(), f.fdiag.size(), m.stream))) return rc;
+  if ((rc = f.d_status.alloc(1))) return rc;
+  if (precision == 32) {
+    if ((rc = f.F32.alloc((size_t)f.nnzb() * 36))) return rc;
+  } else {
+    if ((rc = f.F64.alloc((size_t)f.nnzb() * 36))) return rc;
+  }
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  return 0;
+}
+
 int factor_numeric(Mesh &m, Factor &f, const double *A, const double *A2, double alpha2) {
   int rc;
   A2DS_CUDA_TRY(cudaMemsetAsync(f.d_status.p, 0, sizeof(int), m.stream));
@@ -432,7 +480,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     Sp->lev_fill = opts->lev_fill;
     Sp->precision = opts->precision;
     if ((rc = factor_setup(m, opts->lev_fill, 64, Sp->fk))) return rc;
-    if ((rc = factor_setup(m, opts->lev_fill, opts->precision, Sp->fa))) return rc;
+    if ((rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa))) return rc;
   }
   BucklingState &S = *Sp;
   S.sigma = opts->sigma;

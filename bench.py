@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Buckling-solve benchmark on GB300 (and the CPU reference arm).
+
+Workload (N=1): the 256 x 512 Quad4 MITC cylinder (R = 1 m, L = 2 m,
+t = 2 mm, E = 70 GPa, nu = 0.3, 131 072 elements, 789 504 DOF), one end
+clamped, 1 N/m axial compression at the other, seeded 0.01 t radial
+imperfection; the 10 buckling loads of smallest magnitude by shift-invert
+Lanczos, all-FP64 on the GPU (assembly, complete-LU factor of K and of
+K + sigma G, solves, Lanczos).  Synthetic seeded inputs stand in for a
+dataset (the reference publishes none).
+
+A step is one complete buckling solve (TACSLinearBuckling::solve semantics:
+assemble K, load path, assemble G, factor, Lanczos, eigenpairs) through the
+C ABI call a2ds_buckling_solve:
+  value  -- mesh resident on the device, eigenvalues returned to the host;
+  e2e    -- the same call with host load vector in and host eigenvectors and
+            load path out (the copies inside the timed region).
+Device time comes from CUDA events recorded by the library on its own
+stream around each solve.  The shift sigma is 0.95 x the lowest load found
+by a cheap first solve at 0.35 x the classical load (untimed setup).
+
+--impl reference times the reference's algorithm on the host cores through
+the CPU oracle (oracle/): LU of K, GMRES on K + sigma G, Lanczos with
+K-inner products by SpMV.  A full config solve takes many CPU-minutes, so
+the sample is a complete solve of the 64 x 128 cylinder plus the full-size
+K and G assemblies, scaled to the full size by exact factorization flop and
+factor-size ratios (stated in the JSON line).
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank runs an independent replica on its own GPU
+(replicas only: the solve does not shard); value = all ranks' solves / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "a2d-shells_gb300")
+
+METRIC = ("buckling solves/s on 1 GB300, FP32-IR vs FP64 at <=1e-8 eig err; "
+          "elems/s assembled")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--nx", type=int, default=256)
+    p.add_argument("--ny", type=int, default=512)
+    p.add_argument("--neig", type=int, default=10)
+    p.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def fp64_peak_tflops():
+    """FP64 throughput measured here: a cuBLAS DGEMM through torch."""
+    try:
+        import torch
+        a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        return 2 * 4096 ** 3 / (ms * 1e-3) / 1e12
+    except Exception:
+        return None
+
+
+def build_workload(nx, ny):
+    sys.path.insert(0, PKG)
+    from a2ds import mesh as meshgen
+    return meshgen.cylinder(nx, ny, order=2)
+
+
+def cpu_sample(full_mesh, nx_full, ny_full, neig):
+    """Time the reference algorithm on the host (CPU oracle) and scale it to
+    the full workload.  Returns (solves_per_s, details)."""
+    sys.path.insert(0, PKG)
+    sys.path.insert(0, REPO)
+    import numpy as np
+
+    import oracle
+    from a2ds import capi
+    from a2ds import mesh as meshgen
+
+    def plan(m):
+        a = capi.Assembler(m.X, m.conn)
+        a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+        a.plan(capi.A2DS_TACS_AMD_ORDER)
+        perm = a.get_ordering()
+        rowp, cols = a.get_pattern()
+        return a, perm, rowp, cols
+
+    def fflops(rowp, cols):
+        n = rowp.size - 1
+        diag = np.array([rowp[i] + np.searchsorted(cols[rowp[i]:rowp[i + 1]], i)
+                         for i in range(n)])
+        ucount = rowp[1:] - diag - 1
+        rows = np.repeat(np.arange(n), np.diff(rowp))
+        low = cols < rows
+        return 432.0 * ((1 + ucount[cols[low]]).sum() + n), diag
+
+    threads = os.cpu_count() or 1
+    # full-size assemblies of K and G (the path does not matter for timing)
+    _, perm, rowp, cols = plan(full_mesh)
+    iperm = np.empty_like(perm)
+    iperm[perm] = np.arange(perm.size)
+    br = iperm[full_mesh.bc_nodes].astype(np.int32)
+    t0 = time.perf_counter()
+    oracle.assemble(full_mesh, oracle.STIFFNESS, perm, rowp, cols, None, False, br,
+                    full_mesh.bc_mask)
+    t_k = time.perf_counter() - t0
+    rng = np.random.default_rng(1)
+    pth = 1e-6 * rng.standard_normal((full_mesh.num_nodes, 6))
+    t0 = time.perf_counter()
+    oracle.assemble(full_mesh, oracle.GEOMETRIC, perm, rowp, cols, pth, False, br,
+                    full_mesh.bc_mask)
+    t_g = time.perf_counter() - t0
+    # complete solve of a 64 x 128 cylinder
+    sm = meshgen.cylinder(64, 128, order=2)
+    a, sperm, srowp, scols = plan(sm)
+    fr, fc = a.ilu_pattern(1000000)
+    f_small, sdiag = fflops(fr, fc)
+    siperm = np.empty_like(sperm)
+    siperm[sperm] = np.arange(sperm.size)
+    sbr = siperm[sm.bc_nodes].astype(np.int32)
+    cb = oracle.CpuBuckling(sm, sperm, srowp, scols, fr, fc, sdiag.astype(np.int32), sbr,
+                            sm.bc_mask)
+    lam_cl = meshgen.classical_cylinder_load(sm.E, sm.nu, sm.meta["t"], 1.0)
+    cb.solve(0.35 * lam_cl, sm.rhs, lanczos_iters=neig, num_eig=neig, gm_m=10, gm_restarts=15)
+    ts = dict(cb.times)
+    # scale: factor by exact flop ratio, solves by factor size ratio
+    ffr, ffc = capi.Assembler(full_mesh.X, full_mesh.conn), None
+    ffr.add_bcs(full_mesh.bc_nodes, full_mesh.bc_mask, full_mesh.bc_vals)
+    ffr.plan(capi.A2DS_TACS_AMD_ORDER)
+    Fr, Fc = ffr.ilu_pattern(1000000)
+    f_full, _ = fflops(Fr, Fc)
+    r_flops = f_full / f_small
+    r_nnz = Fc.size / fc.size
+    t_total = (t_k + t_g + ts["factor"] * r_flops + (ts["path"] + ts["lanczos"]) * r_nnz)
+    details = {
+        "cores": threads,
+        "sample": (f"full-size K and G assembly ({full_mesh.num_elements} elements, measured) + "
+                   f"complete reference-algorithm solve of the 64x128 cylinder (LU of K, "
+                   f"GMRES(10,15,1e-12) on K+sigma G, {neig} Lanczos steps: factor "
+                   f"{ts['factor']:.2f}s, path {ts['path']:.2f}s, Lanczos {ts['lanczos']:.2f}s, "
+                   f"{ts['gmres_iters']} GMRES its) scaled by the exact factor-flop ratio "
+                   f"{r_flops:.1f} and factor-size ratio {r_nnz:.1f}"),
+        "assemble_k_s": t_k, "assemble_g_s": t_g, "modeled_solve_s": t_total,
+        "elems_per_s_k": full_mesh.num_elements / t_k,
+    }
+    return 1.0 / t_total, details
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    m = build_workload(args.nx, args.ny)
+    vals = []
+    det = None
+    for _ in range(max(1, min(args.steps, 2))):
+        v, det = cpu_sample(m, args.nx, args.ny, args.neig)
+        vals.append(v)
+    v = sum(vals) / len(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": 0,
+        "steps": len(vals), "warmup": 0, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded cylinder)",
+        "config": workload_config(m, args),
+        "cpu_baseline": {"value": v, "unit": "solves/s", "cores": det["cores"], "kind": "port",
+                         "sample": det["sample"]},
+        "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(m, args):
+    return {
+        "workload": (f"cylinder {args.nx}x{args.ny} Quad4 MITC shell, {6 * m.num_nodes} DOF, "
+                     f"{args.neig} lowest buckling loads, shift-invert Lanczos, complete-LU "
+                     f"factors, FP{args.precision}"),
+        "elements": m.num_elements, "nodes": m.num_nodes, "dof": 6 * m.num_nodes,
+        "num_eigvals": args.neig, "lev_fill": "complete LU (1e6)", "precision": args.precision,
+        "l2": "no flush: every step streams the ~3.5 GB factor and 0.34 GB matrices (> 129 MB L2)",
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args)
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import numpy as np
+
+    sys.path.insert(0, PKG)
+    from a2ds import capi
+    from a2ds import mesh as meshgen
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        tdist.init_process_group("gloo")
+        dist = tdist
+
+    capi.load()
+    m = build_workload(args.nx, args.ny)
+    a = capi.Assembler(m.X, m.conn)
+    a.set_material(m.E, m.nu)
+    a.set_thickness([m.meta["t"]])
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+
+    # shift from a cheap first solve
+    lam_cl = meshgen.classical_cylinder_load(m.E, m.nu, m.meta["t"], 1.0)
+    b0 = capi.LinearBuckling(a, 0.35 * lam_cl, max_lanczos=60, num_eigvals=1, eig_tol=1e-6,
+                             precision=args.precision)
+    try:
+        b0.solve(m.rhs, want_vectors=False)
+    except capi.A2dsError:
+        pass
+    sigma = 0.95 * float(b0.eigvals[0])
+    b = capi.LinearBuckling(a, sigma, max_lanczos=200, num_eigvals=args.neig, eig_tol=1e-8,
+                            precision=args.precision)
+    for _ in range(args.warmup):
+        b.solve(m.rhs, want_vectors=False)
+    ref_lam = b.eigvals.copy()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    barrier()
+    ev_ms, wall, launches, stats = [], [], 0, None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        b.solve(m.rhs, want_vectors=False)
+        wall.append(time.perf_counter() - t0)
+        stats = b.stats()
+        ev_ms.append(stats["solve_event_ms"])
+        launches += int(stats["kernel_launches"])
+    barrier()
+    # e2e: host load vector in, host eigenvectors and path out
+    e2e_wall = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        b.solve(m.rhs, want_vectors=True)
+        e2e_wall.append(time.perf_counter() - t0)
+    barrier()
+    clk = clocks.stop()
+
+    ms = sum(ev_ms) / len(ev_ms)
+    t_rank = sum(ev_ms) / 1000.0
+    t_e2e = sum(e2e_wall)
+    if dist:
+        import torch
+        t = torch.tensor([t_rank, t_e2e], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_rank, t_e2e = float(t[0]), float(t[1])
+    value = world * args.steps / t_rank
+    e2e_value = world * args.steps / t_e2e
+    if rank != 0:
+        return 0
+
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    fp64 = fp64_peak_tflops()
+    # dominant kernel: the numeric factorization of K + sigma G (k_factor_update
+    # with its pivot kernels), FP64-pipe bound; bytes are the factor read and
+    # written once plus the matrix read once.
+    nnzf = stats["factor_nnzb"]
+    fa_ms = stats["factor_a_event_ms"]
+    bytes_factor = nnzf * 36 * 8 * 2 + m.num_nodes * 0  # factor values read + written
+    achieved_gbs = bytes_factor / (fa_ms * 1e-3) / 1e9
+    achieved_tf = stats["factor_flops"] / (fa_ms * 1e-3) / 1e12
+    lam_err = float(np.max(np.abs(b.eigvals - ref_lam) / np.abs(ref_lam)))
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == 64 else "f32+f64",
+        "data": "synthetic (seeded cylinder mesh, loads and imperfection; no dataset)",
+        "config": workload_config(m, args),
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": "solves/s",
+                "h2d_bytes_per_step": int(m.num_nodes * 6 * 8),
+                "d2h_bytes_per_step": int((args.neig * (2 + 6 * m.num_nodes) + 6 * m.num_nodes) * 8)},
+        "roofline": {
+            "kernel": "k_factor_update (+ k_factor_pivot): complete-LU factor of K + sigma G",
+            "bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+            "frac": (achieved_gbs / hbm) if hbm else None, "traffic": None,
+            "fp64_pipe": {"achieved_tflops": achieved_tf, "peak_tflops_measured_dgemm": fp64,
+                          "frac": (achieved_tf / fp64) if fp64 else None,
+                          "flops_per_launch_sequence": stats["factor_flops"]},
+            "note": ("FP64 arithmetic, not HBM, bounds this kernel on GB300 (FP64 ~1/58 of FP32): "
+                     "the HBM fraction is reported for the contract, the FP64-pipe fraction "
+                     "is the meaningful one"),
+        },
+        "phases_s": {k: stats[k] for k in ["assemble_k_s", "assemble_g_s", "factor_s", "path_s",
+                                            "lanczos_s"]},
+        "lanczos_iters": stats["lanczos_iters"],
+        "assembly_elems_per_s": {"K": m.num_elements / stats["assemble_k_s"],
+                                 "G": m.num_elements / stats["assemble_g_s"]},
+        "eigvals": b.eigvals.tolist(), "eig_rel_drift_between_runs": lam_err,
+        "eig_residual_max": float(np.max(b.errors)), "sigma": sigma,
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        try:
+            v, det = cpu_sample(m, args.nx, args.ny, args.neig)
+            line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": det["cores"],
+                                    "kind": "port", "sample": det["sample"],
+                                    "cpu_assembly_elems_per_s_K": det["elems_per_s_k"]}
+        except Exception as ex:  # the GPU number stands on its own
+            line["cpu_baseline"] = {"value": None, "unit": "solves/s", "cores": os.cpu_count(),
+                                    "kind": "port", "sample": f"failed: {ex}"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
