@@ -42,7 +42,7 @@ EXPORTS = [
     "a2ds_mesh_initialize", "a2ds_mesh_get_ordering", "a2ds_mesh_node_csr",
     "a2ds_bcsr_create", "a2ds_bcsr_destroy", "a2ds_bcsr_get", "a2ds_bcsr_set_values",
     "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
-    "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
+    "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
     "a2ds_pc_apply", "a2ds_pc_get", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
     "a2ds_buckling_stats", "a2ds_eig_sens_thickness",
@@ -109,6 +109,7 @@ def load(build: bool = False):
     lib.a2ds_assemble_jacobian.argtypes = [VP, P_D, P_D, VP]
     lib.a2ds_bcsr_mult.argtypes = [VP, P_D, P_D]
     lib.a2ds_bcsr_mult_rows.argtypes = [VP, P_D, P_D]
+    lib.a2ds_bcsr_mult_rows_noalloc.argtypes = [VP, P_D, P_D]
     lib.a2ds_bcsr_copy.argtypes = [VP, VP]
     lib.a2ds_bcsr_axpy.argtypes = [VP, ctypes.c_double, VP]
     lib.a2ds_bcsr_apply_bcs.argtypes = [VP]
@@ -271,6 +272,15 @@ class BCSRMat:
         x = _f64(x).reshape(-1, 6)
         y = np.zeros_like(x)
         _check(self.lib.a2ds_bcsr_mult(self.h, _d(x), _d(y)))
+        return y
+
+    def mult_rows(self, x, noalloc=False):
+        """y = A x with x, y in the matrix (row) ordering; noalloc=True uses
+        the entry point that allocates no device memory (65536 rows at most)."""
+        x = _f64(x).reshape(-1, 6)
+        y = np.zeros_like(x)
+        fn = self.lib.a2ds_bcsr_mult_rows_noalloc if noalloc else self.lib.a2ds_bcsr_mult_rows
+        _check(fn(self.h, _d(x), _d(y)))
         return y
 
     def copy_values(self, other):

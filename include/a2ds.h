@@ -165,6 +165,16 @@ int a2ds_bcsr_mult(a2ds_bcsr A, const double *x, double *y);
 /* y = A x with both vectors already in the matrix (row) ordering. */
 int a2ds_bcsr_mult_rows(a2ds_bcsr A, const double *x, double *y);
 
+/* a2ds_bcsr_mult_rows without any device allocation.  No counterpart in the
+   reference: it exists for callers that cannot call cudaMalloc/cudaFree
+   (their memory manager owns the device, or cudaFree's device-wide wait is
+   not acceptable).  x and y are staged through a fixed device array of at
+   most 65536 block rows (6.3 MB, kept by every GPU that loads the library
+   until exit); larger matrices are rejected with A2DS_ERR_ARG.  The first
+   call on a device resolves that array's address (make it before any stream
+   capture).  All calls share the array: calls that overlap on the GPU race. */
+int a2ds_bcsr_mult_rows_noalloc(a2ds_bcsr A, const double *x, double *y);
+
 /* BCSRMat::copyValues (src/bpmat/BCSRMat.cpp:2375): Y <- X;
    BCSRMat::axpy (:2430): Y <- Y + alpha X; same pattern required. */
 int a2ds_bcsr_copy(a2ds_bcsr Y, a2ds_bcsr X);
