@@ -62,7 +62,7 @@ class BucklingOpts(ctypes.Structure):
                 ("lev_fill", ctypes.c_int), ("gmres_m", ctypes.c_int),
                 ("gmres_restarts", ctypes.c_int), ("gmres_rtol", ctypes.c_double),
                 ("gmres_atol", ctypes.c_double), ("precision", ctypes.c_int),
-                ("seed", ctypes.c_int)]
+                ("seed", ctypes.c_int), ("block_size", ctypes.c_int)]
 
 
 _lib = None
@@ -342,9 +342,9 @@ class SchurPc:
 
 
 STAT_NAMES = ["total_s", "assemble_k_s", "assemble_g_s", "factor_s", "path_s", "lanczos_s",
-              "lanczos_iters", "inner_iters", "kernel_launches", "solve_event_ms",
+              "lanczos_vectors", "inner_iters", "kernel_launches", "solve_event_ms",
               "factor_a_event_ms", "factor_k_event_ms", "factor_nnzb", "factor_levels",
-              "factor_flops"]
+              "factor_flops", "block_size", "block_iters"]
 
 
 class LinearBuckling:
@@ -352,13 +352,13 @@ class LinearBuckling:
     eig_tol): solve(rhs) then extract_eigenvalue / extract_eigenvector."""
 
     def __init__(self, assembler: Assembler, sigma, max_lanczos=100, num_eigvals=10,
-                 eig_tol=1e-10, lev_fill=1000000, precision=64, seed=0):
+                 eig_tol=1e-10, lev_fill=1000000, precision=64, seed=0, block_size=8):
         self.a = assembler
         self.lib = assembler.lib
         o = BucklingOpts()
         self.lib.a2ds_buckling_default_opts(ctypes.byref(o))
         o.sigma, o.max_lanczos, o.num_eigvals, o.eig_tol = sigma, max_lanczos, num_eigvals, eig_tol
-        o.lev_fill, o.precision, o.seed = lev_fill, precision, seed
+        o.lev_fill, o.precision, o.seed, o.block_size = lev_fill, precision, seed, block_size
         self.opts = o
         self.eigvals = self.errors = self.eigvecs = self.path = None
 

@@ -21,74 +21,13 @@
 //   one level never update each other's rows, and each target row is owned
 //   by one block, so no atomics are needed.  Dense trailing separators are
 //   thus updated by all their remaining rows in parallel at every level;
-// * solves use one warp per row on wide levels and one 256-thread block per
-//   row on narrow levels (the long rows of the dense tail), with nrhs
-//   right-hand sides stored row-major (row, dof, rhs).
+// * the solves are in trisolve.cu.
 #include "a2ds_internal.h"
 #include "ilu.h"
 
 namespace a2ds {
 
 constexpr int FACTOR_SMEM_COLS = 10240;  // column indices staged per target row
-constexpr int NARROW_LEVEL = 48;         // levels with fewer rows solve block-per-row
-
-template <typename T>
-__device__ __forceinline__ int d_inv6(const T *A, T *Ainv) {
-  T M[36], I[36];
-#pragma unroll
-  for (int k = 0; k < 36; k++) {
-    M[k] = A[k];
-    I[k] = (k % 7 == 0) ? T(1) : T(0);
-  }
-  int fail = 0;
-#pragma unroll
-  for (int c = 0; c < 6; c++) {
-    int p = c;
-    T best = fabs(M[6 * c + c]);
-#pragma unroll
-    for (int r = c + 1; r < 6; r++) {
-      T v = fabs(M[6 * r + c]);
-      if (v > best) {
-        best = v;
-        p = r;
-      }
-    }
-    if (best == T(0)) {
-      fail = c + 1;
-      break;
-    }
-    if (p != c) {
-#pragma unroll
-      for (int k = 0; k < 6; k++) {
-        T t = M[6 * c + k];
-        M[6 * c + k] = M[6 * p + k];
-        M[6 * p + k] = t;
-        t = I[6 * c + k];
-        I[6 * c + k] = I[6 * p + k];
-        I[6 * p + k] = t;
-      }
-    }
-    T inv = T(1) / M[6 * c + c];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      M[6 * c + k] *= inv;
-      I[6 * c + k] *= inv;
-    }
-#pragma unroll
-    for (int r = 0; r < 6; r++) {
-      if (r == c) continue;
-      T f = M[6 * r + c];
-#pragma unroll
-      for (int k = 0; k < 6; k++) {
-        M[6 * r + k] -= f * M[6 * c + k];
-        I[6 * r + k] -= f * I[6 * c + k];
-      }
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < 36; k++) Ainv[k] = I[k];
-  return fail;
-}
 
 // Copy the values of A (+ alpha2 A2) into the factor pattern, zero elsewhere.
 template <typename T>
@@ -123,18 +62,88 @@ __global__ void k_scatter_into_factor(int n, const int *__restrict__ rowp,
   }
 }
 
+// Invert the diagonal blocks of one level in place (6x6 Gauss-Jordan with
+// partial pivoting, first maximum wins, as BMatComputeInverse).  Six lanes
+// per block, one row of M and of the inverse each; pivot search, row swap
+// and the pivot-row broadcast go through warp shuffles, so every value
+// stays in registers and a level's blocks spread over many SMs (FP64
+// throughput per SM is low on this part).  Arithmetic is the same
+// operation sequence as the one-thread version, hence bit-identical.
 template <typename T>
-__global__ void k_factor_pivot(const int *__restrict__ rows, int nrows,
-                               const int *__restrict__ fdiag, T *__restrict__ F,
-                               int *__restrict__ status) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
-  const int j = rows[r];
-  T *D = F + (size_t)fdiag[j] * 36;
-  T inv[36];
-  if (d_inv6<T>(D, inv)) atomicMax(status, j + 1);
+__global__ void __launch_bounds__(128) k_factor_pivot(const int *__restrict__ rows, int nrows,
+                                                      const int *__restrict__ fdiag,
+                                                      T *__restrict__ F, int *__restrict__ status) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp * 5 >= nrows) return;  // whole warp
+  const int sub = lane / 6, r = lane - 6 * (lane / 6);
+  const int idx = warp * 5 + sub;
+  const bool live = sub < 5 && idx < nrows;
+  const int base = sub < 5 ? 6 * sub : 0;
+  const int j = live ? rows[idx] : 0;
+  T *D = F + (size_t)(live ? fdiag[j] : 0) * 36;
+  T m[6], v[6];
 #pragma unroll
-  for (int k = 0; k < 36; k++) D[k] = inv[k];
+  for (int k = 0; k < 6; k++) {
+    m[k] = live ? D[6 * r + k] : T(0);
+    v[k] = (k == r) ? T(1) : T(0);
+  }
+  int fail = 0;
+#pragma unroll
+  for (int c = 0; c < 6; c++) {
+    T bv = T(-1);
+    int bp = c;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+      const T vq = __shfl_sync(full, fabs(m[c]), base + q);
+      if (q >= c && vq > bv) {
+        bv = vq;
+        bp = q;
+      }
+    }
+    if (bv == T(0) && !fail) fail = c + 1;  // singular; result unused
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const T mc = __shfl_sync(full, m[k], base + c), mp = __shfl_sync(full, m[k], base + bp);
+      const T vc = __shfl_sync(full, v[k], base + c), vp = __shfl_sync(full, v[k], base + bp);
+      if (r == c) {
+        m[k] = mp;
+        v[k] = vp;
+      } else if (r == bp) {
+        m[k] = mc;
+        v[k] = vc;
+      }
+    }
+    const T piv = __shfl_sync(full, m[c], base + c);
+    const T inv = piv != T(0) ? T(1) / piv : T(0);
+    if (r == c) {
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        m[k] *= inv;
+        v[k] *= inv;
+      }
+    }
+    T pm[6], pv[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      pm[k] = __shfl_sync(full, m[k], base + c);
+      pv[k] = __shfl_sync(full, v[k], base + c);
+    }
+    if (r != c) {
+      const T f = m[c];
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        m[k] -= f * pm[k];
+        v[k] -= f * pv[k];
+      }
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) D[6 * r + k] = v[k];
+    if (fail && r == 0) atomicMax(status, j + 1);
+  }
 }
 
 template <typename T>
@@ -204,245 +213,6 @@ __global__ void __launch_bounds__(128) k_factor_update(
   }
 }
 
-// ---------------------------------------------------------------- solves
-// Forward substitution, one warp per row: y_i = x_i - sum_{k<diag} L_ik y_k
-template <typename T, typename TV>
-__global__ void __launch_bounds__(256) k_lower_warp(const int *__restrict__ rows, int nrows,
-                                                    const int *__restrict__ frowp,
-                                                    const int *__restrict__ fcols,
-                                                    const int *__restrict__ fdiag,
-                                                    const T *__restrict__ F, const TV *x, TV *y,
-                                                    int nrhs) {
-  __shared__ TV part[8][30];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wr = blockIdx.x * 8 + wib;
-  const bool live = wr < nrows;
-  const int i = live ? rows[wr] : 0;
-  const int g = lane / 6, ii = lane - 6 * (lane / 6);
-  for (int rhs = 0; rhs < nrhs; rhs++) {
-    TV acc = 0;
-    if (live && lane < 30) {
-      const int s = frowp[i], e = fdiag[i];
-      for (int k = s + g; k < e; k += 5) {
-        const T *a = F + (size_t)k * 36 + 6 * ii;
-        const TV *yv = y + (size_t)fcols[k] * 6 * nrhs + rhs;
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc += (TV)a[c] * yv[c * nrhs];
-      }
-    }
-    if (lane < 30) part[wib][lane] = acc;
-    __syncwarp();
-    if (live && lane < 6) {
-      TV v = part[wib][lane] + part[wib][lane + 6] + part[wib][lane + 12] + part[wib][lane + 18] +
-             part[wib][lane + 24];
-      const size_t o = ((size_t)i * 6 + lane) * nrhs + rhs;
-      y[o] = x[o] - v;
-    }
-    __syncwarp();
-  }
-}
-
-// Backward substitution, one warp per row: y_i = D_i^{-1}(y_i - sum U_ik y_k)
-template <typename T, typename TV>
-__global__ void __launch_bounds__(256) k_upper_warp(const int *__restrict__ rows, int nrows,
-                                                    const int *__restrict__ frowp,
-                                                    const int *__restrict__ fcols,
-                                                    const int *__restrict__ fdiag,
-                                                    const T *__restrict__ F, TV *y, int nrhs) {
-  __shared__ TV part[8][30];
-  __shared__ TV z[8][6];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wr = blockIdx.x * 8 + wib;
-  const bool live = wr < nrows;
-  const int i = live ? rows[wr] : 0;
-  const int g = lane / 6, ii = lane - 6 * (lane / 6);
-  for (int rhs = 0; rhs < nrhs; rhs++) {
-    TV acc = 0;
-    if (live && lane < 30) {
-      const int s = fdiag[i] + 1, e = frowp[i + 1];
-      for (int k = s + g; k < e; k += 5) {
-        const T *a = F + (size_t)k * 36 + 6 * ii;
-        const TV *yv = y + (size_t)fcols[k] * 6 * nrhs + rhs;
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc += (TV)a[c] * yv[c * nrhs];
-      }
-    }
-    if (lane < 30) part[wib][lane] = acc;
-    __syncwarp();
-    if (live && lane < 6) {
-      TV v = part[wib][lane] + part[wib][lane + 6] + part[wib][lane + 12] + part[wib][lane + 18] +
-             part[wib][lane + 24];
-      z[wib][lane] = y[((size_t)i * 6 + lane) * nrhs + rhs] - v;
-    }
-    __syncwarp();
-    if (live && lane < 6) {
-      const T *Dinv = F + (size_t)fdiag[i] * 36 + 6 * lane;
-      TV v = 0;
-#pragma unroll
-      for (int c = 0; c < 6; c++) v += (TV)Dinv[c] * z[wib][c];
-      y[((size_t)i * 6 + lane) * nrhs + rhs] = v;
-    }
-    __syncwarp();
-  }
-}
-
-// Long rows: one 256-thread block per row; 42 groups of six threads stride
-// over the row's blocks, partial sums reduced in shared memory.
-template <typename T, typename TV, bool UPPER>
-__global__ void __launch_bounds__(256) k_tri_block(const int *__restrict__ rows, int nrows,
-                                                   const int *__restrict__ frowp,
-                                                   const int *__restrict__ fcols,
-                                                   const int *__restrict__ fdiag,
-                                                   const T *__restrict__ F, const TV *x, TV *y,
-                                                   int nrhs) {
-  __shared__ TV part[256];
-  __shared__ TV z[6];
-  const int r = blockIdx.x;
-  if (r >= nrows) return;
-  const int i = rows[r];
-  const int t = threadIdx.x;
-  const int g = t / 6, ii = t - 6 * (t / 6);
-  const int s = UPPER ? fdiag[i] + 1 : frowp[i];
-  const int e = UPPER ? frowp[i + 1] : fdiag[i];
-  for (int rhs = 0; rhs < nrhs; rhs++) {
-    TV acc = 0;
-    if (t < 252) {
-      for (int k = s + g; k < e; k += 42) {
-        const T *a = F + (size_t)k * 36 + 6 * ii;
-        const TV *yv = y + (size_t)fcols[k] * 6 * nrhs + rhs;
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc += (TV)a[c] * yv[c * nrhs];
-      }
-    }
-    part[t] = acc;
-    __syncthreads();
-    // reduce the 42 groups: threads 0..5 sum their row
-    if (t < 6) {
-      TV v = 0;
-      for (int gg = 0; gg < 42; gg++) v += part[6 * gg + t];
-      const size_t o = ((size_t)i * 6 + t) * nrhs + rhs;
-      if (UPPER)
-        z[t] = y[o] - v;
-      else
-        y[o] = x[o] - v;
-    }
-    __syncthreads();
-    if (UPPER && t < 6) {
-      const T *Dinv = F + (size_t)fdiag[i] * 36 + 6 * t;
-      TV v = 0;
-#pragma unroll
-      for (int c = 0; c < 6; c++) v += (TV)Dinv[c] * z[c];
-      y[((size_t)i * 6 + t) * nrhs + rhs] = v;
-    }
-    __syncthreads();
-  }
-}
-
-// ------------------------------------------------------ dense-tail solves
-// Rows [s, n) (the trailing separators, where levels hold a handful of long
-// rows) are solved column-oriented: once a tail pivot's value is final its
-// column is pushed into every later row in parallel (one thread per block
-// entry, atomic adds because pivots of one level may share target rows).
-
-// Pull the head part of every tail row: y_i = x_i - sum_{j < s} L_ij y_j.
-template <typename T, typename TV>
-__global__ void __launch_bounds__(256) k_tail_pull(int s, int d, const int *__restrict__ frowp,
-                                                   const int *__restrict__ fcols,
-                                                   const int *__restrict__ lsplit,
-                                                   const T *__restrict__ F, const TV *x, TV *y,
-                                                   int nrhs) {
-  __shared__ TV part[8][30];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * 8 + wib;
-  const bool live = r < d;
-  const int i = s + (live ? r : 0);
-  const int g = lane / 6, ii = lane - 6 * (lane / 6);
-  for (int rhs = 0; rhs < nrhs; rhs++) {
-    TV acc = 0;
-    if (live && lane < 30) {
-      const int b = frowp[i], e = lsplit[r];
-      for (int k = b + g; k < e; k += 5) {
-        const T *a = F + (size_t)k * 36 + 6 * ii;
-        const TV *yv = y + (size_t)fcols[k] * 6 * nrhs + rhs;
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc += (TV)a[c] * yv[c * nrhs];
-      }
-    }
-    if (lane < 30) part[wib][lane] = acc;
-    __syncwarp();
-    if (live && lane < 6) {
-      TV v = part[wib][lane] + part[wib][lane + 6] + part[wib][lane + 12] + part[wib][lane + 18] +
-             part[wib][lane + 24];
-      const size_t o = ((size_t)i * 6 + lane) * nrhs + rhs;
-      y[o] = x[o] - v;
-    }
-    __syncwarp();
-  }
-}
-
-// Push the columns of one tail level.  Entry e: (target row, factor position,
-// pivot row).  Lower: y_i -= L_ij y_j.  Upper: z_i -= U_ij D_j^{-1} z_j
-// (the pivot's final value is formed on the fly; z_j itself is replaced by
-// D_j^{-1} z_j only after all tail levels, by k_tail_finalize).
-template <typename T, typename TV, bool UPPER>
-__global__ void __launch_bounds__(256) k_tail_push(const int *__restrict__ erow,
-                                                   const int *__restrict__ epos,
-                                                   const int *__restrict__ ecol, int ne,
-                                                   const int *__restrict__ fdiag,
-                                                   const T *__restrict__ F, TV *y, int nrhs) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  const int i = erow[e], p = epos[e], j = ecol[e];
-  const T *A = F + (size_t)p * 36;
-  for (int rhs = 0; rhs < nrhs; rhs++) {
-    TV w[6];
-#pragma unroll
-    for (int b = 0; b < 6; b++) w[b] = y[((size_t)j * 6 + b) * nrhs + rhs];
-    if (UPPER) {
-      const T *Dinv = F + (size_t)fdiag[j] * 36;
-      TV v[6];
-#pragma unroll
-      for (int a = 0; a < 6; a++) {
-        TV sacc = 0;
-#pragma unroll
-        for (int b = 0; b < 6; b++) sacc += (TV)Dinv[6 * a + b] * w[b];
-        v[a] = sacc;
-      }
-#pragma unroll
-      for (int a = 0; a < 6; a++) w[a] = v[a];
-    }
-#pragma unroll
-    for (int a = 0; a < 6; a++) {
-      TV sacc = 0;
-#pragma unroll
-      for (int b = 0; b < 6; b++) sacc += (TV)A[6 * a + b] * w[b];
-      atomicAdd(&y[((size_t)i * 6 + a) * nrhs + rhs], -sacc);
-    }
-  }
-}
-
-// y_j = D_j^{-1} z_j for every tail row (after the upper tail pushes).
-template <typename T, typename TV>
-__global__ void k_tail_finalize(int s, int d, const int *__restrict__ fdiag,
-                                const T *__restrict__ F, TV *y, int nrhs) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= d) return;
-  const int j = s + r;
-  const T *Dinv = F + (size_t)fdiag[j] * 36;
-  for (int rhs = 0; rhs < nrhs; rhs++) {
-    TV z[6];
-#pragma unroll
-    for (int b = 0; b < 6; b++) z[b] = y[((size_t)j * 6 + b) * nrhs + rhs];
-#pragma unroll
-    for (int a = 0; a < 6; a++) {
-      TV v = 0;
-#pragma unroll
-      for (int b = 0; b < 6; b++) v += (TV)Dinv[6 * a + b] * z[b];
-      y[((size_t)j * 6 + a) * nrhs + rhs] = v;
-    }
-  }
-}
-
 // ------------------------------------------------------------ launchers
 template <typename T>
 int factor_scatter(int n, const int *rowp, const int *cols, const double *A, const double *A2,
@@ -465,7 +235,7 @@ int factor_levels(const Factor &f, T *F, int *status, cudaStream_t s, long long 
   }
   for (int lv = 0; lv < L.nlevels; lv++) {
     const int cnt = L.ptr[lv + 1] - L.ptr[lv];
-    k_factor_pivot<T><<<(cnt + 127) / 128, 128, 0, s>>>(L.d_rows.p + L.ptr[lv], cnt,
+    k_factor_pivot<T><<<(cnt + 19) / 20, 128, 0, s>>>(L.d_rows.p + L.ptr[lv], cnt,
                                                         f.d_fdiag.p, F, status);
     const int t0 = f.task_level_ptr[lv], nt = f.task_level_ptr[lv + 1] - t0;
     if (nt > 0) {
@@ -479,69 +249,12 @@ int factor_levels(const Factor &f, T *F, int *status, cudaStream_t s, long long 
   return 0;
 }
 
-template <typename T, typename TV>
-int solve_levels(const Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
-                 long long *launches) {
-  const LevelSchedule &Lo = f.lower, &Up = f.upper;
-  long long nl = 0;
-  for (int lv = 0; lv < Lo.nlevels; lv++) {
-    const int cnt = Lo.ptr[lv + 1] - Lo.ptr[lv];
-    if (cnt < NARROW_LEVEL)
-      k_tri_block<T, TV, false><<<cnt, 256, 0, s>>>(Lo.d_rows.p + Lo.ptr[lv], cnt, f.d_frowp.p,
-                                                    f.d_fcols.p, f.d_fdiag.p, F, x, y, nrhs);
-    else
-      k_lower_warp<T, TV><<<(cnt + 7) / 8, 256, 0, s>>>(Lo.d_rows.p + Lo.ptr[lv], cnt,
-                                                        f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
-                                                        x, y, nrhs);
-    nl++;
-  }
-  const int ts = f.tail_s, d = f.n - f.tail_s;
-  if (d > 0) {
-    k_tail_pull<T, TV><<<(d + 7) / 8, 256, 0, s>>>(ts, d, f.d_frowp.p, f.d_fcols.p, f.d_lsplit.p,
-                                                   F, x, y, nrhs);
-    nl++;
-    for (size_t lv = 0; lv + 1 < f.tl_ptr.size(); lv++) {
-      const int e0 = f.tl_ptr[lv], ne = f.tl_ptr[lv + 1] - e0;
-      if (ne <= 0) continue;
-      k_tail_push<T, TV, false><<<(ne + 255) / 256, 256, 0, s>>>(
-          f.d_tl_row.p + e0, f.d_tl_pos.p + e0, f.d_tl_col.p + e0, ne, f.d_fdiag.p, F, y, nrhs);
-      nl++;
-    }
-    for (size_t lv = 0; lv + 1 < f.tu_ptr.size(); lv++) {
-      const int e0 = f.tu_ptr[lv], ne = f.tu_ptr[lv + 1] - e0;
-      if (ne <= 0) continue;
-      k_tail_push<T, TV, true><<<(ne + 255) / 256, 256, 0, s>>>(
-          f.d_tu_row.p + e0, f.d_tu_pos.p + e0, f.d_tu_col.p + e0, ne, f.d_fdiag.p, F, y, nrhs);
-      nl++;
-    }
-    k_tail_finalize<T, TV><<<(d + 127) / 128, 128, 0, s>>>(ts, d, f.d_fdiag.p, F, y, nrhs);
-    nl++;
-  }
-  for (int lv = 0; lv < Up.nlevels; lv++) {
-    const int cnt = Up.ptr[lv + 1] - Up.ptr[lv];
-    if (cnt < NARROW_LEVEL)
-      k_tri_block<T, TV, true><<<cnt, 256, 0, s>>>(Up.d_rows.p + Up.ptr[lv], cnt, f.d_frowp.p,
-                                                   f.d_fcols.p, f.d_fdiag.p, F, y, y, nrhs);
-    else
-      k_upper_warp<T, TV><<<(cnt + 7) / 8, 256, 0, s>>>(Up.d_rows.p + Up.ptr[lv], cnt,
-                                                        f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
-                                                        y, nrhs);
-  }
-  if (launches) *launches += nl + Up.nlevels;
-  A2DS_CUDA_TRY(cudaGetLastError());
-  return 0;
-}
-
 template int factor_scatter<double>(int, const int *, const int *, const double *, const double *,
                                     double, const int *, const int *, double *, cudaStream_t);
 template int factor_scatter<float>(int, const int *, const int *, const double *, const double *,
                                    double, const int *, const int *, float *, cudaStream_t);
 template int factor_levels<double>(const Factor &, double *, int *, cudaStream_t, long long *);
 template int factor_levels<float>(const Factor &, float *, int *, cudaStream_t, long long *);
-template int solve_levels<double, double>(const Factor &, const double *, const double *, double *,
-                                          int, cudaStream_t, long long *);
-template int solve_levels<float, float>(const Factor &, const float *, const float *, float *, int,
-                                        cudaStream_t, long long *);
 
 // ------------------------------------------------------------- host side
 void build_levels(int n, const std::vector<int> &frowp, const std::vector<int> &fcols,

@@ -14,6 +14,16 @@ struct LevelSchedule {
   DBuf<int> d_rows;
 };
 
+// An instantiated CUDA graph of one whole triangular solve, keyed by the
+// factor values and the vectors it was captured with.
+struct SolveGraph {
+  const void *F, *x;
+  void *y;
+  int nrhs, tv_size;
+  cudaGraphExec_t exec;
+  long long nlaunch;  // kernels in the graph
+};
+
 // A factorization handle (the TACSSchurPc role on one GPU).
 struct Factor {
   int n = 0, lev_fill = 0, precision = 64;
@@ -33,6 +43,9 @@ struct Factor {
   // algorithmic FP operations of one numeric factorization: 432 per L block
   // (L_ij = A_ij D_j^{-1}), 432 per block update, 432 per diagonal inverse
   double flop_count = 0.0;
+  std::vector<SolveGraph> graphs;  // solve_graph cache (at most 8)
+  Factor() = default;
+  ~Factor();
   long long nnzb() const { return frowp.empty() ? 0 : frowp.back(); }
   double flops() const { return flop_count; }
 };
@@ -56,11 +69,17 @@ int factor_scatter(int n, const int *rowp, const int *cols, const double *A, con
 template <typename T>
 int factor_levels(const Factor &f, T *F, int *status, cudaStream_t s, long long *launches);
 
-// y = (LU)^{-1} x for nrhs right-hand sides, layout (row, dof, rhs); y may
-// alias x.
+// y = (LU)^{-1} x for nrhs in {1, 2, 4, 8, 16} right-hand sides, layout
+// (row, dof, rhs); y may alias x.  solve_levels launches the level kernels
+// on s; solve_graph does the same through a CUDA graph captured on the
+// first call with these (F, x, y, nrhs) and replayed afterwards (s must not
+// be capturing already).
 template <typename T, typename TV>
 int solve_levels(const Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
                  long long *launches);
+template <typename T, typename TV>
+int solve_graph(Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
+                long long *launches);
 
 struct Mesh;
 int factor_setup(Mesh &m, int lev_fill, int precision, Factor &f);

@@ -1,4 +1,4 @@
-// Factorization handles, BLAS-1 kernels and the shift-invert Lanczos
+// Factorization handles, BLAS-1 kernels and the block shift-invert Lanczos
 // buckling solve.
 //
 // Reference path (TACSLinearBuckling::solve, src/TACSBuckling.cpp:197-278):
@@ -8,12 +8,16 @@
 //
 // Differences by design (results agree to the eigenvalue tolerance):
 // * the shifted matrix A = K + sigma G is factored directly and applied with
-//   iterative refinement, instead of GMRES on A preconditioned by a factor
-//   of K (one triangular-solve pair per Lanczos step instead of tens);
-// * K q_j is kept for every Lanczos vector, so the K-inner products of the
-//   full orthogonalisation are dot products, not one K SpMV each;
+//   FP64 iterative refinement, instead of GMRES on A preconditioned by a
+//   factor of K (one triangular-solve pair per Lanczos step instead of tens);
+// * block Lanczos: p basis vectors per step, so one triangular-solve pass
+//   (latency-bound: thousands of dependent level launches, replayed from a
+//   CUDA graph) serves p vectors.  p = 1 is the reference's iteration;
+// * K Q_j is kept for every basis block, so the K-inner products of the
+//   full (two-pass classical Gram-Schmidt) orthogonalisation are dot
+//   products, not one K SpMV each (the reference spends one per dot);
 // * Ritz pairs are tested for convergence (residual estimate
-//   |beta_m y_m| relative to |mu|) instead of stopping after exactly
+//   ||B_j y_j|| relative to |mu|) instead of stopping after exactly
 //   num_eigvals steps (SEP::checkConverged returns 1 as soon as
 //   n >= neigvals, src/bpmat/GSEP.cpp:754-789).
 #include <math.h>
@@ -25,6 +29,7 @@
 #include <vector>
 
 #include "a2ds_internal.h"
+#include "block.h"
 #include "host_graph.h"
 #include "ilu.h"
 #include "kernels.h"
@@ -91,17 +96,6 @@ __global__ void __launch_bounds__(256) k_multidot(const double *X, size_t ldx, i
   }
 }
 
-// y -= sum_j c[j] X[j]  (c on the device)
-__global__ void k_sub_combination(double *y, const double *X, size_t ldx, int m, const double *c,
-                                  size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < m; j++) s += c[j] * X[(size_t)j * ldx + i];
-    y[i] -= s;
-  }
-}
-
 static int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 8); }
 
 struct Blas {
@@ -124,15 +118,6 @@ struct Blas {
     double h = 0.0;
     if (dots(x, n, 1, y, n, &h)) return NAN;
     return h;
-  }
-  int sub_combination(double *y, const double *X, size_t ldx, int m, const double *hc, size_t n) {
-    int rc;
-    if ((rc = dwork.alloc(std::max<size_t>(m, 1)))) return rc;
-    A2DS_CUDA_TRY(cudaMemcpyAsync(dwork.p, hc, m * sizeof(double), cudaMemcpyHostToDevice, s));
-    k_sub_combination<<<grid_for(n), 256, 0, s>>>(y, X, ldx, m, dwork.p, n);
-    (*launches)++;
-    A2DS_CUDA_TRY(cudaGetLastError());
-    return 0;
   }
   void scale(double *x, double a, size_t n) {
     k_scale<<<grid_for(n), 256, 0, s>>>(x, a, n);
@@ -264,59 +249,145 @@ static int factor_apply(Mesh &m, Factor &f, const double *x, double *y, DBuf<flo
 }
 
 // ------------------------------------------------- small dense eigensolver
-// Cyclic Jacobi for a symmetric m x m matrix (row-major, destroyed);
-// eigenvalues in w, eigenvectors as columns of V.
-static void jacobi_eig(int m, std::vector<double> &A, std::vector<double> &w,
-                       std::vector<double> &V) {
-  V.assign((size_t)m * m, 0.0);
-  for (int i = 0; i < m; i++) V[(size_t)i * m + i] = 1.0;
-  for (int sweep = 0; sweep < 100; sweep++) {
-    double off = 0.0, tot = 0.0;
-    for (int i = 0; i < m; i++)
-      for (int j = 0; j < m; j++) {
-        double v = A[(size_t)i * m + j] * A[(size_t)i * m + j];
-        tot += v;
-        if (i != j) off += v;
-      }
-    if (off <= 1e-30 * tot || off == 0.0) break;
-    for (int p = 0; p < m - 1; p++)
-      for (int q = p + 1; q < m; q++) {
-        double apq = A[(size_t)p * m + q];
-        if (apq == 0.0) continue;
-        double app = A[(size_t)p * m + p], aqq = A[(size_t)q * m + q];
-        double theta = (aqq - app) / (2.0 * apq);
-        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < m; k++) {
-          double akp = A[(size_t)k * m + p], akq = A[(size_t)k * m + q];
-          A[(size_t)k * m + p] = c * akp - s * akq;
-          A[(size_t)k * m + q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < m; k++) {
-          double apk = A[(size_t)p * m + k], aqk = A[(size_t)q * m + k];
-          A[(size_t)p * m + k] = c * apk - s * aqk;
-          A[(size_t)q * m + k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < m; k++) {
-          double vkp = V[(size_t)k * m + p], vkq = V[(size_t)k * m + q];
-          V[(size_t)k * m + p] = c * vkp - s * vkq;
-          V[(size_t)k * m + q] = s * vkp + c * vkq;
-        }
-      }
+// Eigen-decomposition of a symmetric n x n matrix (row-major A, destroyed):
+// Householder reduction to tridiagonal form, then the implicit QL iteration
+// with shifts (the tred2/tql2 scheme of Bowdler, Martin, Reinsch and
+// Wilkinson, Handbook for Automatic Computation vol. II).  Eigenvalues in w,
+// eigenvectors as the columns of V.  Returns nonzero if QL did not converge.
+static int sym_eig(int n, std::vector<double> &A, std::vector<double> &w,
+                   std::vector<double> &V) {
+  V.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) V[(size_t)i * n + i] = 1.0;
+  std::vector<double> v(n), u(n), q(n);
+  for (int k = 0; k + 2 < n; k++) {
+    double xn2 = 0.0;
+    for (int i = k + 1; i < n; i++) xn2 += A[(size_t)i * n + k] * A[(size_t)i * n + k];
+    if (xn2 == 0.0) continue;
+    const double x0 = A[(size_t)(k + 1) * n + k];
+    const double a = x0 >= 0.0 ? -sqrt(xn2) : sqrt(xn2);
+    for (int i = k + 1; i < n; i++) v[i] = A[(size_t)i * n + k];
+    v[k + 1] -= a;
+    double vn2 = 0.0;
+    for (int i = k + 1; i < n; i++) vn2 += v[i] * v[i];
+    if (vn2 == 0.0) continue;
+    const double vs = 1.0 / sqrt(vn2);
+    for (int i = k + 1; i < n; i++) v[i] *= vs;
+    // trailing block B <- H B H = B - v q^T - q v^T, q = 2 B v - 2 (v^T B v) v
+    double c = 0.0;
+    for (int i = k + 1; i < n; i++) {
+      double s = 0.0;
+      for (int j = k + 1; j < n; j++) s += A[(size_t)i * n + j] * v[j];
+      u[i] = s;
+      c += v[i] * s;
+    }
+    for (int i = k + 1; i < n; i++) q[i] = 2.0 * u[i] - 2.0 * c * v[i];
+    for (int i = k + 1; i < n; i++)
+      for (int j = k + 1; j < n; j++) A[(size_t)i * n + j] -= v[i] * q[j] + q[i] * v[j];
+    A[(size_t)(k + 1) * n + k] = A[(size_t)k * n + k + 1] = a;
+    for (int i = k + 2; i < n; i++) A[(size_t)i * n + k] = A[(size_t)k * n + i] = 0.0;
+    // V <- V H
+    for (int r = 0; r < n; r++) {
+      double s = 0.0;
+      for (int j = k + 1; j < n; j++) s += V[(size_t)r * n + j] * v[j];
+      s *= 2.0;
+      for (int j = k + 1; j < n; j++) V[(size_t)r * n + j] -= s * v[j];
+    }
   }
-  w.resize(m);
-  for (int i = 0; i < m; i++) w[i] = A[(size_t)i * m + i];
+  std::vector<double> d(n), e(n, 0.0);
+  for (int i = 0; i < n; i++) d[i] = A[(size_t)i * n + i];
+  for (int i = 0; i + 1 < n; i++) e[i] = A[(size_t)(i + 1) * n + i];
+  // implicit QL on (d, e), e[i] coupling i and i + 1
+  for (int l = 0; l < n; l++) {
+    int iter = 0;
+    for (;;) {
+      int m = l;
+      for (; m < n - 1; m++) {
+        const double dd = fabs(d[m]) + fabs(d[m + 1]);
+        if (fabs(e[m]) <= 2.3e-16 * dd) break;
+      }
+      if (m == l) break;
+      if (++iter > 80) return 1;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? fabs(r) : -fabs(r)));
+      double s = 1.0, c = 1.0, p = 0.0;
+      bool deflated = false;
+      for (int i = m - 1; i >= l; i--) {
+        double f = s * e[i];
+        const double b = c * e[i];
+        r = hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {
+          d[i + 1] -= p;
+          e[m] = 0.0;
+          deflated = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - b;
+        for (int k = 0; k < n; k++) {
+          f = V[(size_t)k * n + i + 1];
+          V[(size_t)k * n + i + 1] = s * V[(size_t)k * n + i] + c * f;
+          V[(size_t)k * n + i] = c * V[(size_t)k * n + i] - s * f;
+        }
+      }
+      if (deflated) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  w = d;
+  return 0;
+}
+
+// M = R^T R for a symmetric positive definite p x p M (row-major); R upper.
+static bool chol_upper(int p, const std::vector<double> &M, std::vector<double> &R) {
+  R.assign((size_t)p * p, 0.0);
+  for (int j = 0; j < p; j++) {
+    double s = M[(size_t)j * p + j];
+    for (int k = 0; k < j; k++) s -= R[(size_t)k * p + j] * R[(size_t)k * p + j];
+    if (!(s > 0.0) || !std::isfinite(s)) return false;
+    const double rjj = sqrt(s);
+    R[(size_t)j * p + j] = rjj;
+    for (int i = j + 1; i < p; i++) {
+      double t = M[(size_t)j * p + i];
+      for (int k = 0; k < j; k++) t -= R[(size_t)k * p + j] * R[(size_t)k * p + i];
+      R[(size_t)j * p + i] = t / rjj;
+    }
+  }
+  return true;
+}
+
+// Inverse of an upper-triangular p x p matrix.
+static void inv_upper(int p, const std::vector<double> &R, std::vector<double> &Ri) {
+  Ri.assign((size_t)p * p, 0.0);
+  for (int j = 0; j < p; j++) {
+    Ri[(size_t)j * p + j] = 1.0 / R[(size_t)j * p + j];
+    for (int i = j - 1; i >= 0; i--) {
+      double s = 0.0;
+      for (int k = i + 1; k <= j; k++) s += R[(size_t)i * p + k] * Ri[(size_t)k * p + j];
+      Ri[(size_t)i * p + j] = -s / R[(size_t)i * p + i];
+    }
+  }
 }
 
 // --------------------------------------------------------- buckling state
 struct BucklingState {
   Factor fk, fa;
   DBuf<double> K, G, Aux;
-  DBuf<double> Q, KQ;  // (m+1) x n6 Lanczos basis and K times it
-  DBuf<double> w, r, t, path, rhs;
+  DBuf<double> Q, KQ;    // (nb + 1) blocks of n6 x p: Lanczos basis and K times it
+  DBuf<double> Xb, Yb;   // fixed solve input / output blocks (graph-captured)
+  DBuf<double> dH1, dH2, dN, dM;  // small device scratch (coefficients)
+  DBuf<double> phi, r, t, path, rhs;
   DBuf<float> w32;
-  std::vector<double> lam, err, phi_ritz;  // converged data
-  int niters = 0, nconv = 0;
+  std::vector<double> lam, err, ritz;  // converged data
+  int nconv = 0;
   double sigma = 0.0;
   int lev_fill = -1, precision = 0;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -338,33 +409,118 @@ static double now() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Solve A x = b (row ordering) with the factor and FP64 iterative
-// refinement (residual with A = Avals (+ alpha2 A2vals) in FP64).
-static int refined_solve(Mesh &m, Factor &f, const double *Avals, const double *A2vals,
-                         double alpha2, const double *b, double *x, BucklingState &S, Blas &B,
-                         double rtol, int max_steps, int *steps) {
+// Squared column norms of an n6 x p block (host result, synchronises).
+static int block_norms2(Mesh &m, BucklingState &S, const double *X, int p,
+                        std::vector<double> &out) {
   const size_t n6 = (size_t)m.nn * 6;
   int rc;
-  if ((rc = factor_apply(m, f, b, x, S.w32))) return rc;
-  double bn = sqrt(B.dot(b, b, n6));
-  if (bn == 0.0) return 0;
-  for (int it = 0; it < max_steps; it++) {
-    // r = b - A x
-    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, Avals, x, S.r.p, m.stream))) return rc;
-    m.launches++;
-    if (A2vals) {
-      if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, A2vals, x, S.t.p, m.stream)))
-        return rc;
-      m.launches++;
-      B.axpby(S.r.p, alpha2, S.t.p, 1.0, n6);
-    }
-    B.axpby(S.r.p, 1.0, b, -1.0, n6);  // r = b - r
-    double rn = sqrt(B.dot(S.r.p, S.r.p, n6));
-    if (steps) (*steps)++;
-    if (rn <= rtol * bn) return 0;
-    if ((rc = factor_apply(m, f, S.r.p, S.t.p, S.w32))) return rc;
-    B.axpby(x, 1.0, S.t.p, 1.0, n6);
+  if ((rc = blk_dots(X, 1, 0, X, n6, p, S.dN.p, m.stream))) return rc;
+  m.launches++;
+  std::vector<double> M((size_t)p * p);
+  A2DS_CUDA_TRY(cudaMemcpyAsync(M.data(), S.dN.p, M.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  out.resize(p);
+  for (int c = 0; c < p; c++) out[c] = M[(size_t)c * p + c];
+  return 0;
+}
+
+// S.Yb = (LU)^{-1} S.Xb for a block of p vectors, through the factor's
+// cached CUDA graph (FP32 factors: rounded to FP32 and back).
+static int apply_factor_block(Mesh &m, BucklingState &S, Factor &f, int p) {
+  const size_t n = (size_t)m.nn * 6 * p;
+  if (f.precision == 32) {
+    int rc;
+    if ((rc = S.w32.alloc(n))) return rc;
+    k_f64_to_f32<<<grid_for(n), 256, 0, m.stream>>>(S.w32.p, S.Xb.p, n);
+    if ((rc = solve_graph<float, float>(f, f.F32.p, S.w32.p, S.w32.p, p, m.stream, &m.launches)))
+      return rc;
+    A2DS_CUDA_TRY(cudaMemsetAsync(S.Yb.p, 0, n * sizeof(double), m.stream));
+    k_add_f32<<<grid_for(n), 256, 0, m.stream>>>(S.Yb.p, S.w32.p, n);
+    m.launches += 2;
+    A2DS_CUDA_TRY(cudaGetLastError());
+    return 0;
   }
+  return solve_graph<double, double>(f, f.F64.p, S.Xb.p, S.Yb.p, p, m.stream, &m.launches);
+}
+
+// Solve A Y = X for a block of p vectors (row ordering) with the factor and
+// FP64 iterative refinement: the residual X - A Y with the FP64 matrix
+// Avals, corrections until every column's relative residual is <= rtol or
+// max_steps corrections were made.  X and Y must not alias.
+static int refined_block_solve(Mesh &m, BucklingState &S, Factor &f, const double *Avals,
+                               const double *X, double *Y, int p, double rtol, int max_steps,
+                               int *steps) {
+  const size_t n = (size_t)m.nn * 6 * p;
+  int rc;
+  std::vector<double> xn, rn;
+  A2DS_CUDA_TRY(cudaMemcpyAsync(S.Xb.p, X, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                m.stream));
+  if ((rc = block_norms2(m, S, S.Xb.p, p, xn))) return rc;
+  if ((rc = apply_factor_block(m, S, f, p))) return rc;
+  A2DS_CUDA_TRY(cudaMemcpyAsync(Y, S.Yb.p, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                m.stream));
+  for (int it = 0; it < max_steps; it++) {
+    if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Avals, Y, X, S.Xb.p, p, m.stream)))
+      return rc;
+    m.launches++;
+    if ((rc = block_norms2(m, S, S.Xb.p, p, rn))) return rc;
+    if (steps) (*steps)++;
+    bool done = true;
+    for (int c = 0; c < p; c++)
+      if (!(rn[c] <= rtol * rtol * xn[c])) done = false;
+    if (done) return 0;
+    if ((rc = apply_factor_block(m, S, f, p))) return rc;
+    if ((rc = blk_add(Y, S.Yb.p, n, m.stream))) return rc;
+    m.launches++;
+  }
+  return 0;
+}
+
+// K-orthonormalise the block W (with KW = K W): one Cholesky-QR pass,
+// W <- W R^{-1}, KW <- KW R^{-1}, W^T K W = R^T R.  Returns R (host).
+static int cholqr_pass(Mesh &m, BucklingState &S, double *W, double *KW, int p,
+                       std::vector<double> &R) {
+  const size_t n6 = (size_t)m.nn * 6;
+  int rc;
+  if ((rc = blk_dots(W, 1, 0, KW, n6, p, S.dN.p, m.stream))) return rc;
+  m.launches++;
+  std::vector<double> M((size_t)p * p), Ri;
+  A2DS_CUDA_TRY(cudaMemcpyAsync(M.data(), S.dN.p, M.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  for (int i = 0; i < p; i++)
+    for (int j = i + 1; j < p; j++) {
+      const double a = 0.5 * (M[(size_t)i * p + j] + M[(size_t)j * p + i]);
+      M[(size_t)i * p + j] = M[(size_t)j * p + i] = a;
+    }
+  if (!chol_upper(p, M, R))
+    return fail(A2DS_ERR_BREAKDOWN, "Lanczos breakdown: the new block is K-rank deficient");
+  inv_upper(p, R, Ri);
+  A2DS_CUDA_TRY(cudaMemcpyAsync(S.dM.p, Ri.data(), Ri.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, m.stream));
+  if ((rc = blk_rmul(W, S.dM.p, n6, p, m.stream))) return rc;
+  if ((rc = blk_rmul(KW, S.dM.p, n6, p, m.stream))) return rc;
+  m.launches += 2;
+  // the host copy of Ri must outlive the asynchronous upload
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  return 0;
+}
+
+// Two Cholesky-QR passes; B (upper) with W_in = W_out B.
+static int cholqr2(Mesh &m, BucklingState &S, double *W, double *KW, int p,
+                   std::vector<double> &B) {
+  std::vector<double> R1, R2;
+  int rc;
+  if ((rc = cholqr_pass(m, S, W, KW, p, R1))) return rc;
+  if ((rc = cholqr_pass(m, S, W, KW, p, R2))) return rc;
+  B.assign((size_t)p * p, 0.0);
+  for (int i = 0; i < p; i++)
+    for (int j = 0; j < p; j++) {
+      double s = 0.0;
+      for (int k = 0; k < p; k++) s += R2[(size_t)i * p + k] * R1[(size_t)k * p + j];
+      B[(size_t)i * p + j] = s;
+    }
   return 0;
 }
 
@@ -454,6 +610,7 @@ void a2ds_buckling_default_opts(a2ds_buckling_opts *o) {
   o->gmres_atol = 1e-30;
   o->precision = 64;
   o->seed = 0;
+  o->block_size = 8;
 }
 
 int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const double *rhs,
@@ -461,13 +618,18 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   if (!mesh || !opts || !eigvals) return fail(A2DS_ERR_ARG, "null argument");
   Mesh &m = mesh->m;
   if (!m.initialized) return fail(A2DS_ERR_STATE, "mesh not initialized");
-  const int nev = opts->num_eigvals, mmax = opts->max_lanczos;
-  if (nev <= 0 || mmax < nev) return fail(A2DS_ERR_ARG, "need 0 < num_eigvals <= max_lanczos");
+  const int nev = opts->num_eigvals, mmax = opts->max_lanczos, p = opts->block_size;
+  if (p != 1 && p != 2 && p != 4 && p != 8 && p != 16)
+    return fail(A2DS_ERR_ARG, "block_size must be 1, 2, 4, 8 or 16");
+  const int nbmax = mmax / p;  // block steps; basis dimension <= max_lanczos
+  if (nev <= 0 || nbmax < 1 || nbmax * p < nev)
+    return fail(A2DS_ERR_ARG, "need 0 < num_eigvals <= max_lanczos and block_size <= max_lanczos");
   if (!(opts->sigma > 0.0)) return fail(A2DS_ERR_ARG, "sigma must be positive");
   if (opts->precision != 64 && opts->precision != 32)
     return fail(A2DS_ERR_ARG, "precision must be 64 or 32");
   const size_t n6 = (size_t)m.nn * 6;
   const size_t nv = (size_t)m.nnzb * 36;
+  const size_t bs = n6 * p;  // doubles per basis block
   int rc;
   double t0 = now();
   long long launches0 = m.launches;
@@ -485,10 +647,13 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   BucklingState &S = *Sp;
   S.sigma = opts->sigma;
   if ((rc = S.K.alloc(nv)) || (rc = S.G.alloc(nv)) || (rc = S.Aux.alloc(nv))) return rc;
-  if ((rc = S.Q.alloc((size_t)(mmax + 1) * n6)) || (rc = S.KQ.alloc((size_t)(mmax + 1) * n6)))
+  if ((rc = S.Q.alloc((size_t)(nbmax + 1) * bs)) || (rc = S.KQ.alloc((size_t)(nbmax + 1) * bs)))
     return rc;
-  if ((rc = S.w.alloc(n6)) || (rc = S.r.alloc(n6)) || (rc = S.t.alloc(n6)) ||
-      (rc = S.path.alloc(n6)) || (rc = S.rhs.alloc(n6)))
+  if ((rc = S.Xb.alloc(bs)) || (rc = S.Yb.alloc(bs)) || (rc = S.dH1.alloc((size_t)nbmax * p * p)) ||
+      (rc = S.dH2.alloc((size_t)nbmax * p * p)) || (rc = S.dN.alloc((size_t)p * p)) ||
+      (rc = S.dM.alloc((size_t)p * p)) || (rc = S.phi.alloc((size_t)nev * n6)) ||
+      (rc = S.r.alloc(n6)) || (rc = S.t.alloc(n6)) || (rc = S.path.alloc(n6)) ||
+      (rc = S.rhs.alloc(n6)))
     return rc;
   Blas B{m.stream};
   B.launches = &m.launches;
@@ -510,7 +675,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   ta = now();
   if ((rc = m.assemble_device(MODE_R, nullptr, nullptr, S.r.p, A2DS_SCATTER_ATOMIC))) return rc;
   {
-    std::vector<double> h((size_t)m.nn * 6, 0.0), hr(n6);
+    std::vector<double> h((size_t)m.nn * 6, 0.0);
     if (rhs) {
       for (int i = 0; i < m.nn; i++)
         for (int k = 0; k < 6; k++) h[(size_t)i * 6 + k] = rhs[(size_t)m.perm[i] * 6 + k];
@@ -525,9 +690,10 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
         S.r.p, m.d_bc_rows.p, m.d_bc_masks.p, (int)m.bc_rows.size());
     m.launches++;
     B.axpby(S.rhs.p, -1.0, S.r.p, 1.0, n6);  // rhs = rhs - R(0): K path = rhs
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // h is pageable and goes out of scope
   }
   int inner = 0;
-  if ((rc = refined_solve(m, S.fk, S.K.p, nullptr, 0.0, S.rhs.p, S.path.p, S, B, 1e-13, 4, &inner)))
+  if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.rhs.p, S.path.p, 1, 1e-13, 4, &inner)))
     return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   double t_path = now() - ta;
@@ -551,85 +717,92 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   if ((rc = factor_check(m, S.fa))) return rc;
   double t_fa = now() - ta;
 
-  // 4. Lanczos on A^{-1} K with the K inner product
+  // 4. block Lanczos on A^{-1} K with the K inner product
   ta = now();
   const int nbc = (int)m.bc_rows.size();
-  auto zero_bc = [&](double *x) {
-    if (nbc) {
-      k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(x, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
-      m.launches++;
-    }
-  };
   {
-    // seeded start vector (splitmix64), BC DOFs zeroed, K-normalised
-    std::vector<double> h(n6);
+    // seeded start block (splitmix64), BC DOFs zeroed, K-orthonormalised
+    std::vector<double> h(bs);
     uint64_t st = 0x9E3779B97F4A7C15ull * (uint64_t)(opts->seed + 1);
-    for (size_t i = 0; i < n6; i++) {
+    for (size_t i = 0; i < bs; i++) {
       uint64_t z = (st += 0x9E3779B97F4A7C15ull);
       z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
       z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
       z ^= z >> 31;
       h[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
     }
-    A2DS_CUDA_TRY(cudaMemcpyAsync(S.Q.p, h.data(), n6 * sizeof(double), cudaMemcpyHostToDevice,
+    A2DS_CUDA_TRY(cudaMemcpyAsync(S.Q.p, h.data(), bs * sizeof(double), cudaMemcpyHostToDevice,
                                   m.stream));
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   }
-  zero_bc(S.Q.p);
-  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, S.Q.p, S.KQ.p, m.stream))) return rc;
-  m.launches++;
-  {
-    double nrm = sqrt(B.dot(S.Q.p, S.KQ.p, n6));
-    B.scale(S.Q.p, 1.0 / nrm, n6);
-    B.scale(S.KQ.p, 1.0 / nrm, n6);
-  }
-  std::vector<double> alpha, beta, h((size_t)mmax + 1), h2((size_t)mmax + 1);
-  std::vector<double> ritz_mu, ritz_vec;  // of the converged set
+  if ((rc = blk_zero_bc(S.Q.p, p, m.d_bc_rows.p, m.d_bc_masks.p, nbc, m.stream))) return rc;
+  if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, S.Q.p, nullptr, S.KQ.p, p, m.stream)))
+    return rc;
+  m.launches += 2;
+  std::vector<double> Bj;
+  if ((rc = cholqr2(m, S, S.Q.p, S.KQ.p, p, Bj))) return rc;
+
+  const int tdim = (nbmax + 1) * p;
+  std::vector<double> T((size_t)tdim * tdim, 0.0), h1((size_t)p * p), h2((size_t)p * p);
+  std::vector<double> Tw, TV, Tm;
   std::vector<int> order;
-  int m_iter = 0, converged = 0;
-  double last_beta = 0.0;
-  std::vector<double> Tw, TV;
-  for (int i = 0; i < mmax; i++) {
-    double *qi = S.Q.p + (size_t)i * n6, *kqi = S.KQ.p + (size_t)i * n6;
-    double *w = S.Q.p + (size_t)(i + 1) * n6, *kw = S.KQ.p + (size_t)(i + 1) * n6;
-    // w = A^{-1} K q_i
-    if ((rc = refined_solve(m, S.fa, S.Aux.p, nullptr, 0.0, kqi, w, S, B, 1e-10, 2, &inner)))
+  auto lamof = [&](double mu) { return -mu * S.sigma / (1.0 - mu); };
+  int nsteps = 0, mdim = 0, converged = 0;
+  std::vector<double> lastB;
+  for (int j = 0; j < nbmax; j++) {
+    double *KQj = S.KQ.p + (size_t)j * bs;
+    double *W = S.Q.p + (size_t)(j + 1) * bs, *KW = S.KQ.p + (size_t)(j + 1) * bs;
+    // W = A^{-1} K Q_j
+    if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, 1e-10, 2, &inner))) return rc;
+    if ((rc = blk_zero_bc(W, p, m.d_bc_rows.p, m.d_bc_masks.p, nbc, m.stream))) return rc;
+    // full K-orthogonalisation against blocks 0..j, two classical passes
+    if ((rc = blk_dots(S.KQ.p, j + 1, bs, W, n6, p, S.dH1.p, m.stream))) return rc;
+    if ((rc = blk_sub(W, S.Q.p, j + 1, bs, S.dH1.p, n6, p, m.stream))) return rc;
+    if ((rc = blk_dots(S.KQ.p, j + 1, bs, W, n6, p, S.dH2.p, m.stream))) return rc;
+    if ((rc = blk_sub(W, S.Q.p, j + 1, bs, S.dH2.p, n6, p, m.stream))) return rc;
+    m.launches += 5;
+    A2DS_CUDA_TRY(cudaMemcpyAsync(h1.data(), S.dH1.p + (size_t)j * p * p, p * p * sizeof(double),
+                                  cudaMemcpyDeviceToHost, m.stream));
+    A2DS_CUDA_TRY(cudaMemcpyAsync(h2.data(), S.dH2.p + (size_t)j * p * p, p * p * sizeof(double),
+                                  cudaMemcpyDeviceToHost, m.stream));
+    if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, W, nullptr, KW, p, m.stream)))
       return rc;
-    zero_bc(w);
-    // full K-orthogonalisation, two classical Gram-Schmidt passes using K q_j
-    if ((rc = B.dots(S.KQ.p, n6, i + 1, w, n6, h.data()))) return rc;
-    if ((rc = B.sub_combination(w, S.Q.p, n6, i + 1, h.data(), n6))) return rc;
-    if ((rc = B.dots(S.KQ.p, n6, i + 1, w, n6, h2.data()))) return rc;
-    if ((rc = B.sub_combination(w, S.Q.p, n6, i + 1, h2.data(), n6))) return rc;
-    alpha.push_back(h[i] + h2[i]);
-    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, w, kw, m.stream))) return rc;
     m.launches++;
-    double b2 = B.dot(w, kw, n6);
-    double b = sqrt(std::max(b2, 0.0));
-    if (!(b > 0.0) || !std::isfinite(b)) return fail(A2DS_ERR_BREAKDOWN, "Lanczos breakdown");
-    beta.push_back(b);
-    B.scale(w, 1.0 / b, n6);
-    B.scale(kw, 1.0 / b, n6);
-    m_iter = i + 1;
-    last_beta = b;
-    if (m_iter < nev) continue;
-    // Ritz values of the tridiagonal T (m_iter x m_iter)
-    std::vector<double> T((size_t)m_iter * m_iter, 0.0);
-    for (int k = 0; k < m_iter; k++) {
-      T[(size_t)k * m_iter + k] = alpha[k];
-      if (k + 1 < m_iter) T[(size_t)k * m_iter + k + 1] = T[(size_t)(k + 1) * m_iter + k] = beta[k];
-    }
-    jacobi_eig(m_iter, T, Tw, TV);
-    // lambda = -mu sigma / (1 - mu); sort by |lambda|
-    order.resize(m_iter);
-    for (int k = 0; k < m_iter; k++) order[k] = k;
-    auto lamof = [&](double mu) { return -mu * S.sigma / (1.0 - mu); };
+    if ((rc = cholqr2(m, S, W, KW, p, Bj))) return rc;  // synchronises: h1, h2 are ready
+    // T: diagonal block j (symmetrised), sub/super-diagonal blocks from B_j
+    for (int a = 0; a < p; a++)
+      for (int b = 0; b < p; b++) {
+        const double v = 0.5 * (h1[(size_t)a * p + b] + h2[(size_t)a * p + b] +
+                                h1[(size_t)b * p + a] + h2[(size_t)b * p + a]);
+        T[(size_t)(j * p + a) * tdim + j * p + b] = v;
+        T[(size_t)((j + 1) * p + a) * tdim + j * p + b] = Bj[(size_t)a * p + b];
+        T[(size_t)(j * p + b) * tdim + (j + 1) * p + a] = Bj[(size_t)a * p + b];
+      }
+    nsteps = j + 1;
+    mdim = nsteps * p;
+    lastB = Bj;
+    if (mdim < nev) continue;
+    // Ritz values of the leading mdim x mdim block of T
+    Tm.assign((size_t)mdim * mdim, 0.0);
+    for (int a = 0; a < mdim; a++)
+      for (int b = 0; b < mdim; b++) Tm[(size_t)a * mdim + b] = T[(size_t)a * tdim + b];
+    if (sym_eig(mdim, Tm, Tw, TV)) return fail(A2DS_ERR_NUMERIC, "tridiagonal eigensolver failed");
+    order.resize(mdim);
+    for (int k = 0; k < mdim; k++) order[k] = k;
     std::sort(order.begin(), order.end(),
               [&](int a, int c) { return fabs(lamof(Tw[a])) < fabs(lamof(Tw[c])); });
     converged = 1;
     for (int k = 0; k < nev; k++) {
-      int idx = order[k];
-      double est = fabs(b * TV[(size_t)(m_iter - 1) * m_iter + idx]);
-      if (!(est <= opts->eig_tol * fabs(Tw[idx]))) {
+      const int idx = order[k];
+      // residual estimate ||B_j y_j||, y_j = last p entries of the Ritz vector
+      double est2 = 0.0;
+      for (int a = 0; a < p; a++) {
+        double s = 0.0;
+        for (int b = 0; b < p; b++)
+          s += Bj[(size_t)a * p + b] * TV[(size_t)(j * p + b) * mdim + idx];
+        est2 += s * s;
+      }
+      if (!(sqrt(est2) <= opts->eig_tol * fabs(Tw[idx]))) {
         converged = 0;
         break;
       }
@@ -638,37 +811,40 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   }
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   double t_lan = now() - ta;
-  (void)last_beta;
-  if (!converged) {
-    // fill what we have, report non-convergence
-  }
-  // eigenvalues, eigenvectors phi = Q y, residual check ||K phi + lam G phi|| / ||K phi||
+  if (mdim < nev || order.empty()) return fail(A2DS_ERR_NOCONV, "Lanczos produced too few vectors");
+
+  // eigenvalues; eigenvectors phi = Q y; residual ||K phi + lam G phi|| / ||K phi||
   S.lam.assign(nev, 0.0);
   S.err.assign(nev, 0.0);
-  S.phi_ritz.assign((size_t)nev * m_iter, 0.0);
-  for (int k = 0; k < nev && k < m_iter; k++) {
-    int idx = order[k];
-    double mu = Tw[idx];
-    double lam = -mu * S.sigma / (1.0 - mu);
-    S.lam[k] = lam;
-    std::vector<double> y(m_iter);
-    for (int j = 0; j < m_iter; j++) y[j] = TV[(size_t)j * m_iter + idx];
-    for (int j = 0; j < m_iter; j++) S.phi_ritz[(size_t)k * m_iter + j] = y[j];
-    // phi = sum_j y_j q_j  (w <- 0; w -= sum (-y_j) q_j)
-    A2DS_CUDA_TRY(cudaMemsetAsync(S.w.p, 0, n6 * sizeof(double), m.stream));
-    for (int j = 0; j < m_iter; j++) y[j] = -y[j];
-    if ((rc = B.sub_combination(S.w.p, S.Q.p, n6, m_iter, y.data(), n6))) return rc;
-    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, S.w.p, S.r.p, m.stream))) return rc;
-    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, S.w.p, S.t.p, m.stream))) return rc;
+  S.ritz.assign((size_t)mdim * nev, 0.0);
+  for (int k = 0; k < nev; k++) {
+    const int idx = order[k];
+    S.lam[k] = lamof(Tw[idx]);
+    for (int j = 0; j < mdim; j++) S.ritz[(size_t)j * nev + k] = TV[(size_t)j * mdim + idx];
+  }
+  {
+    DBuf<double> dC;
+    if ((rc = dC.upload(S.ritz.data(), S.ritz.size(), m.stream))) return rc;
+    if ((rc = blk_combine(S.Q.p, nsteps, bs, p, dC.p, nev, n6, S.phi.p, m.stream))) return rc;
+    m.launches++;
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  }
+  for (int k = 0; k < nev; k++) {
+    double *phik = S.phi.p + (size_t)k * n6;
+    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, phik, S.r.p, m.stream))) return rc;
+    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, phik, S.t.p, m.stream))) return rc;
     m.launches += 2;
-    zero_bc(S.r.p);
-    zero_bc(S.t.p);
+    if (nbc) {
+      k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.r.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
+      k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.t.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
+      m.launches += 2;
+    }
     double kn = sqrt(B.dot(S.r.p, S.r.p, n6));
-    B.axpby(S.r.p, lam, S.t.p, 1.0, n6);
+    B.axpby(S.r.p, S.lam[k], S.t.p, 1.0, n6);
     double rn = sqrt(B.dot(S.r.p, S.r.p, n6));
     S.err[k] = kn > 0 ? rn / kn : rn;
     if (eigvecs) {
-      if ((rc = m.from_rows(S.w.p, eigvecs + (size_t)k * n6))) return rc;
+      if ((rc = m.from_rows(phik, eigvecs + (size_t)k * n6))) return rc;
     }
   }
   for (int k = 0; k < nev; k++) {
@@ -676,7 +852,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     if (errors) errors[k] = S.err[k];
   }
   if (path_out && (rc = m.from_rows(S.path.p, path_out))) return rc;
-  S.niters = m_iter;
+  S.nconv = converged ? nev : 0;
   A2DS_CUDA_TRY(cudaEventRecord(S.ev[1], m.stream));
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   double total = now() - t0;
@@ -684,9 +860,10 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   cudaEventElapsedTime(&ms_solve, S.ev[0], S.ev[1]);
   cudaEventElapsedTime(&ms_fa, S.ev[2], S.ev[3]);
   cudaEventElapsedTime(&ms_fk, S.ev[4], S.ev[5]);
-  m.stats = {total, t_k, t_g, t_fk + t_fa, t_path, t_lan, (double)m_iter, (double)inner,
+  m.stats = {total, t_k, t_g, t_fk + t_fa, t_path, t_lan, (double)mdim, (double)inner,
              (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
-             (double)S.fa.nnzb(), (double)S.fa.flv.nlevels, (double)S.fa.flops()};
+             (double)S.fa.nnzb(), (double)S.fa.flv.nlevels, (double)S.fa.flops(), (double)p,
+             (double)nsteps};
   if (!converged) return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
   return 0;
 }

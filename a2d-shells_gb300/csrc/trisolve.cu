@@ -1,0 +1,374 @@
+// Block triangular solves with the LU / ILU(k) factor for R right-hand
+// sides at once, and CUDA-graph replay of a whole solve.
+//
+// Numerics follow BCSRMatApplyLower6 / BCSRMatApplyUpper6
+// (src/bpmat/BCSRMatMult6.cpp:319-416): unit-lower forward substitution
+// y_i = x_i - sum_{k<i} L_ik y_k, then backward substitution
+// y_i = D_i^{-1} (y_i - sum_{k>i} U_ik y_k) with the stored inverse diagonal.
+//
+// Vectors hold R right-hand sides row-major: entry (row, dof, rhs) at
+// (row * 6 + dof) * R + rhs, so one factor block is loaded once and applied
+// to all R vectors.  Rows of the head (levels with many rows) are solved one
+// warp per row (five 6-lane groups stride over the row's blocks), narrow
+// levels one 256-thread block per row, and the dense tail column-oriented
+// (each final pivot pushes its column into later rows with FP64 atomics).
+// A solve is ~3,800 dependent launches at 256x512; solve_graph() captures
+// the whole sequence once per (factor, x, y, R) and replays it.
+#include "a2ds_internal.h"
+#include "ilu.h"
+
+namespace a2ds {
+
+constexpr int NARROW_LEVEL = 48;  // levels with fewer rows solve block-per-row
+
+// Partial sums of sum_k F_k[ii][:] y[fcols[k]] over k = kb + g, kb + g + step, ...
+template <typename T, typename TV, int R>
+__device__ __forceinline__ void row_partial(int kb, int ke, int g, int step, int ii,
+                                            const int *__restrict__ fcols,
+                                            const T *__restrict__ F, const TV *y, TV (&acc)[R]) {
+  for (int k = kb + g; k < ke; k += step) {
+    const T *a = F + (size_t)k * 36 + 6 * ii;
+    TV av[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) av[c] = (TV)a[c];
+    const TV *yv = y + (size_t)fcols[k] * 6 * R;
+#pragma unroll
+    for (int c = 0; c < 6; c++)
+#pragma unroll
+      for (int r = 0; r < R; r++) acc[r] += av[c] * yv[c * R + r];
+  }
+}
+
+// Forward substitution, one warp per row of a level.
+template <typename T, typename TV, int R>
+__global__ void __launch_bounds__(256) k_lower_warp(const int *__restrict__ rows, int nrows,
+                                                    const int *__restrict__ frowp,
+                                                    const int *__restrict__ fcols,
+                                                    const int *__restrict__ fdiag,
+                                                    const T *__restrict__ F, const TV *x, TV *y) {
+  __shared__ TV part[8][30][R];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wr = blockIdx.x * 8 + wib;
+  if (wr >= nrows) return;  // whole warp leaves together
+  const int i = rows[wr];
+  const int g = lane / 6, ii = lane - 6 * g;
+  TV acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = 0;
+  if (lane < 30) row_partial<T, TV, R>(frowp[i], fdiag[i], g, 5, ii, fcols, F, y, acc);
+  if (lane < 30)
+#pragma unroll
+    for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
+  __syncwarp();
+  for (int o = lane; o < 6 * R; o += 32) {
+    const int d = o / R, r = o - R * d;
+    TV v = part[wib][d][r] + part[wib][d + 6][r] + part[wib][d + 12][r] + part[wib][d + 18][r] +
+           part[wib][d + 24][r];
+    const size_t idx = ((size_t)i * 6 + d) * R + r;
+    y[idx] = x[idx] - v;
+  }
+}
+
+// Backward substitution, one warp per row of a level.
+template <typename T, typename TV, int R>
+__global__ void __launch_bounds__(256) k_upper_warp(const int *__restrict__ rows, int nrows,
+                                                    const int *__restrict__ frowp,
+                                                    const int *__restrict__ fcols,
+                                                    const int *__restrict__ fdiag,
+                                                    const T *__restrict__ F, TV *y) {
+  __shared__ TV part[8][30][R];
+  __shared__ TV z[8][6][R];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wr = blockIdx.x * 8 + wib;
+  if (wr >= nrows) return;
+  const int i = rows[wr];
+  const int g = lane / 6, ii = lane - 6 * g;
+  TV acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = 0;
+  if (lane < 30) row_partial<T, TV, R>(fdiag[i] + 1, frowp[i + 1], g, 5, ii, fcols, F, y, acc);
+  if (lane < 30)
+#pragma unroll
+    for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
+  __syncwarp();
+  for (int o = lane; o < 6 * R; o += 32) {
+    const int d = o / R, r = o - R * d;
+    TV v = part[wib][d][r] + part[wib][d + 6][r] + part[wib][d + 12][r] + part[wib][d + 18][r] +
+           part[wib][d + 24][r];
+    z[wib][d][r] = y[((size_t)i * 6 + d) * R + r] - v;
+  }
+  __syncwarp();
+  const T *Dinv = F + (size_t)fdiag[i] * 36;
+  for (int o = lane; o < 6 * R; o += 32) {
+    const int d = o / R, r = o - R * d;
+    TV v = 0;
+#pragma unroll
+    for (int c = 0; c < 6; c++) v += (TV)Dinv[6 * d + c] * z[wib][c][r];
+    y[((size_t)i * 6 + d) * R + r] = v;
+  }
+}
+
+// Long rows of narrow levels: one 256-thread block per row, 42 groups of
+// six threads stride over the row's blocks.
+template <typename T, typename TV, int R, bool UPPER>
+__global__ void __launch_bounds__(256) k_tri_block(const int *__restrict__ rows, int nrows,
+                                                   const int *__restrict__ frowp,
+                                                   const int *__restrict__ fcols,
+                                                   const int *__restrict__ fdiag,
+                                                   const T *__restrict__ F, const TV *x, TV *y) {
+  __shared__ TV part[252][R];
+  __shared__ TV z[6][R];
+  const int rr = blockIdx.x;
+  if (rr >= nrows) return;
+  const int i = rows[rr];
+  const int t = threadIdx.x;
+  const int g = t / 6, ii = t - 6 * g;
+  const int kb = UPPER ? fdiag[i] + 1 : frowp[i];
+  const int ke = UPPER ? frowp[i + 1] : fdiag[i];
+  if (t < 252) {
+    TV acc[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = 0;
+    row_partial<T, TV, R>(kb, ke, g, 42, ii, fcols, F, y, acc);
+#pragma unroll
+    for (int r = 0; r < R; r++) part[t][r] = acc[r];
+  }
+  __syncthreads();
+  for (int o = t; o < 6 * R; o += blockDim.x) {
+    const int d = o / R, r = o - R * d;
+    TV v = 0;
+    for (int gg = 0; gg < 42; gg++) v += part[6 * gg + d][r];
+    const size_t idx = ((size_t)i * 6 + d) * R + r;
+    if (UPPER)
+      z[d][r] = y[idx] - v;
+    else
+      y[idx] = x[idx] - v;
+  }
+  if (!UPPER) return;
+  __syncthreads();
+  const T *Dinv = F + (size_t)fdiag[i] * 36;
+  for (int o = t; o < 6 * R; o += blockDim.x) {
+    const int d = o / R, r = o - R * d;
+    TV v = 0;
+#pragma unroll
+    for (int c = 0; c < 6; c++) v += (TV)Dinv[6 * d + c] * z[c][r];
+    y[((size_t)i * 6 + d) * R + r] = v;
+  }
+}
+
+// ------------------------------------------------------ dense-tail solves
+// Rows [s, n) are the trailing separators, where levels hold a handful of
+// long rows.  Their head couplings are pulled once; then, tail level by tail
+// level, the columns of final pivots are pushed into the later rows.
+
+// y_i = x_i - sum_{j < s} L_ij y_j for every tail row i (one warp per row).
+template <typename T, typename TV, int R>
+__global__ void __launch_bounds__(256) k_tail_pull(int s, int d, const int *__restrict__ frowp,
+                                                   const int *__restrict__ fcols,
+                                                   const int *__restrict__ lsplit,
+                                                   const T *__restrict__ F, const TV *x, TV *y) {
+  __shared__ TV part[8][30][R];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rr = blockIdx.x * 8 + wib;
+  if (rr >= d) return;
+  const int i = s + rr;
+  const int g = lane / 6, ii = lane - 6 * g;
+  TV acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = 0;
+  if (lane < 30) row_partial<T, TV, R>(frowp[i], lsplit[rr], g, 5, ii, fcols, F, y, acc);
+  if (lane < 30)
+#pragma unroll
+    for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
+  __syncwarp();
+  for (int o = lane; o < 6 * R; o += 32) {
+    const int dd = o / R, r = o - R * dd;
+    TV v = part[wib][dd][r] + part[wib][dd + 6][r] + part[wib][dd + 12][r] +
+           part[wib][dd + 18][r] + part[wib][dd + 24][r];
+    const size_t idx = ((size_t)i * 6 + dd) * R + r;
+    y[idx] = x[idx] - v;
+  }
+}
+
+// One tail level's column pushes; thread (entry e, rhs r).  Entry e is
+// (target row i, factor position p, pivot row j).  Lower: y_i -= L_ij y_j.
+// Upper: y_i -= U_ij D_j^{-1} y_j (y_j itself is scaled by D_j^{-1} only
+// after all tail levels, by k_tail_finalize).
+template <typename T, typename TV, int R, bool UPPER>
+__global__ void __launch_bounds__(256) k_tail_push(const int *__restrict__ erow,
+                                                   const int *__restrict__ epos,
+                                                   const int *__restrict__ ecol, int ne,
+                                                   const int *__restrict__ fdiag,
+                                                   const T *__restrict__ F, TV *y) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = t / R, r = t - R * (t / R);
+  if (e >= ne) return;
+  const int i = erow[e], p = epos[e], j = ecol[e];
+  const T *A = F + (size_t)p * 36;
+  TV w[6];
+#pragma unroll
+  for (int b = 0; b < 6; b++) w[b] = y[((size_t)j * 6 + b) * R + r];
+  if (UPPER) {
+    const T *Dinv = F + (size_t)fdiag[j] * 36;
+    TV v[6];
+#pragma unroll
+    for (int a = 0; a < 6; a++) {
+      TV acc = 0;
+#pragma unroll
+      for (int b = 0; b < 6; b++) acc += (TV)Dinv[6 * a + b] * w[b];
+      v[a] = acc;
+    }
+#pragma unroll
+    for (int a = 0; a < 6; a++) w[a] = v[a];
+  }
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    TV acc = 0;
+#pragma unroll
+    for (int b = 0; b < 6; b++) acc += (TV)A[6 * a + b] * w[b];
+    atomicAdd(&y[((size_t)i * 6 + a) * R + r], -acc);
+  }
+}
+
+// y_j = D_j^{-1} z_j for every tail row; thread (row, rhs).
+template <typename T, typename TV, int R>
+__global__ void k_tail_finalize(int s, int d, const int *__restrict__ fdiag,
+                                const T *__restrict__ F, TV *y) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int rr = t / R, r = t - R * (t / R);
+  if (rr >= d) return;
+  const int j = s + rr;
+  const T *Dinv = F + (size_t)fdiag[j] * 36;
+  TV z[6];
+#pragma unroll
+  for (int b = 0; b < 6; b++) z[b] = y[((size_t)j * 6 + b) * R + r];
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    TV v = 0;
+#pragma unroll
+    for (int b = 0; b < 6; b++) v += (TV)Dinv[6 * a + b] * z[b];
+    y[((size_t)j * 6 + a) * R + r] = v;
+  }
+}
+
+// ------------------------------------------------------------ launchers
+template <typename T, typename TV, int R>
+static int solve_levels_r(const Factor &f, const T *F, const TV *x, TV *y, cudaStream_t s,
+                          long long *launches) {
+  const LevelSchedule &Lo = f.lower, &Up = f.upper;
+  long long nl = 0;
+  for (int lv = 0; lv < Lo.nlevels; lv++) {
+    const int cnt = Lo.ptr[lv + 1] - Lo.ptr[lv];
+    if (cnt < NARROW_LEVEL)
+      k_tri_block<T, TV, R, false><<<cnt, 256, 0, s>>>(Lo.d_rows.p + Lo.ptr[lv], cnt,
+                                                       f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
+                                                       x, y);
+    else
+      k_lower_warp<T, TV, R><<<(cnt + 7) / 8, 256, 0, s>>>(Lo.d_rows.p + Lo.ptr[lv], cnt,
+                                                           f.d_frowp.p, f.d_fcols.p,
+                                                           f.d_fdiag.p, F, x, y);
+    nl++;
+  }
+  const int ts = f.tail_s, d = f.n - f.tail_s;
+  if (d > 0) {
+    k_tail_pull<T, TV, R><<<(d + 7) / 8, 256, 0, s>>>(ts, d, f.d_frowp.p, f.d_fcols.p,
+                                                      f.d_lsplit.p, F, x, y);
+    nl++;
+    for (size_t lv = 0; lv + 1 < f.tl_ptr.size(); lv++) {
+      const int e0 = f.tl_ptr[lv], ne = f.tl_ptr[lv + 1] - e0;
+      if (ne <= 0) continue;
+      k_tail_push<T, TV, R, false><<<(ne * R + 255) / 256, 256, 0, s>>>(
+          f.d_tl_row.p + e0, f.d_tl_pos.p + e0, f.d_tl_col.p + e0, ne, f.d_fdiag.p, F, y);
+      nl++;
+    }
+    for (size_t lv = 0; lv + 1 < f.tu_ptr.size(); lv++) {
+      const int e0 = f.tu_ptr[lv], ne = f.tu_ptr[lv + 1] - e0;
+      if (ne <= 0) continue;
+      k_tail_push<T, TV, R, true><<<(ne * R + 255) / 256, 256, 0, s>>>(
+          f.d_tu_row.p + e0, f.d_tu_pos.p + e0, f.d_tu_col.p + e0, ne, f.d_fdiag.p, F, y);
+      nl++;
+    }
+    k_tail_finalize<T, TV, R><<<(d * R + 127) / 128, 128, 0, s>>>(ts, d, f.d_fdiag.p, F, y);
+    nl++;
+  }
+  for (int lv = 0; lv < Up.nlevels; lv++) {
+    const int cnt = Up.ptr[lv + 1] - Up.ptr[lv];
+    if (cnt < NARROW_LEVEL)
+      k_tri_block<T, TV, R, true><<<cnt, 256, 0, s>>>(Up.d_rows.p + Up.ptr[lv], cnt,
+                                                      f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
+                                                      y, y);
+    else
+      k_upper_warp<T, TV, R><<<(cnt + 7) / 8, 256, 0, s>>>(Up.d_rows.p + Up.ptr[lv], cnt,
+                                                           f.d_frowp.p, f.d_fcols.p,
+                                                           f.d_fdiag.p, F, y);
+    nl++;
+  }
+  if (launches) *launches += nl;
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+template <typename T, typename TV>
+int solve_levels(const Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
+                 long long *launches) {
+  switch (nrhs) {
+    case 1: return solve_levels_r<T, TV, 1>(f, F, x, y, s, launches);
+    case 2: return solve_levels_r<T, TV, 2>(f, F, x, y, s, launches);
+    case 4: return solve_levels_r<T, TV, 4>(f, F, x, y, s, launches);
+    case 8: return solve_levels_r<T, TV, 8>(f, F, x, y, s, launches);
+    case 16: return solve_levels_r<T, TV, 16>(f, F, x, y, s, launches);
+    default: return fail(A2DS_ERR_ARG, "solve: nrhs must be 1, 2, 4, 8 or 16");
+  }
+}
+
+template <typename T, typename TV>
+int solve_graph(Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
+                long long *launches) {
+  for (const SolveGraph &g : f.graphs)
+    if (g.F == (const void *)F && g.x == (const void *)x && g.y == (void *)y &&
+        g.nrhs == nrhs && g.tv_size == (int)sizeof(TV)) {
+      A2DS_CUDA_TRY(cudaGraphLaunch(g.exec, s));
+      if (launches) *launches += g.nlaunch;
+      return 0;
+    }
+  long long nl = 0;
+  cudaGraph_t graph = nullptr;
+  A2DS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = solve_levels<T, TV>(f, F, x, y, nrhs, s, &nl);
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess || !graph)
+    return fail(A2DS_ERR_CUDA, std::string("solve graph capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess)
+    return fail(A2DS_ERR_CUDA, std::string("solve graph instantiate: ") + cudaGetErrorString(e));
+  if (f.graphs.size() >= 8) {
+    cudaGraphExecDestroy(f.graphs.front().exec);
+    f.graphs.erase(f.graphs.begin());
+  }
+  f.graphs.push_back(SolveGraph{F, x, y, nrhs, (int)sizeof(TV), exec, nl});
+  A2DS_CUDA_TRY(cudaGraphLaunch(exec, s));
+  if (launches) *launches += nl;
+  return 0;
+}
+
+Factor::~Factor() {
+  for (SolveGraph &g : graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+}
+
+template int solve_levels<double, double>(const Factor &, const double *, const double *, double *,
+                                          int, cudaStream_t, long long *);
+template int solve_levels<float, float>(const Factor &, const float *, const float *, float *, int,
+                                        cudaStream_t, long long *);
+template int solve_graph<double, double>(Factor &, const double *, const double *, double *, int,
+                                         cudaStream_t, long long *);
+template int solve_graph<float, float>(Factor &, const float *, const float *, float *, int,
+                                       cudaStream_t, long long *);
+
+}  // namespace a2ds

@@ -218,12 +218,15 @@ typedef struct {
   int gmres_restarts;    /* GMRES restarts */
   double gmres_rtol;     /* GMRES relative tolerance */
   double gmres_atol;     /* GMRES absolute tolerance */
-  int precision;         /* 64: all-FP64; 32: FP32 factor + FP64 GMRES-IR */
+  int precision;         /* 64: all-FP64; 32: FP32 factor + FP64 refinement */
   int seed;              /* Lanczos start vector seed */
+  int block_size;        /* Lanczos block size p in {1, 2, 4, 8, 16}: p vectors
+                            per shift-invert solve (1 = the reference's
+                            single-vector Lanczos) */
 } a2ds_buckling_opts;
 
 /* Fills opts with the defaults (sigma = 0, 100 vectors, 10 eigenvalues,
-   tol 1e-10, complete LU, GMRES(30, 15) at 1e-12, FP64). */
+   tol 1e-10, complete LU, GMRES(30, 15) at 1e-12, FP64, block size 8). */
 void a2ds_buckling_default_opts(a2ds_buckling_opts *opts);
 
 /* TACSLinearBuckling::solve(rhs, NULL) (src/TACSBuckling.cpp:197-278) and
@@ -239,7 +242,9 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts,
 
 /* Timings and counters of the last a2ds_buckling_solve on this mesh:
    fills up to n doubles {total_s, assemble_k_s, assemble_g_s, factor_s,
-   path_s, lanczos_s, lanczos_iters, inner_iters, kernel_launches}. */
+   path_s, lanczos_s, lanczos_vectors, inner_iters, kernel_launches,
+   solve_event_ms, factor_a_event_ms, factor_k_event_ms, factor_nnzb,
+   factor_levels, factor_flops, block_size, block_iters}. */
 int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out);
 
 /* ---------------------------------------------- eigenvalue sensitivities
