@@ -344,7 +344,7 @@ class SchurPc:
 STAT_NAMES = ["total_s", "assemble_k_s", "assemble_g_s", "factor_s", "path_s", "lanczos_s",
               "lanczos_vectors", "inner_iters", "kernel_launches", "solve_event_ms",
               "factor_a_event_ms", "factor_k_event_ms", "factor_nnzb", "factor_levels",
-              "factor_flops", "block_size", "block_iters"]
+              "factor_flops", "block_size", "block_iters", "trisolve_ms", "trisolve_calls"]
 
 
 class LinearBuckling:

@@ -1,0 +1,521 @@
+// Numeric block LU / ILU(k) factorization of 6x6-block CSR matrices on the
+// GPU, level-scheduled and right-looking, in FP64, FP32 or "df64"
+// (double-float: an unevaluated sum of two FP32 numbers, ~48-bit mantissa,
+// computed on the FP32 pipe).
+//
+// Numerics follow BCSRMatFactor6 (src/bpmat/BCSRMatFact6.cpp:946-1330):
+// every L block becomes L_ij = A_ij D_j^{-1}, the row is updated with
+// -L_ij U_jk on the factor pattern, and each diagonal block is replaced by
+// its inverse (partial pivoting, as BMatComputeInverse,
+// src/bpmat/BCSRMatMult.cpp:308).
+//
+// Why df64: on GB300 the FP64 pipe runs at ~1/58 of FP32 (about 1.75 DFMA
+// per clock per SM), and the factorization is bound by it.  A df64
+// multiply-subtract costs ~12 FP32 instructions, so the update runs several
+// times faster on the FP32 pipe, with a rounding unit of ~2^-48 instead of
+// 2^-53; the factor is converted to FP64 afterwards and every solve that
+// uses it is FP64 with FP64 iterative refinement.
+//
+// Schedule: rows are grouped by dependency level.  For level l,
+// (1) k_factor_pivot inverts the diagonal blocks of the level's rows (final
+// once every lower level has been applied), (2) k_factor_lcol forms every
+// L_ij = A_ij D_j^{-1} with j in level l, (3) the update kernels process one
+// task per target row i with L entries in level-l columns and apply
+// -L_ij U_j* to row i.  Pivots of one level never update each other's rows
+// or L entries, and one task owns its target row, so no atomics are needed.
+// Six threads share each 6x6 block update (one output column each).  Long
+// rows: one 384-thread CTA per task.  Short rows: a group of 6, 12 or 30
+// lanes per task within a warp, sized to the level's U-row lengths.
+#include "a2ds_internal.h"
+#include "ilu.h"
+
+namespace a2ds {
+
+struct __align__(8) df64 {
+  float hi, lo;
+};
+
+// ------------------------------------------------------------ value types
+template <typename T>
+struct Traits;
+template <>
+struct Traits<double> {
+  using C = double;  // type of the pivot inverse arithmetic
+};
+template <>
+struct Traits<float> {
+  using C = float;
+};
+template <>
+struct Traits<df64> {
+  using C = double;
+};
+
+__device__ __forceinline__ double to_c(double v) { return v; }
+__device__ __forceinline__ float to_c(float v) { return v; }
+__device__ __forceinline__ double to_c(df64 v) { return (double)v.hi + (double)v.lo; }
+
+template <typename T>
+__device__ __forceinline__ T from_f64(double v);
+template <>
+__device__ __forceinline__ double from_f64<double>(double v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ float from_f64<float>(double v) {
+  return (float)v;
+}
+template <>
+__device__ __forceinline__ df64 from_f64<df64>(double v) {
+  const float h = __double2float_rn(v);
+  return df64{h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ double from_c(double v, double *) { return v; }
+__device__ __forceinline__ float from_c(float v, float *) { return v; }
+__device__ __forceinline__ df64 from_c(double v, df64 *) { return from_f64<df64>(v); }
+
+// --------------------------------------------------------- df64 arithmetic
+// (hi, lo) -= a b: the FP32 product a.hi b.hi with its exact error (FMA),
+// cross terms in FP32, Knuth's two-sum for the leading parts, and the
+// low-order terms gathered in lo.  The _rn intrinsics keep the compiler from
+// fusing the two-sum's operations into FMAs, which would break its exactness.
+__device__ __forceinline__ void df_sub_prod(float &hi, float &lo, df64 a, df64 b) {
+  const float ph = __fmul_rn(a.hi, b.hi);
+  float pe = fmaf(a.hi, b.hi, -ph);
+  pe = fmaf(a.hi, b.lo, pe);
+  pe = fmaf(a.lo, b.hi, pe);
+  const float s = __fsub_rn(hi, ph);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(-ph, bb));
+  hi = s;
+  lo = __fadd_rn(lo, __fsub_rn(err, pe));
+}
+__device__ __forceinline__ df64 df_norm(float hi, float lo) {
+  const float s = __fadd_rn(hi, lo);
+  return df64{s, __fsub_rn(lo, __fsub_rn(s, hi))};
+}
+
+// ------------------------------------------------------- 6x6 block kernels
+// Entry e = 6 a + b of A B (L_ij = A_ij D_j^{-1}).
+__device__ __forceinline__ double blk_mul_entry(const double *A, const double *B, int e) {
+  const int a = e / 6, b = e - 6 * (e / 6);
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 6; k++) s += A[6 * a + k] * B[6 * k + b];
+  return s;
+}
+__device__ __forceinline__ float blk_mul_entry(const float *A, const float *B, int e) {
+  const int a = e / 6, b = e - 6 * (e / 6);
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 6; k++) s += A[6 * a + k] * B[6 * k + b];
+  return s;
+}
+__device__ __forceinline__ df64 blk_mul_entry(const df64 *A, const df64 *B, int e) {
+  const int a = e / 6, b = e - 6 * (e / 6);
+  float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const df64 x = A[6 * a + k];
+    df_sub_prod(hi, lo, df64{-x.hi, -x.lo}, B[6 * k + b]);
+  }
+  return df_norm(hi, lo);
+}
+
+// ------------------------------------------------------------- scatter
+// F <- pattern-embedded copy of A (+ alpha2 A2), zero elsewhere; one warp per row.
+template <typename T>
+__global__ void k_scatter_into_factor(int n, const int *__restrict__ rowp,
+                                      const int *__restrict__ cols, const double *__restrict__ A,
+                                      const double *__restrict__ A2, double alpha2,
+                                      const int *__restrict__ frowp, const int *__restrict__ fcols,
+                                      T *__restrict__ F) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const int i = warp;
+  const int fs = frowp[i], fe = frowp[i + 1];
+  for (int idx = lane; idx < (fe - fs) * 36; idx += 32) F[(size_t)fs * 36 + idx] = from_f64<T>(0.0);
+  __syncwarp();
+  const int s = rowp[i], e = rowp[i + 1];
+  for (int jp = s; jp < e; jp++) {
+    const int c = cols[jp];
+    int lo = fs, hi = fe - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (fcols[mid] < c)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    for (int k = lane; k < 36; k += 32) {
+      double v = A[(size_t)jp * 36 + k];
+      if (A2) v += alpha2 * A2[(size_t)jp * 36 + k];
+      F[(size_t)lo * 36 + k] = from_f64<T>(v);
+    }
+  }
+}
+
+// ------------------------------------------------------------- pivots
+// Invert the diagonal blocks of one level in place (6x6 Gauss-Jordan with
+// partial pivoting, first maximum wins, as BMatComputeInverse).  Six lanes
+// per block, one row of M and of the inverse each; pivot search, row swap
+// and the pivot-row broadcast go through warp shuffles, so every value stays
+// in registers and a level's blocks spread over many SMs.  Arithmetic in
+// FP64 for FP64 and df64 factors, FP32 for FP32 factors.
+template <typename T>
+__global__ void __launch_bounds__(128) k_factor_pivot(const int *__restrict__ rows, int nrows,
+                                                      const int *__restrict__ fdiag,
+                                                      T *__restrict__ F, int *__restrict__ status) {
+  using C = typename Traits<T>::C;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp * 5 >= nrows) return;  // whole warp
+  const int sub = lane / 6, r = lane - 6 * (lane / 6);
+  const int idx = warp * 5 + sub;
+  const bool live = sub < 5 && idx < nrows;
+  const int base = sub < 5 ? 6 * sub : 0;
+  const int j = live ? rows[idx] : 0;
+  T *D = F + (size_t)(live ? fdiag[j] : 0) * 36;
+  C m[6], v[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    m[k] = live ? to_c(D[6 * r + k]) : C(0);
+    v[k] = (k == r) ? C(1) : C(0);
+  }
+  int fail = 0;
+#pragma unroll
+  for (int c = 0; c < 6; c++) {
+    C bv = C(-1);
+    int bp = c;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+      const C vq = __shfl_sync(full, fabs(m[c]), base + q);
+      if (q >= c && vq > bv) {
+        bv = vq;
+        bp = q;
+      }
+    }
+    if (bv == C(0) && !fail) fail = c + 1;  // singular; result unused
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const C mc = __shfl_sync(full, m[k], base + c), mp = __shfl_sync(full, m[k], base + bp);
+      const C vc = __shfl_sync(full, v[k], base + c), vp = __shfl_sync(full, v[k], base + bp);
+      if (r == c) {
+        m[k] = mp;
+        v[k] = vp;
+      } else if (r == bp) {
+        m[k] = mc;
+        v[k] = vc;
+      }
+    }
+    const C piv = __shfl_sync(full, m[c], base + c);
+    const C inv = piv != C(0) ? C(1) / piv : C(0);
+    if (r == c) {
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        m[k] *= inv;
+        v[k] *= inv;
+      }
+    }
+    C pm[6], pv[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      pm[k] = __shfl_sync(full, m[k], base + c);
+      pv[k] = __shfl_sync(full, v[k], base + c);
+    }
+    if (r != c) {
+      const C f = m[c];
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        m[k] -= f * pm[k];
+        v[k] -= f * pv[k];
+      }
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) D[6 * r + k] = from_c(v[k], (T *)nullptr);
+    if (fail && r == 0) atomicMax(status, j + 1);
+  }
+}
+
+// ------------------------------------------------------------- updates
+// Position of column c in cols[lo, hi) (sorted), or -1.
+__device__ __forceinline__ int find_col(const int *cols, int lo, int hi, int c) {
+  int h = hi - 1;
+  while (lo < h) {
+    const int mid = (lo + h) >> 1;
+    if (cols[mid] < c)
+      lo = mid + 1;
+    else
+      h = mid;
+  }
+  return (lo < hi && cols[lo] == c) ? lo : -1;
+}
+
+// L_ij = A_ij D_j^{-1} for every L entry of one level, in place; a CTA of
+// 288 threads handles 8 entries, thread (entry q, element e).  D_j^{-1} is
+// final (the level's pivot kernel ran), A_ij is final (every pivot that
+// updates it lies in a lower level), and the level's updates read the L
+// blocks only after this kernel.  All 36 threads of an entry are in one CTA,
+// so a barrier separates the reads of A_ij from the in-place writes.
+template <typename T>
+__global__ void __launch_bounds__(288) k_factor_lcol(const int *__restrict__ jps, int nq,
+                                                     const int *__restrict__ fcols,
+                                                     const int *__restrict__ fdiag,
+                                                     T *__restrict__ F) {
+  const int q = blockIdx.x * 8 + threadIdx.x / 36, e = threadIdx.x % 36;
+  const bool live = q < nq;
+  T v{};
+  size_t pos = 0;
+  if (live) {
+    const int jp = jps[q];
+    pos = (size_t)jp * 36;
+    v = blk_mul_entry(F + pos, F + (size_t)fdiag[fcols[jp]] * 36, e);
+  }
+  __syncthreads();
+  if (live) F[pos + e] = v;
+}
+
+// Column b of the target block: C[:, b] -= L U[:, b] (L in shared memory).
+// Six threads share one block update, thread b owning column b: the six
+// threads read each 48-byte row of U and C together (coalesced), and a
+// thread holds only 18 values, so many warps fit on an SM to hide the
+// memory latency of the scattered U and target blocks.
+__device__ __forceinline__ void blk_col_update(double *C, const double *L, const double *U,
+                                               int b) {
+  double u[6], c[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) u[k] = U[6 * k + b];
+#pragma unroll
+  for (int a = 0; a < 6; a++) c[a] = C[6 * a + b];
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 6; k++) s += L[6 * a + k] * u[k];
+    C[6 * a + b] = c[a] - s;
+  }
+}
+__device__ __forceinline__ void blk_col_update(float *C, const float *L, const float *U, int b) {
+  float u[6], c[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) u[k] = U[6 * k + b];
+#pragma unroll
+  for (int a = 0; a < 6; a++) c[a] = C[6 * a + b];
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) s += L[6 * a + k] * u[k];
+    C[6 * a + b] = c[a] - s;
+  }
+}
+__device__ __forceinline__ void blk_col_update(df64 *C, const df64 *L, const df64 *U, int b) {
+  df64 u[6], c[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) u[k] = U[6 * k + b];
+#pragma unroll
+  for (int a = 0; a < 6; a++) c[a] = C[6 * a + b];
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    float hi = c[a].hi, lo = c[a].lo;
+#pragma unroll
+    for (int k = 0; k < 6; k++) df_sub_prod(hi, lo, L[6 * a + k], u[k]);
+    C[6 * a + b] = df_norm(hi, lo);
+  }
+}
+
+// Long target rows: one 384-thread CTA per task (64 block updates at a
+// time, six threads each); every pivot's U blocks are strided over the
+// slots (a pivot's U columns are distinct, so no two slots touch one target
+// block), one barrier between pivots.  The row's column indices are staged
+// in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ task_row,
+                                                        const int *__restrict__ task_ptr,
+                                                        const int *__restrict__ task_jp,
+                                                        int ntasks, const int *__restrict__ frowp,
+                                                        const int *__restrict__ fcols,
+                                                        const int *__restrict__ fdiag,
+                                                        T *__restrict__ F) {
+  extern __shared__ int s_cols[];
+  __shared__ T s_L[36];
+  const int t = blockIdx.x;
+  if (t >= ntasks) return;
+  const int slot = threadIdx.x / 6, b = threadIdx.x - 6 * (threadIdx.x / 6);
+  const int nslots = blockDim.x / 6;
+  const int i = task_row[t];
+  const int rs = frowp[i], len = frowp[i + 1] - rs;
+  const bool staged = len <= FACTOR_CTA_COLS;
+  if (staged)
+    for (int k = threadIdx.x; k < len; k += blockDim.x) s_cols[k] = fcols[rs + k];
+  const int *cols = staged ? s_cols : fcols + rs;
+  for (int q = task_ptr[t]; q < task_ptr[t + 1]; q++) {
+    const int jp = task_jp[q];
+    const int j = fcols[jp];
+    if (threadIdx.x < 36) s_L[threadIdx.x] = F[(size_t)jp * 36 + threadIdx.x];
+    __syncthreads();  // s_L (and, first time, s_cols) ready
+    const int ue = frowp[j + 1], lo0 = jp + 1 - rs;
+    if (slot < nslots)
+#pragma unroll 1
+      for (int pu = fdiag[j] + 1 + slot; pu < ue; pu += nslots) {
+        // re-read s_L each block (cheap) rather than pinning 36 values in
+        // registers for the whole loop, which would halve the resident warps
+        asm volatile("" ::: "memory");
+        const int pos = find_col(cols, lo0, len, fcols[pu]);
+        if (pos >= 0) blk_col_update(F + (size_t)(rs + pos) * 36, s_L, F + (size_t)pu * 36, b);
+      }
+    __syncthreads();  // this pivot's updates done before the next pivot's
+  }
+}
+
+// Short target rows: a group of 6 S lanes per task inside one warp (S block
+// updates at a time; S = 1, 2 or 5 gives 5, 2 or 1 groups per warp, chosen
+// per level from the mean U-row length of its pivots); the task's pivots
+// are applied in order, each pivot's U blocks strided over the S slots.
+template <typename T, int S>
+__global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ task_row,
+                                                      const int *__restrict__ task_ptr,
+                                                      const int *__restrict__ task_jp,
+                                                      int ntasks, const int *__restrict__ frowp,
+                                                      const int *__restrict__ fcols,
+                                                      const int *__restrict__ fdiag,
+                                                      T *__restrict__ F) {
+  constexpr int G = 6 * S, GW = 32 / G;
+  __shared__ T s_L[8][GW][36];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gw = lane / G, gl = lane - G * (lane / G);
+  const int t = (blockIdx.x * 8 + wib) * GW + gw;
+  if (gw >= GW || t >= ntasks) return;  // spare lanes; whole groups past the end
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
+  const int slot = gl / 6, b = gl - 6 * (gl / 6);
+  const int i = task_row[t];
+  const int rs = frowp[i], len = frowp[i + 1] - rs;
+  const int *cols = fcols + rs;
+  T *L = s_L[wib][gw];
+  for (int q = task_ptr[t]; q < task_ptr[t + 1]; q++) {
+    const int jp = task_jp[q];
+    const int j = fcols[jp];
+    for (int e = gl; e < 36; e += G) L[e] = F[(size_t)jp * 36 + e];
+    __syncwarp(gmask);
+    const int ue = frowp[j + 1], lo0 = jp + 1 - rs;
+#pragma unroll 1
+    for (int pu = fdiag[j] + 1 + slot; pu < ue; pu += S) {
+      const int pos = find_col(cols, lo0, len, fcols[pu]);
+      if (pos >= 0) blk_col_update(F + (size_t)(rs + pos) * 36, L, F + (size_t)pu * 36, b);
+    }
+    __syncwarp(gmask);
+  }
+}
+
+// df64 factor values -> FP64, in place (same 8 bytes per value).
+__global__ void k_df64_to_f64(double *F, size_t n) {
+  df64 *D = reinterpret_cast<df64 *>(F);
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const df64 v = D[k];
+    F[k] = (double)v.hi + (double)v.lo;
+  }
+}
+
+// ------------------------------------------------------------ launchers
+template <typename T>
+static int scatter_t(int n, const int *rowp, const int *cols, const double *A, const double *A2,
+                     double alpha2, const int *frowp, const int *fcols, T *F, cudaStream_t s) {
+  k_scatter_into_factor<T><<<(n * 32 + 255) / 256, 256, 0, s>>>(n, rowp, cols, A, A2, alpha2,
+                                                               frowp, fcols, F);
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+template <typename T>
+static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long long *launches) {
+  const LevelSchedule &L = f.flv;
+  static bool configured = false;
+  const int smem = FACTOR_CTA_COLS * (int)sizeof(int);
+  if (!configured) {
+    A2DS_CUDA_TRY(cudaFuncSetAttribute(k_update_long<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured = true;
+  }
+  long long nl = 0;
+  for (int lv = 0; lv < L.nlevels; lv++) {
+    const int cnt = L.ptr[lv + 1] - L.ptr[lv];
+    k_factor_pivot<T><<<(cnt + 19) / 20, 128, 0, s>>>(L.d_rows.p + L.ptr[lv], cnt, f.d_fdiag.p, F,
+                                                      status);
+    nl++;
+    const int t0 = f.task_level_ptr[lv], nt = f.task_level_ptr[lv + 1] - t0;
+    if (nt <= 0) continue;
+    const int q0 = f.task_ptr[t0], nq = f.task_ptr[t0 + nt] - q0;
+    k_factor_lcol<T><<<(nq + 7) / 8, 288, 0, s>>>(f.d_task_jp.p + q0, nq, f.d_fcols.p,
+                                                  f.d_fdiag.p, F);
+    nl++;
+    const int nlong = f.task_nlong[lv], ns = nt - nlong;
+    if (nlong > 0) {
+      k_update_long<T><<<nlong, 384, smem, s>>>(f.d_task_row.p + t0, f.d_task_ptr.p + t0,
+                                                f.d_task_jp.p, nlong, f.d_frowp.p, f.d_fcols.p,
+                                                f.d_fdiag.p, F);
+      nl++;
+    }
+    if (ns > 0) {
+      const int S = f.task_group[lv], GW = 32 / (6 * S);
+      const int grid = (ns + 8 * GW - 1) / (8 * GW);
+      const int *tr = f.d_task_row.p + t0 + nlong, *tp = f.d_task_ptr.p + t0 + nlong;
+      if (S == 1)
+        k_update_group<T, 1><<<grid, 256, 0, s>>>(tr, tp, f.d_task_jp.p, ns, f.d_frowp.p,
+                                                  f.d_fcols.p, f.d_fdiag.p, F);
+      else if (S == 2)
+        k_update_group<T, 2><<<grid, 256, 0, s>>>(tr, tp, f.d_task_jp.p, ns, f.d_frowp.p,
+                                                  f.d_fcols.p, f.d_fdiag.p, F);
+      else
+        k_update_group<T, 5><<<grid, 256, 0, s>>>(tr, tp, f.d_task_jp.p, ns, f.d_frowp.p,
+                                                  f.d_fcols.p, f.d_fdiag.p, F);
+      nl++;
+    }
+  }
+  if (launches) *launches += nl;
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int factor_scatter(const Factor &f, int n, const int *rowp, const int *cols, const double *A,
+                   const double *A2, double alpha2, void *F, cudaStream_t s) {
+  switch (f.precision) {
+    case 64:
+      return scatter_t<double>(n, rowp, cols, A, A2, alpha2, f.d_frowp.p, f.d_fcols.p,
+                               (double *)F, s);
+    case 48:
+      return scatter_t<df64>(n, rowp, cols, A, A2, alpha2, f.d_frowp.p, f.d_fcols.p, (df64 *)F, s);
+    case 32:
+      return scatter_t<float>(n, rowp, cols, A, A2, alpha2, f.d_frowp.p, f.d_fcols.p, (float *)F,
+                              s);
+    default:
+      return fail(A2DS_ERR_ARG, "factor precision must be 64, 48 or 32");
+  }
+}
+
+int factor_levels(const Factor &f, void *F, int *status, cudaStream_t s, long long *launches) {
+  switch (f.precision) {
+    case 64:
+      return levels_t<double>(f, (double *)F, status, s, launches);
+    case 48: {
+      int rc = levels_t<df64>(f, (df64 *)F, status, s, launches);
+      if (rc) return rc;
+      const size_t n = (size_t)f.nnzb() * 36;
+      k_df64_to_f64<<<(int)std::min<size_t>((n + 255) / 256, 152 * 32), 256, 0, s>>>((double *)F,
+                                                                                     n);
+      if (launches) (*launches)++;
+      A2DS_CUDA_TRY(cudaGetLastError());
+      return 0;
+    }
+    case 32:
+      return levels_t<float>(f, (float *)F, status, s, launches);
+    default:
+      return fail(A2DS_ERR_ARG, "factor precision must be 64, 48 or 32");
+  }
+}
+
+}  // namespace a2ds

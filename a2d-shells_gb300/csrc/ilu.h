@@ -33,13 +33,24 @@ struct Factor {
   DBuf<float> F32;
   LevelSchedule flv;           // dependency levels of all rows (factorization)
   LevelSchedule lower, upper;  // head rows [0, tail_s): row-oriented solves
-  // right-looking update tasks, grouped by level
-  std::vector<int> task_level_ptr, task_row, task_ptr, task_jp;
+  // right-looking update tasks, grouped by level; within a level the tasks
+  // of long target rows (> FACTOR_WARP_COLS blocks) come first
+  std::vector<int> task_level_ptr, task_nlong, task_row, task_ptr, task_jp;
+  std::vector<int> task_group;  // block updates in flight per short task, per level (1, 2, 5)
   DBuf<int> d_task_row, d_task_ptr, d_task_jp;
   // dense tail rows [tail_s, n): head pull split and column push lists
   int tail_s = 0;
   std::vector<int> lsplit, tl_ptr, tl_row, tl_pos, tl_col, tu_ptr, tu_row, tu_pos, tu_col;
+  std::vector<int> td_row, td_pos, td_col;  // upper couplings of middle rows to dense columns
   DBuf<int> d_lsplit, d_tl_row, d_tl_pos, d_tl_col, d_tu_row, d_tu_pos, d_tu_col;
+  DBuf<int> d_td_row, d_td_pos, d_td_col;
+  // dense trailing block rows [dense_t0, n), dense_n = n - dense_t0 (a
+  // multiple of DENSE_PANEL, 0 = none): the factor's blocks there copied into
+  // a dense row-major (6 dense_n)^2 array, plus the inverses of its diagonal
+  // panels (unit-lower L and D + U, (6 DENSE_PANEL)^2 each)
+  int dense_t0 = 0, dense_n = 0;
+  DBuf<double> dense64, pinvL64, pinvU64, dwork64;
+  DBuf<float> dense32, pinvL32, pinvU32, dwork32;
   // algorithmic FP operations of one numeric factorization: 432 per L block
   // (L_ij = A_ij D_j^{-1}), 432 per block update, 432 per diagonal inverse
   double flop_count = 0.0;
@@ -58,16 +69,36 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev);
 // (column-oriented pushes) and build both schedules; lev = factor levels.
 void build_solve_schedule(Factor &f, const std::vector<int> &lev, int narrow);
 int upload_schedules(Factor &f, cudaStream_t s);
+// Allocate the dense-block buffers of f for its precision.
+int dense_alloc(Factor &f);
+// Copy the factored values of the dense block out of F and invert its
+// diagonal panels (after the numeric factorization).
+int dense_build(Factor &f, const void *F, cudaStream_t s, long long *launches);
 
-// F <- pattern-embedded copy of A (+ alpha2 * A2 when A2 != NULL), as T.
-template <typename T>
-int factor_scatter(int n, const int *rowp, const int *cols, const double *A, const double *A2,
-                   double alpha2, const int *frowp, const int *fcols, T *F, cudaStream_t s);
+// Update kernels: target rows with at most FACTOR_WARP_COLS blocks are
+// updated by a group of 6, 12 or 30 lanes, longer ones by one CTA (column
+// indices staged in shared memory up to FACTOR_CTA_COLS).
+constexpr int FACTOR_WARP_COLS = 512;
+constexpr int FACTOR_CTA_COLS = 10240;
+
+// Dense trailing block of the solves: panels of DENSE_PANEL block rows,
+// between DENSE_MIN and DENSE_MAX block rows, used when the factor fills at
+// least DENSE_MIN_FILL of it.
+constexpr int DENSE_PANEL = 32;
+constexpr int DENSE_MIN = 64;
+constexpr int DENSE_MAX = 2048;
+constexpr double DENSE_MIN_FILL = 0.4;
+
+// F (f.precision: 64 double, 48 double-float, 32 float values; 8 bytes per
+// value for 64 and 48) <- pattern-embedded copy of A (+ alpha2 * A2 when
+// A2 != NULL).
+int factor_scatter(const Factor &f, int n, const int *rowp, const int *cols, const double *A,
+                   const double *A2, double alpha2, void *F, cudaStream_t s);
 
 // In-place numeric factorization of F.  *status receives max(row+1) of any
-// singular diagonal block (0 = none).
-template <typename T>
-int factor_levels(const Factor &f, T *F, int *status, cudaStream_t s, long long *launches);
+// singular diagonal block (0 = none).  A double-float factor is converted to
+// FP64 in place at the end.
+int factor_levels(const Factor &f, void *F, int *status, cudaStream_t s, long long *launches);
 
 // y = (LU)^{-1} x for nrhs in {1, 2, 4, 8, 16} right-hand sides, layout
 // (row, dof, rhs); y may alias x.  solve_levels launches the level kernels

@@ -151,6 +151,7 @@ int factor_setup(Mesh &m, int lev_fill, int precision, Factor &f) {
   } else {
     if ((rc = f.F64.alloc((size_t)f.nnzb() * 36))) return rc;
   }
+  if ((rc = dense_alloc(f))) return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   return 0;
 }
@@ -175,6 +176,8 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   f.upper.ptr = src.upper.ptr;
   f.upper.rows = src.upper.rows;
   f.task_level_ptr = src.task_level_ptr;
+  f.task_nlong = src.task_nlong;
+  f.task_group = src.task_group;
   f.task_row = src.task_row;
   f.task_ptr = src.task_ptr;
   f.task_jp = src.task_jp;
@@ -188,6 +191,11 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   f.tu_row = src.tu_row;
   f.tu_pos = src.tu_pos;
   f.tu_col = src.tu_col;
+  f.td_row = src.td_row;
+  f.td_pos = src.td_pos;
+  f.td_col = src.td_col;
+  f.dense_t0 = src.dense_t0;
+  f.dense_n = src.dense_n;
   f.flop_count = src.flop_count;
   if ((rc = upload_schedules(f, m.stream))) return rc;
   if ((rc = f.d_frowp.upload(f.frowp.data(), f.frowp.size(), m.stream))) return rc;
@@ -199,6 +207,7 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   } else {
     if ((rc = f.F64.alloc((size_t)f.nnzb() * 36))) return rc;
   }
+  if ((rc = dense_alloc(f))) return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   return 0;
 }
@@ -206,18 +215,11 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
 int factor_numeric(Mesh &m, Factor &f, const double *A, const double *A2, double alpha2) {
   int rc;
   A2DS_CUDA_TRY(cudaMemsetAsync(f.d_status.p, 0, sizeof(int), m.stream));
-  if (f.precision == 32) {
-    if ((rc = factor_scatter<float>(m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, f.d_frowp.p,
-                                    f.d_fcols.p, f.F32.p, m.stream)))
-      return rc;
-    m.launches++;
-    return factor_levels<float>(f, f.F32.p, f.d_status.p, m.stream, &m.launches);
-  }
-  if ((rc = factor_scatter<double>(m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, f.d_frowp.p,
-                                   f.d_fcols.p, f.F64.p, m.stream)))
-    return rc;
+  void *F = f.precision == 32 ? (void *)f.F32.p : (void *)f.F64.p;
+  if ((rc = factor_scatter(f, m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, F, m.stream))) return rc;
   m.launches++;
-  return factor_levels<double>(f, f.F64.p, f.d_status.p, m.stream, &m.launches);
+  if ((rc = factor_levels(f, F, f.d_status.p, m.stream, &m.launches))) return rc;
+  return dense_build(f, F, m.stream, &m.launches);
 }
 
 int factor_check(Mesh &m, Factor &f) {
@@ -391,12 +393,34 @@ struct BucklingState {
   double sigma = 0.0;
   int lev_fill = -1, precision = 0;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // event pairs around every triangular-solve pass of this solve (device
+  // time of the solves, read once at the end)
+  std::vector<cudaEvent_t> tev;
+  int ntev = 0;
   BucklingState() {
     for (auto &e : ev) cudaEventCreate(&e);
   }
   ~BucklingState() {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
+    for (auto &e : tev)
+      if (e) cudaEventDestroy(e);
+  }
+  cudaEvent_t next_event() {
+    if (ntev == (int)tev.size()) {
+      cudaEvent_t e = nullptr;
+      cudaEventCreate(&e);
+      tev.push_back(e);
+    }
+    return tev[ntev++];
+  }
+  double solve_ms() {
+    double t = 0.0;
+    for (int k = 0; k + 1 < ntev; k += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, tev[k], tev[k + 1]) == cudaSuccess) t += ms;
+    }
+    return t;
   }
 };
 
@@ -427,7 +451,14 @@ static int block_norms2(Mesh &m, BucklingState &S, const double *X, int p,
 
 // S.Yb = (LU)^{-1} S.Xb for a block of p vectors, through the factor's
 // cached CUDA graph (FP32 factors: rounded to FP32 and back).
+static int apply_factor_block_(Mesh &m, BucklingState &S, Factor &f, int p);
 static int apply_factor_block(Mesh &m, BucklingState &S, Factor &f, int p) {
+  A2DS_CUDA_TRY(cudaEventRecord(S.next_event(), m.stream));
+  int rc = apply_factor_block_(m, S, f, p);
+  A2DS_CUDA_TRY(cudaEventRecord(S.next_event(), m.stream));
+  return rc;
+}
+static int apply_factor_block_(Mesh &m, BucklingState &S, Factor &f, int p) {
   const size_t n = (size_t)m.nn * 6 * p;
   if (f.precision == 32) {
     int rc;
@@ -532,7 +563,8 @@ extern "C" {
 
 int a2ds_pc_create(a2ds_bcsr A, int lev_fill, int precision, a2ds_pc *out) {
   if (!A || !out) return fail(A2DS_ERR_ARG, "null argument");
-  if (precision != 64 && precision != 32) return fail(A2DS_ERR_ARG, "precision must be 64 or 32");
+  if (precision != 64 && precision != 48 && precision != 32)
+    return fail(A2DS_ERR_ARG, "precision must be 64, 48 or 32");
   if (lev_fill < 0) return fail(A2DS_ERR_ARG, "lev_fill must be >= 0");
   a2ds_pc pc = new a2ds_pc_s();
   pc->mat = A;
@@ -625,8 +657,8 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   if (nev <= 0 || nbmax < 1 || nbmax * p < nev)
     return fail(A2DS_ERR_ARG, "need 0 < num_eigvals <= max_lanczos and block_size <= max_lanczos");
   if (!(opts->sigma > 0.0)) return fail(A2DS_ERR_ARG, "sigma must be positive");
-  if (opts->precision != 64 && opts->precision != 32)
-    return fail(A2DS_ERR_ARG, "precision must be 64 or 32");
+  if (opts->precision != 64 && opts->precision != 48 && opts->precision != 32)
+    return fail(A2DS_ERR_ARG, "precision must be 64, 48 or 32");
   const size_t n6 = (size_t)m.nn * 6;
   const size_t nv = (size_t)m.nnzb * 36;
   const size_t bs = n6 * p;  // doubles per basis block
@@ -641,11 +673,15 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     m.solver = Sp;
     Sp->lev_fill = opts->lev_fill;
     Sp->precision = opts->precision;
-    if ((rc = factor_setup(m, opts->lev_fill, 64, Sp->fk))) return rc;
+    // K's factor serves the load-path solve (FP64 refinement to 1e-13): FP64,
+    // or double-float when the shifted factor is double-float too; an FP32
+    // factor of K is too coarse for this (cond(K) ~ 1e11)
+    if ((rc = factor_setup(m, opts->lev_fill, opts->precision == 48 ? 48 : 64, Sp->fk))) return rc;
     if ((rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa))) return rc;
   }
   BucklingState &S = *Sp;
   S.sigma = opts->sigma;
+  S.ntev = 0;
   if ((rc = S.K.alloc(nv)) || (rc = S.G.alloc(nv)) || (rc = S.Aux.alloc(nv))) return rc;
   if ((rc = S.Q.alloc((size_t)(nbmax + 1) * bs)) || (rc = S.KQ.alloc((size_t)(nbmax + 1) * bs)))
     return rc;
@@ -863,7 +899,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   m.stats = {total, t_k, t_g, t_fk + t_fa, t_path, t_lan, (double)mdim, (double)inner,
              (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
              (double)S.fa.nnzb(), (double)S.fa.flv.nlevels, (double)S.fa.flops(), (double)p,
-             (double)nsteps};
+             (double)nsteps, S.solve_ms(), (double)(S.ntev / 2)};
   if (!converged) return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
   return 0;
 }

@@ -10,10 +10,11 @@
 // (row * 6 + dof) * R + rhs, so one factor block is loaded once and applied
 // to all R vectors.  Rows of the head (levels with many rows) are solved one
 // warp per row (five 6-lane groups stride over the row's blocks), narrow
-// levels one 256-thread block per row, and the dense tail column-oriented
-// (each final pivot pushes its column into later rows with FP64 atomics).
-// A solve is ~3,800 dependent launches at 256x512; solve_graph() captures
-// the whole sequence once per (factor, x, y, R) and replays it.
+// levels one 256-thread block per row, the middle of the tail
+// column-oriented (each final pivot pushes its column into later rows with
+// FP64 atomics), and the trailing separator rows as one dense block, panel
+// by panel.  solve_graph() captures the whole launch sequence once per
+// (factor, x, y, R) and replays it.
 #include "a2ds_internal.h"
 #include "ilu.h"
 
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(256) k_tri_block(const int *__restrict__ rows,
   }
 }
 
-// ------------------------------------------------------ dense-tail solves
+// ------------------------------------------------------------ tail solves
 // Rows [s, n) are the trailing separators, where levels hold a handful of
 // long rows.  Their head couplings are pulled once; then, tail level by tail
 // level, the columns of final pivots are pushed into the later rows.
@@ -191,10 +192,12 @@ __global__ void __launch_bounds__(256) k_tail_pull(int s, int d, const int *__re
 }
 
 // One tail level's column pushes; thread (entry e, rhs r).  Entry e is
-// (target row i, factor position p, pivot row j).  Lower: y_i -= L_ij y_j.
-// Upper: y_i -= U_ij D_j^{-1} y_j (y_j itself is scaled by D_j^{-1} only
-// after all tail levels, by k_tail_finalize).
-template <typename T, typename TV, int R, bool UPPER>
+// (target row i, factor position p, pivot row j).  PUSH_L: y_i -= L_ij y_j.
+// PUSH_U: y_i -= U_ij D_j^{-1} y_j (y_j itself is scaled by D_j^{-1} only
+// after all tail levels, by k_tail_finalize).  PUSH_U_FINAL: y_i -= U_ij y_j
+// with y_j already final (dense-block columns).
+enum { PUSH_L = 0, PUSH_U = 1, PUSH_U_FINAL = 2 };
+template <typename T, typename TV, int R, int MODE>
 __global__ void __launch_bounds__(256) k_tail_push(const int *__restrict__ erow,
                                                    const int *__restrict__ epos,
                                                    const int *__restrict__ ecol, int ne,
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(256) k_tail_push(const int *__restrict__ erow,
   TV w[6];
 #pragma unroll
   for (int b = 0; b < 6; b++) w[b] = y[((size_t)j * 6 + b) * R + r];
-  if (UPPER) {
+  if (MODE == PUSH_U) {
     const T *Dinv = F + (size_t)fdiag[j] * 36;
     TV v[6];
 #pragma unroll
@@ -230,7 +233,7 @@ __global__ void __launch_bounds__(256) k_tail_push(const int *__restrict__ erow,
   }
 }
 
-// y_j = D_j^{-1} z_j for every tail row; thread (row, rhs).
+// y_j = D_j^{-1} z_j for tail rows j in [s, s + d); thread (row, rhs).
 template <typename T, typename TV, int R>
 __global__ void k_tail_finalize(int s, int d, const int *__restrict__ fdiag,
                                 const T *__restrict__ F, TV *y) {
@@ -248,6 +251,217 @@ __global__ void k_tail_finalize(int s, int d, const int *__restrict__ fdiag,
 #pragma unroll
     for (int b = 0; b < 6; b++) v += (TV)Dinv[6 * a + b] * z[b];
     y[((size_t)j * 6 + a) * R + r] = v;
+  }
+}
+
+// ------------------------------------------------------ dense trailing block
+// The last dense_n block rows are solved as a dense (6 dense_n)^2 system,
+// DENSE_PANEL block rows (PB6 unknowns) at a time: w = P_pp y_p with the
+// precomputed inverse of the diagonal panel, then the rows beyond the panel
+// (below it for L, above it for U) subtract M[rows, panel] w.  Two launches
+// per panel instead of one per row, and the work of a panel is spread over
+// the whole GPU.
+constexpr int PB6 = 6 * DENSE_PANEL;
+
+template <typename TV, int R>
+__device__ __forceinline__ void warp_sum(TV (&acc)[R]) {
+#pragma unroll
+  for (int r = 0; r < R; r++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+}
+
+// w = P v, P = PB6 x PB6 row-major, v and w PB6 x R; one warp per row of P.
+template <typename T, typename TV, int R>
+__global__ void __launch_bounds__(256) k_dense_panel_apply(const T *__restrict__ P, const TV *v,
+                                                           TV *__restrict__ w) {
+  __shared__ TV sv[PB6 * R];
+  for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) sv[k] = v[k];
+  __syncthreads();
+  const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (row >= PB6) return;
+  TV acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = 0;
+  const T *prow = P + (size_t)row * PB6;
+  for (int c = lane; c < PB6; c += 32) {
+    const TV m = (TV)prow[c];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] += m * sv[c * R + r];
+  }
+  warp_sum<TV, R>(acc);
+  TV out = 0;
+#pragma unroll
+  for (int r = 0; r < R; r++)
+    if (lane == r) out = acc[r];
+  if (lane < R) w[(size_t)row * R + lane] = out;
+}
+
+// Rows [r0, r0 + nrows) of the dense segment yD: y -= M[rows, c0 : c0 + PB6] w;
+// CTA 0 also stores w as the panel's final values (yD rows c0 ..).  One warp
+// per row; M is the dense block, leading dimension ld.
+template <typename T, typename TV, int R>
+__global__ void __launch_bounds__(256) k_dense_panel_update(const T *__restrict__ M, int ld,
+                                                            int r0, int nrows, int c0,
+                                                            const TV *__restrict__ w, TV *yD) {
+  __shared__ TV sw[PB6 * R];
+  for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) sw[k] = w[k];
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) yD[(size_t)c0 * R + k] = sw[k];
+  const int rr = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (rr >= nrows) return;
+  const int row = r0 + rr;
+  TV acc[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) acc[r] = 0;
+  const T *mrow = M + (size_t)row * ld + c0;
+  for (int c = lane; c < PB6; c += 32) {
+    const TV m = (TV)mrow[c];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] += m * sw[c * R + r];
+  }
+  warp_sum<TV, R>(acc);
+  TV out = 0;
+#pragma unroll
+  for (int r = 0; r < R; r++)
+    if (lane == r) out = acc[r];
+  if (lane < R) yD[(size_t)row * R + lane] -= out;
+}
+
+// Copy the factor's blocks of the dense block rows into the dense array
+// (zeroed beforehand); one warp per block row.
+template <typename T>
+__global__ void k_dense_scatter(int t0, int nd, const int *__restrict__ frowp,
+                                const int *__restrict__ fcols, const T *__restrict__ F,
+                                T *__restrict__ M) {
+  const int rr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (rr >= nd) return;
+  const int i = t0 + rr, ld = 6 * nd;
+  int k0 = frowp[i];
+  const int k1 = frowp[i + 1];
+  while (k0 < k1 && fcols[k0] < t0) k0++;  // columns are sorted
+  const int nb = k1 - k0;
+  for (int idx = lane; idx < nb * 36; idx += 32) {
+    const int k = k0 + idx / 36, e = idx % 36;
+    const int a = e / 6, b = e % 6;
+    M[(size_t)(6 * rr + a) * ld + 6 * (fcols[k] - t0) + b] = F[(size_t)k * 36 + e];
+  }
+}
+
+// Inverse of every diagonal panel, thread (panel, column c).  Lower: the
+// unit block-lower L_pp, forward substitution on e_c.  Upper: D + U_pp with
+// the stored D_i^{-1}: z_i = D_i^{-1} (e_c - sum_{j > i} U_ij z_j), backward.
+template <typename T, bool UPPER>
+__global__ void k_dense_panel_inverse(const T *__restrict__ M, int ld, int npanels,
+                                      T *__restrict__ Pinv) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = t / PB6, c = t % PB6;
+  if (p >= npanels) return;
+  const T *Mp = M + (size_t)p * PB6 * ld + (size_t)p * PB6;
+  T *X = Pinv + (size_t)p * PB6 * PB6;
+  if (!UPPER) {
+    for (int i = 0; i < DENSE_PANEL; i++)
+      for (int a = 0; a < 6; a++) {
+        const int r = 6 * i + a;
+        T v = (r == c) ? T(1) : T(0);
+        for (int q = 0; q < 6 * i; q++) v -= Mp[(size_t)r * ld + q] * X[(size_t)q * PB6 + c];
+        X[(size_t)r * PB6 + c] = v;
+      }
+  } else {
+    for (int i = DENSE_PANEL - 1; i >= 0; i--) {
+      T z[6];
+      for (int a = 0; a < 6; a++) {
+        const int r = 6 * i + a;
+        T v = (r == c) ? T(1) : T(0);
+        for (int q = 6 * (i + 1); q < PB6; q++) v -= Mp[(size_t)r * ld + q] * X[(size_t)q * PB6 + c];
+        z[a] = v;
+      }
+      for (int a = 0; a < 6; a++) {
+        T v = 0;
+        for (int b = 0; b < 6; b++) v += Mp[(size_t)(6 * i + a) * ld + 6 * i + b] * z[b];
+        X[(size_t)(6 * i + a) * PB6 + c] = v;
+      }
+    }
+  }
+}
+
+template <typename T>
+struct DenseBufs;
+template <>
+struct DenseBufs<double> {
+  static double *M(const Factor &f) { return f.dense64.p; }
+  static double *L(const Factor &f) { return f.pinvL64.p; }
+  static double *U(const Factor &f) { return f.pinvU64.p; }
+  static double *W(const Factor &f) { return f.dwork64.p; }
+};
+template <>
+struct DenseBufs<float> {
+  static float *M(const Factor &f) { return f.dense32.p; }
+  static float *L(const Factor &f) { return f.pinvL32.p; }
+  static float *U(const Factor &f) { return f.pinvU32.p; }
+  static float *W(const Factor &f) { return f.dwork32.p; }
+};
+
+int dense_alloc(Factor &f) {
+  if (f.dense_n <= 0) return 0;
+  const size_t nd6 = (size_t)6 * f.dense_n, np = (size_t)f.dense_n / DENSE_PANEL;
+  int rc;
+  if (f.precision == 32) {
+    if ((rc = f.dense32.alloc(nd6 * nd6)) || (rc = f.pinvL32.alloc(np * PB6 * PB6)) ||
+        (rc = f.pinvU32.alloc(np * PB6 * PB6)) || (rc = f.dwork32.alloc((size_t)PB6 * 16)))
+      return rc;
+  } else {
+    if ((rc = f.dense64.alloc(nd6 * nd6)) || (rc = f.pinvL64.alloc(np * PB6 * PB6)) ||
+        (rc = f.pinvU64.alloc(np * PB6 * PB6)) || (rc = f.dwork64.alloc((size_t)PB6 * 16)))
+      return rc;
+  }
+  return 0;
+}
+
+template <typename T>
+static int dense_build_t(Factor &f, const T *F, cudaStream_t s, long long *launches) {
+  const int nd = f.dense_n, ld = 6 * nd, np = nd / DENSE_PANEL;
+  T *M = DenseBufs<T>::M(f);
+  A2DS_CUDA_TRY(cudaMemsetAsync(M, 0, (size_t)ld * ld * sizeof(T), s));
+  k_dense_scatter<T><<<(nd * 32 + 255) / 256, 256, 0, s>>>(f.dense_t0, nd, f.d_frowp.p,
+                                                           f.d_fcols.p, F, M);
+  k_dense_panel_inverse<T, false><<<(np * PB6 + 127) / 128, 128, 0, s>>>(M, ld, np,
+                                                                          DenseBufs<T>::L(f));
+  k_dense_panel_inverse<T, true><<<(np * PB6 + 127) / 128, 128, 0, s>>>(M, ld, np,
+                                                                         DenseBufs<T>::U(f));
+  if (launches) *launches += 3;
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int dense_build(Factor &f, const void *F, cudaStream_t s, long long *launches) {
+  if (f.dense_n <= 0) return 0;
+  if (f.precision == 32) return dense_build_t<float>(f, (const float *)F, s, launches);
+  return dense_build_t<double>(f, (const double *)F, s, launches);
+}
+
+template <typename T, typename TV, int R>
+static void dense_solve(const Factor &f, TV *y, cudaStream_t s, long long &nl) {
+  const int nd = f.dense_n, ld = 6 * nd, np = nd / DENSE_PANEL;
+  const T *M = DenseBufs<T>::M(f);
+  TV *w = DenseBufs<TV>::W(f);
+  TV *yD = y + (size_t)f.dense_t0 * 6 * R;
+  for (int p = 0; p < np; p++) {  // L: forward
+    k_dense_panel_apply<T, TV, R><<<PB6 / 8, 256, 0, s>>>(
+        DenseBufs<T>::L(f) + (size_t)p * PB6 * PB6, yD + (size_t)p * PB6 * R, w);
+    const int r0 = (p + 1) * PB6, nr = ld - r0;
+    k_dense_panel_update<T, TV, R><<<std::max(1, (nr + 7) / 8), 256, 0, s>>>(M, ld, r0, nr,
+                                                                             p * PB6, w, yD);
+    nl += 2;
+  }
+  for (int p = np - 1; p >= 0; p--) {  // D + U: backward
+    k_dense_panel_apply<T, TV, R><<<PB6 / 8, 256, 0, s>>>(
+        DenseBufs<T>::U(f) + (size_t)p * PB6 * PB6, yD + (size_t)p * PB6 * R, w);
+    const int nr = p * PB6;
+    k_dense_panel_update<T, TV, R><<<std::max(1, (nr + 7) / 8), 256, 0, s>>>(M, ld, 0, nr,
+                                                                             p * PB6, w, yD);
+    nl += 2;
   }
 }
 
@@ -277,19 +491,31 @@ static int solve_levels_r(const Factor &f, const T *F, const TV *x, TV *y, cudaS
     for (size_t lv = 0; lv + 1 < f.tl_ptr.size(); lv++) {
       const int e0 = f.tl_ptr[lv], ne = f.tl_ptr[lv + 1] - e0;
       if (ne <= 0) continue;
-      k_tail_push<T, TV, R, false><<<(ne * R + 255) / 256, 256, 0, s>>>(
+      k_tail_push<T, TV, R, PUSH_L><<<(ne * R + 255) / 256, 256, 0, s>>>(
           f.d_tl_row.p + e0, f.d_tl_pos.p + e0, f.d_tl_col.p + e0, ne, f.d_fdiag.p, F, y);
       nl++;
+    }
+    if (f.dense_n > 0) {
+      dense_solve<T, TV, R>(f, y, s, nl);
+      const int ne = (int)f.td_row.size();
+      if (ne > 0) {
+        k_tail_push<T, TV, R, PUSH_U_FINAL><<<(ne * R + 255) / 256, 256, 0, s>>>(
+            f.d_td_row.p, f.d_td_pos.p, f.d_td_col.p, ne, f.d_fdiag.p, F, y);
+        nl++;
+      }
     }
     for (size_t lv = 0; lv + 1 < f.tu_ptr.size(); lv++) {
       const int e0 = f.tu_ptr[lv], ne = f.tu_ptr[lv + 1] - e0;
       if (ne <= 0) continue;
-      k_tail_push<T, TV, R, true><<<(ne * R + 255) / 256, 256, 0, s>>>(
+      k_tail_push<T, TV, R, PUSH_U><<<(ne * R + 255) / 256, 256, 0, s>>>(
           f.d_tu_row.p + e0, f.d_tu_pos.p + e0, f.d_tu_col.p + e0, ne, f.d_fdiag.p, F, y);
       nl++;
     }
-    k_tail_finalize<T, TV, R><<<(d * R + 127) / 128, 128, 0, s>>>(ts, d, f.d_fdiag.p, F, y);
-    nl++;
+    const int dm = f.dense_t0 - ts;  // middle rows: finalized here (dense rows are final)
+    if (dm > 0) {
+      k_tail_finalize<T, TV, R><<<(dm * R + 127) / 128, 128, 0, s>>>(ts, dm, f.d_fdiag.p, F, y);
+      nl++;
+    }
   }
   for (int lv = 0; lv < Up.nlevels; lv++) {
     const int cnt = Up.ptr[lv + 1] - Up.ptr[lv];

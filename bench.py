@@ -57,7 +57,9 @@ def parse():
     p.add_argument("--nx", type=int, default=256)
     p.add_argument("--ny", type=int, default=512)
     p.add_argument("--neig", type=int, default=10)
-    p.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    p.add_argument("--precision", type=int, default=64, choices=[64, 48, 32],
+                   help="factor arithmetic: 64 FP64, 48 double-float on the FP32 pipe, 32 FP32 "
+                        "(solves and refinement are FP64 in every case)")
     p.add_argument("--block", type=int, default=8, choices=[1, 2, 4, 8, 16],
                    help="Lanczos block size")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -369,11 +371,18 @@ def main():
     achieved_gbs = bytes_factor / (fa_ms * 1e-3) / 1e9
     achieved_tf = stats["factor_flops"] / (fa_ms * 1e-3) / 1e12
     lam_err = float(np.max(np.abs(b.eigvals - ref_lam) / np.abs(ref_lam)))
+    vs_fp64 = None
+    if args.precision != 64:
+        # eigenvalue error of this precision against an all-FP64 solve (untimed)
+        b64 = capi.LinearBuckling(a, sigma, max_lanczos=200, num_eigvals=args.neig, eig_tol=1e-8,
+                                  precision=64, block_size=args.block)
+        lam64 = b64.solve(m.rhs, want_vectors=False).copy()
+        vs_fp64 = float(np.max(np.abs(b.eigvals - lam64) / np.abs(lam64)))
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == 64 else "f32+f64",
+        "dtype": {64: "f64", 48: "df64 factor (2 x f32) + f64", 32: "f32 factor + f64"}[args.precision],
         "data": "synthetic (seeded cylinder mesh, loads and imperfection; no dataset)",
         "config": workload_config(m, args),
         "gpu_launches": launches,
@@ -394,11 +403,13 @@ def main():
         "phases_s": {k: stats[k] for k in ["assemble_k_s", "assemble_g_s", "factor_s", "path_s",
                                             "lanczos_s"]},
         "lanczos": {"vectors": stats["lanczos_vectors"], "block_size": stats["block_size"],
-                    "block_steps": stats["block_iters"], "refinement_checks": stats["inner_iters"]},
+                    "block_steps": stats["block_iters"], "refinement_checks": stats["inner_iters"],
+                    "trisolve_ms_total": stats["trisolve_ms"], "trisolve_calls": stats["trisolve_calls"]},
         "assembly_elems_per_s": {"K": m.num_elements / stats["assemble_k_s"],
                                  "G": m.num_elements / stats["assemble_g_s"]},
         "eigvals": b.eigvals.tolist(), "eig_rel_drift_between_runs": lam_err,
         "eig_residual_max": float(np.max(b.errors)), "sigma": sigma,
+        "eig_rel_err_vs_fp64": vs_fp64,
         "clocks": clk,
     }
     if not args.no_cpu_baseline and world == 1:

@@ -188,7 +188,9 @@ int a2ds_bcsr_apply_bcs(a2ds_bcsr A);
    Replaces TACSSchurPc(kmat, levFill, fill, 1) (src/bpmat/TACSSchurMat.cpp:
    944): symbolic ILU(levFill) of A's pattern (BCSRMat::computeILUk,
    src/bpmat/BCSRMat.cpp:625); levFill >= num_nodes gives the complete LU.
-   precision: 64 (FP64 factor) or 32 (FP32 factor). */
+   precision: 64 (FP64 factor), 48 (factored in double-float arithmetic on
+   the FP32 pipe, ~48-bit mantissa, then stored as FP64) or 32 (FP32
+   factor). */
 int a2ds_pc_create(a2ds_bcsr A, int lev_fill, int precision, a2ds_pc *out);
 int a2ds_pc_destroy(a2ds_pc pc);
 
@@ -218,7 +220,9 @@ typedef struct {
   int gmres_restarts;    /* GMRES restarts */
   double gmres_rtol;     /* GMRES relative tolerance */
   double gmres_atol;     /* GMRES absolute tolerance */
-  int precision;         /* 64: all-FP64; 32: FP32 factor + FP64 refinement */
+  int precision;         /* 64: all-FP64; 48: double-float factors + FP64
+                            solves and refinement; 32: FP32 factors + FP64
+                            refinement */
   int seed;              /* Lanczos start vector seed */
   int block_size;        /* Lanczos block size p in {1, 2, 4, 8, 16}: p vectors
                             per shift-invert solve (1 = the reference's
@@ -244,7 +248,8 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts,
    fills up to n doubles {total_s, assemble_k_s, assemble_g_s, factor_s,
    path_s, lanczos_s, lanczos_vectors, inner_iters, kernel_launches,
    solve_event_ms, factor_a_event_ms, factor_k_event_ms, factor_nnzb,
-   factor_levels, factor_flops, block_size, block_iters}. */
+   factor_levels, factor_flops, block_size, block_iters, trisolve_ms,
+   trisolve_calls}. */
 int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out);
 
 /* ---------------------------------------------- eigenvalue sensitivities

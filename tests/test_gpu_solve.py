@@ -33,7 +33,7 @@ def setup(f):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu"])
-@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("precision", [64, 48, 32])
 def test_factor_matches_reference(case, precision):
     f = np.load(os.path.join(GOLDEN, case + ".npz"))
     a = setup(f)
@@ -43,8 +43,9 @@ def test_factor_matches_reference(case, precision):
     pc.factor()
     rowp, cols, vals = pc.get_arrays()
     assert np.array_equal(rowp, f["ilu_rowp"]) and np.array_equal(cols, f["ilu_cols"])
-    tol = 1e-10 if precision == 64 else 1e-3
-    # compare factor blocks scaled per block row (inverted diagonals differ in scale)
+    # FP64: reference rounding differences only; double-float (48): ~2^-48
+    # rounding in the update chain; FP32 factors are only checked for pattern
+    tol = {64: 1e-10, 48: 1e-10, 32: 1e-3}[precision]
     assert rel(vals, f["ilu_K"]) < tol or precision == 32
     # applyFactor in the row ordering: the fixture vector is in row order
     perm = a.get_ordering()
@@ -53,17 +54,23 @@ def test_factor_matches_reference(case, precision):
     x_nodes[perm] = x_rows
     y_nodes = pc.apply_factor(x_nodes)
     y_rows = y_nodes[perm].ravel()
-    assert rel(y_rows, f["ilu_apply_y"]) < (1e-9 if precision == 64 else 1e-2)
+    # the apply amplifies factor rounding by up to cond(K) ~ 1e11
+    assert rel(y_rows, f["ilu_apply_y"]) < {64: 1e-9, 48: 1e-6, 32: 1e-2}[precision]
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu"])
-def test_buckling_loads_match_dense_reference(case):
+@pytest.mark.parametrize("precision,block", [(64, 1), (64, 8), (48, 8)])
+def test_buckling_loads_match_dense_reference(case, precision, block):
+    """Eigenvalues within 1e-8 (relative) of a dense FP64 solution, for the
+    single-vector and block Lanczos and for double-float factors (FP64
+    refinement of every shift-invert solve)."""
     f = np.load(os.path.join(GOLDEN, case + ".npz"))
     a = setup(f)
     nev = 5
     b = capi.LinearBuckling(a, float(f["sigma"]), max_lanczos=120, num_eigvals=nev,
-                            eig_tol=1e-12, lev_fill=1000000)
+                            eig_tol=1e-12, lev_fill=1000000, precision=precision,
+                            block_size=block)
     lam = b.solve(f["rhs"])
     assert np.all(b.errors < 1e-8), b.errors
     # dense FP64 solution of K x + lam G x = 0 with G at this solve's path
@@ -95,7 +102,7 @@ def dense_buckling(K, G, bc_nodes, bc_mask):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [64])
+@pytest.mark.parametrize("precision", [64, 48])
 def test_factor_solve_residual_mid_size(precision):
     """A 24x48 cylinder: wide head levels (row-oriented solves) and a dense
     tail (column pushes) are both exercised; K y = x to the factor's
@@ -117,5 +124,37 @@ def test_factor_solve_residual_mid_size(precision):
     x = rng.standard_normal((m.num_nodes, 6))
     y = pc.apply_factor(x)
     r = K.mult(y) - x
-    tol = 1e-6 if precision == 64 else 5e-1
-    assert np.linalg.norm(r) / np.linalg.norm(x) < tol
+    # (the trailing dense block is solved with precomputed inverses of its
+    # diagonal panels, which costs a few bits against substitution; every
+    # solve inside the buckling path is refined in FP64)
+    tol = {64: 1e-5, 48: 1e-4}[precision]
+    res = np.linalg.norm(r) / np.linalg.norm(x)
+    print("relative residual", precision, res)
+    assert res < tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,block", [(64, 8), (48, 8), (64, 1)])
+def test_buckling_mid_size_dense_tail(precision, block):
+    """A 16x32 cylinder, large enough that the trailing separator rows of the
+    factor are solved as a dense block (and the middle of the tail by column
+    pushes): the lowest buckling loads match a dense FP64 eigensolve of
+    K x + lam G x = 0 (G at this solve's path) to 1e-8."""
+    from a2ds import mesh as meshgen
+    m = meshgen.cylinder(16, 32)
+    a = capi.Assembler(m.X, m.conn)
+    a.set_material(m.E, m.nu)
+    a.set_thickness([m.meta["t"]])
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    nev = 6
+    lam_cl = meshgen.classical_cylinder_load(m.E, m.nu, m.meta["t"], 1.0)
+    b = capi.LinearBuckling(a, 0.3 * lam_cl, max_lanczos=160, num_eigvals=nev, eig_tol=1e-12,
+                            precision=precision, block_size=block)
+    lam = b.solve(m.rhs)
+    assert np.all(b.errors < 1e-8), b.errors
+    K, G = a.create_mat(), a.create_mat()
+    a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
+    a.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, b.path)
+    dense = dense_buckling(K.to_dense_nodes(), G.to_dense_nodes(), m.bc_nodes, m.bc_mask)
+    assert np.max(np.abs(lam - dense[:nev]) / np.abs(dense[:nev])) < 1e-8, (lam, dense[:nev])
