@@ -44,7 +44,7 @@ EXPORTS = [
     "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
-    "a2ds_pc_apply", "a2ds_pc_get", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
+    "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
     "a2ds_buckling_stats", "a2ds_eig_sens_thickness",
 ]
 
@@ -117,6 +117,7 @@ def load(build: bool = False):
     lib.a2ds_pc_destroy.argtypes = [VP]
     lib.a2ds_pc_factor.argtypes = [VP, VP]
     lib.a2ds_pc_apply.argtypes = [VP, P_D, P_D]
+    lib.a2ds_pc_apply_multi.argtypes = [VP, ctypes.c_int, P_D, P_D]
     lib.a2ds_pc_get.argtypes = [VP, P_I, P_I, P_I, P_I, P_D]
     lib.a2ds_buckling_default_opts.argtypes = [ctypes.POINTER(BucklingOpts)]
     lib.a2ds_buckling_default_opts.restype = None
@@ -330,6 +331,13 @@ class SchurPc:
         y = np.zeros_like(x)
         _check(self.lib.a2ds_pc_apply(self.h, _d(x), _d(y)))
         return y
+
+    def apply_factor_multi(self, X):
+        """applyFactor on nrhs stacked vectors X (nrhs, num_nodes, 6)."""
+        X = _f64(X)
+        Y = np.zeros_like(X)
+        _check(self.lib.a2ds_pc_apply_multi(self.h, X.shape[0], _d(X), _d(Y)))
+        return Y
 
     def get_arrays(self):
         nr, nz = ctypes.c_int(), ctypes.c_int()

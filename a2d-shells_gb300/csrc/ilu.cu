@@ -152,6 +152,20 @@ void build_solve_schedule(Factor &f, const std::vector<int> &lev, int narrow) {
     std::vector<int> fill(L.ptr.begin(), L.ptr.end() - 1);
     for (int i = 0; i < s; i++) L.rows[fill[remap[lev[i]]]++] = i;
   }
+  // kernel choice per head level (see SOLVE_LONG_ROW)
+  auto choose = [&](const LevelSchedule &L, bool upper, std::vector<char> &cta) {
+    cta.assign(L.nlevels, 0);
+    for (int l = 0; l < L.nlevels; l++) {
+      int maxlen = 0;
+      for (int k = L.ptr[l]; k < L.ptr[l + 1]; k++) {
+        const int i = L.rows[k];
+        const int len = upper ? f.frowp[i + 1] - f.fdiag[i] - 1 : f.fdiag[i] - f.frowp[i];
+        maxlen = std::max(maxlen, len);
+      }
+      cta[l] = (L.ptr[l + 1] - L.ptr[l] < SOLVE_NARROW_ROWS || maxlen > SOLVE_LONG_ROW) ? 1 : 0;
+    }
+  };
+  choose(f.lower, false, f.lower_cta);
   // head upper: levels counting only head columns (tail values are final)
   {
     std::vector<int> ul(s, 0);
@@ -174,6 +188,7 @@ void build_solve_schedule(Factor &f, const std::vector<int> &lev, int narrow) {
     std::vector<int> fill(U.ptr.begin(), U.ptr.end() - 1);
     for (int i = 0; i < s; i++) U.rows[fill[ul[i]]++] = i;
   }
+  choose(f.upper, true, f.upper_cta);
   f.lsplit.assign(d, 0);
   f.tl_ptr.assign(1, 0);
   f.tu_ptr.assign(1, 0);

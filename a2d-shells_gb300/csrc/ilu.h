@@ -33,6 +33,8 @@ struct Factor {
   DBuf<float> F32;
   LevelSchedule flv;           // dependency levels of all rows (factorization)
   LevelSchedule lower, upper;  // head rows [0, tail_s): row-oriented solves
+  // per head level: 1 = one CTA per row (few or long rows), 0 = one warp per row
+  std::vector<char> lower_cta, upper_cta;
   // right-looking update tasks, grouped by level; within a level the tasks
   // of long target rows (> FACTOR_WARP_COLS blocks) come first
   std::vector<int> task_level_ptr, task_nlong, task_row, task_ptr, task_jp;
@@ -85,6 +87,11 @@ constexpr int FACTOR_CTA_COLS = 10240;
 // between DENSE_MIN and DENSE_MAX block rows, used when the factor fills at
 // least DENSE_MIN_FILL of it.
 constexpr int DENSE_PANEL = 32;
+// Head solve levels use one CTA per row when they have fewer than
+// SOLVE_NARROW_ROWS rows or a row longer than SOLVE_LONG_ROW blocks (a warp
+// would walk the long row alone), one warp per row otherwise.
+constexpr int SOLVE_NARROW_ROWS = 48;
+constexpr int SOLVE_LONG_ROW = 24;
 constexpr int DENSE_MIN = 64;
 constexpr int DENSE_MAX = 2048;
 constexpr double DENSE_MIN_FILL = 0.4;

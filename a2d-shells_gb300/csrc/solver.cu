@@ -175,6 +175,8 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   f.upper.nlevels = src.upper.nlevels;
   f.upper.ptr = src.upper.ptr;
   f.upper.rows = src.upper.rows;
+  f.lower_cta = src.lower_cta;
+  f.upper_cta = src.upper_cta;
   f.task_level_ptr = src.task_level_ptr;
   f.task_nlong = src.task_nlong;
   f.task_group = src.task_group;
@@ -602,6 +604,48 @@ int a2ds_pc_apply(a2ds_pc pc, const double *x, double *y) {
   if ((rc = dy.alloc((size_t)m.nn * 6))) return rc;
   if ((rc = factor_apply(m, pc->f, dx.p, dy.p, w32))) return rc;
   return m.from_rows(dy.p, y);
+}
+
+int a2ds_pc_apply_multi(a2ds_pc pc, int nrhs, const double *x, double *y) {
+  if (!pc || !x || !y) return fail(A2DS_ERR_ARG, "null argument");
+  if (nrhs != 1 && nrhs != 2 && nrhs != 4 && nrhs != 8 && nrhs != 16)
+    return fail(A2DS_ERR_ARG, "nrhs must be 1, 2, 4, 8 or 16");
+  Mesh &m = pc->mat->mesh->m;
+  Factor &f = pc->f;
+  const size_t n6 = (size_t)m.nn * 6, tot = n6 * nrhs;
+  // node-ordered vectors -> row order, right-hand sides interleaved
+  std::vector<double> h(tot);
+  for (int k = 0; k < nrhs; k++)
+    for (int r = 0; r < m.nn; r++)
+      for (int d = 0; d < 6; d++)
+        h[((size_t)r * 6 + d) * nrhs + k] = x[(size_t)k * n6 + (size_t)m.perm[r] * 6 + d];
+  DBuf<double> dx, dy;
+  int rc;
+  if ((rc = dx.upload(h.data(), tot, m.stream)) || (rc = dy.alloc(tot))) return rc;
+  if (f.precision == 32) {
+    DBuf<float> w;
+    if ((rc = w.alloc(tot))) return rc;
+    k_f64_to_f32<<<grid_for(tot), 256, 0, m.stream>>>(w.p, dx.p, tot);
+    if ((rc = solve_levels<float, float>(f, f.F32.p, w.p, w.p, nrhs, m.stream, &m.launches)))
+      return rc;
+    A2DS_CUDA_TRY(cudaMemsetAsync(dy.p, 0, tot * sizeof(double), m.stream));
+    k_add_f32<<<grid_for(tot), 256, 0, m.stream>>>(dy.p, w.p, tot);
+    A2DS_CUDA_TRY(cudaGetLastError());
+    A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), dy.p, tot * sizeof(double), cudaMemcpyDeviceToHost,
+                                  m.stream));
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  } else {
+    if ((rc = solve_levels<double, double>(f, f.F64.p, dx.p, dy.p, nrhs, m.stream, &m.launches)))
+      return rc;
+    A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), dy.p, tot * sizeof(double), cudaMemcpyDeviceToHost,
+                                  m.stream));
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  }
+  for (int k = 0; k < nrhs; k++)
+    for (int r = 0; r < m.nn; r++)
+      for (int d = 0; d < 6; d++)
+        y[(size_t)k * n6 + (size_t)m.perm[r] * 6 + d] = h[((size_t)r * 6 + d) * nrhs + k];
+  return 0;
 }
 
 int a2ds_pc_get(a2ds_pc pc, int *nrows, int *nnzb, int *rowp, int *cols, double *vals) {

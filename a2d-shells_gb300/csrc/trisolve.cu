@@ -20,7 +20,6 @@
 
 namespace a2ds {
 
-constexpr int NARROW_LEVEL = 48;  // levels with fewer rows solve block-per-row
 
 // Partial sums of sum_k F_k[ii][:] y[fcols[k]] over k = kb + g, kb + g + step, ...
 template <typename T, typename TV, int R>
@@ -473,7 +472,7 @@ static int solve_levels_r(const Factor &f, const T *F, const TV *x, TV *y, cudaS
   long long nl = 0;
   for (int lv = 0; lv < Lo.nlevels; lv++) {
     const int cnt = Lo.ptr[lv + 1] - Lo.ptr[lv];
-    if (cnt < NARROW_LEVEL)
+    if (f.lower_cta[lv])
       k_tri_block<T, TV, R, false><<<cnt, 256, 0, s>>>(Lo.d_rows.p + Lo.ptr[lv], cnt,
                                                        f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
                                                        x, y);
@@ -519,7 +518,7 @@ static int solve_levels_r(const Factor &f, const T *F, const TV *x, TV *y, cudaS
   }
   for (int lv = 0; lv < Up.nlevels; lv++) {
     const int cnt = Up.ptr[lv + 1] - Up.ptr[lv];
-    if (cnt < NARROW_LEVEL)
+    if (f.upper_cta[lv])
       k_tri_block<T, TV, R, true><<<cnt, 256, 0, s>>>(Up.d_rows.p + Up.ptr[lv], cnt,
                                                       f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
                                                       y, y);

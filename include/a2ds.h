@@ -203,6 +203,12 @@ int a2ds_pc_factor(a2ds_pc pc, a2ds_bcsr from);
    node-ordered num_nodes x 6 host vectors. */
 int a2ds_pc_apply(a2ds_pc pc, const double *x, double *y);
 
+/* applyFactor for nrhs right-hand sides at once (nrhs in {1, 2, 4, 8, 16};
+   the reference applies one vector per call): x and y hold nrhs node-ordered
+   num_nodes x 6 vectors one after another.  Each factor block is read once
+   for all of them. */
+int a2ds_pc_apply_multi(a2ds_pc pc, int nrhs, const double *x, double *y);
+
 /* BCSRMat::getArrays on the factor: the ILU(k) pattern (bit-exact with the
    reference's) and the factored values (diagonal blocks stored inverted,
    as BCSRMatFactor6 leaves them). */
