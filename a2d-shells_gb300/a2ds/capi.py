@@ -44,7 +44,7 @@ EXPORTS = [
     "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
-    "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
+    "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
     "a2ds_buckling_stats", "a2ds_eig_sens_thickness",
 ]
 
@@ -118,6 +118,8 @@ def load(build: bool = False):
     lib.a2ds_pc_factor.argtypes = [VP, VP]
     lib.a2ds_pc_apply.argtypes = [VP, P_D, P_D]
     lib.a2ds_pc_apply_multi.argtypes = [VP, ctypes.c_int, P_D, P_D]
+    lib.a2ds_gmres_solve.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, P_D, P_D, P_I, P_D]
     lib.a2ds_pc_get.argtypes = [VP, P_I, P_I, P_I, P_I, P_D]
     lib.a2ds_buckling_default_opts.argtypes = [ctypes.POINTER(BucklingOpts)]
     lib.a2ds_buckling_default_opts.restype = None
@@ -349,6 +351,21 @@ class SchurPc:
         return rowp, cols, vals
 
 
+def gmres_solve(A: "BCSRMat", pc: "SchurPc", b, msub=30, nrestart=15, rtol=1e-12, atol=1e-30,
+                raise_on_noconv=True):
+    """GMRES(mat, pc, msub, nrestart) solve(b, x) (src/bpmat/KSM.cpp:785):
+    returns (x, iterations, residual estimate)."""
+    b = _f64(b).reshape(-1, 6)
+    x = np.zeros_like(b)
+    it, rn = ctypes.c_int(), ctypes.c_double()
+    rc = A.lib.a2ds_gmres_solve(A.h, pc.h if pc is not None else None, int(msub), int(nrestart),
+                                float(rtol), float(atol), _d(b), _d(x), ctypes.byref(it),
+                                ctypes.byref(rn))
+    if rc != 6 or raise_on_noconv:
+        _check(rc)
+    return x, it.value, rn.value
+
+
 STAT_NAMES = ["total_s", "assemble_k_s", "assemble_g_s", "factor_s", "path_s", "lanczos_s",
               "lanczos_vectors", "inner_iters", "kernel_launches", "solve_event_ms",
               "factor_a_event_ms", "factor_k_event_ms", "factor_nnzb", "factor_levels",
@@ -360,13 +377,16 @@ class LinearBuckling:
     eig_tol): solve(rhs) then extract_eigenvalue / extract_eigenvector."""
 
     def __init__(self, assembler: Assembler, sigma, max_lanczos=100, num_eigvals=10,
-                 eig_tol=1e-10, lev_fill=1000000, precision=64, seed=0, block_size=8):
+                 eig_tol=1e-10, lev_fill=1000000, precision=64, seed=0, block_size=8,
+                 gmres_m=30, gmres_restarts=15, gmres_rtol=1e-12, gmres_atol=1e-30):
         self.a = assembler
         self.lib = assembler.lib
         o = BucklingOpts()
         self.lib.a2ds_buckling_default_opts(ctypes.byref(o))
         o.sigma, o.max_lanczos, o.num_eigvals, o.eig_tol = sigma, max_lanczos, num_eigvals, eig_tol
         o.lev_fill, o.precision, o.seed, o.block_size = lev_fill, precision, seed, block_size
+        o.gmres_m, o.gmres_restarts = gmres_m, gmres_restarts
+        o.gmres_rtol, o.gmres_atol = gmres_rtol, gmres_atol
         self.opts = o
         self.eigvals = self.errors = self.eigvecs = self.path = None
 

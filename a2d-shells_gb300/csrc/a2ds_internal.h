@@ -84,6 +84,14 @@ struct ElemLaunch {
   double *vals;          // BCSR values (36 per block) or NULL
   double *res;           // residual (Nn x 6) or NULL
   int atomic_scatter;    // 1 atomics, 0 plain adds (colour-ordered launch)
+  // Design sensitivities: dconst = 1 evaluates the matrix with the thickness
+  // derivative of the constitutive matrix (the element matrices are linear
+  // in it); cout != NULL replaces the scatter by the contraction
+  // cout[group(e)] += ccoef * cx_e^T M_e cy_e (cx, cy node-major, matrix ordering).
+  int dconst;
+  const double *cx, *cy;
+  double *cout;
+  double ccoef;
 };
 
 int launch_element_kernel(const ElemLaunch &L, cudaStream_t s);

@@ -274,6 +274,24 @@ __device__ __forceinline__ Stiff d_stiff(double E, double nu, double t) {
   c.drill = 0.5 * 10.0 * (c.As + c.As);
   return c;
 }
+// d/dt of d_stiff: A' = Q, D' = t^2/4 Q, As' = 5/6 G, drill' = 10 As'
+// (TACSIsoShellConstitutive::addStressDVSens, TACSIsoShellConstitutive.cpp:229-251).
+__device__ __forceinline__ Stiff d_stiff_dt(double E, double nu, double t) {
+  Stiff c;
+  double Q = E / (1.0 - nu * nu), G = 0.5 * E / (1.0 + nu);
+  double I = 0.25 * t * t;
+  c.A0 = Q;
+  c.A1 = nu * Q;
+  c.A3 = Q;
+  c.A5 = G;
+  c.D0 = I * Q;
+  c.D1 = I * (nu * Q);
+  c.D3 = I * Q;
+  c.D5 = I * G;
+  c.As = (5.0 / 6.0) * c.A5;
+  c.drill = 0.5 * 10.0 * (c.As + c.As);
+  return c;
+}
 __device__ __forceinline__ void d_stress(const Stiff &c, const double *e, double *s) {
   s[0] = c.A0 * e[0] + c.A1 * e[1];
   s[1] = c.A1 * e[0] + c.A3 * e[1];
@@ -353,7 +371,7 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
       S.st[i] = (NEED_STATE && L.state) ? L.state[(size_t)conn[i / 6] * 6 + i % 6] : 0.0;
   }
   const double t = active ? L.tvals[L.tgroup[e]] : 1.0;
-  const Stiff C = d_stiff(L.E, L.nu, t);
+  const Stiff C = L.dconst ? d_stiff_dt(L.E, L.nu, t) : d_stiff(L.E, L.nu, t);
   esync<O>();
 
   // ---- node normals and node frames (TacsShellComputeNodeNormals,
@@ -813,6 +831,27 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
   }
 
   if (!active) return;
+
+  // ---- contraction cx^T M_e cy into the element's design group (a warp
+  //      belongs to one element: reduce in the warp, one atomic per warp)
+  if (NEED_MAT && L.cout) {
+    double v = 0.0;
+#pragma unroll
+    for (int m = 0; m < D::EPT; m++) {
+      int idx = tid + TPE * m;
+      if (idx < D::NTRI) {
+        int a, b;
+        tri_ab(idx, a, b);
+        const size_t ga = (size_t)conn[a / 6] * 6 + a % 6, gb = (size_t)conn[b / 6] * 6 + b % 6;
+        const double xy = (a == b) ? L.cx[ga] * L.cy[ga] : L.cx[ga] * L.cy[gb] + L.cx[gb] * L.cy[ga];
+        v += acc[m] * xy;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(L.cout + L.tgroup[e], L.ccoef * v);
+    return;
+  }
 
   // ---- scatter into the BCSR blocks (mirrored)
   if (NEED_MAT && L.vals) {

@@ -71,6 +71,18 @@ __global__ void k_zero_bc(double *x, const int *bc_rows, const int *bc_masks, in
   if (bc_masks[b] & (1 << k)) x[(size_t)bc_rows[b] * 6 + k] = 0.0;
 }
 
+// column c of an n6 x p row-major block <-> a contiguous vector
+__global__ void k_col_get(const double *X, int p, int c, double *v, size_t n6) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n6;
+       i += (size_t)gridDim.x * blockDim.x)
+    v[i] = X[i * p + c];
+}
+__global__ void k_col_put(double *X, int p, int c, const double *v, size_t n6) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n6;
+       i += (size_t)gridDim.x * blockDim.x)
+    X[i * p + c] = v[i];
+}
+
 // out[j] = sum_i X[j][i] * y[i] for j < m (X rows are vectors of length n);
 // block partial sums then one atomic add per (block, j).
 __global__ void __launch_bounds__(256) k_multidot(const double *X, size_t ldx, int m,
@@ -557,6 +569,145 @@ static int cholqr2(Mesh &m, BucklingState &S, double *W, double *KW, int p,
   return 0;
 }
 
+// ------------------------------------------------------------------ GMRES
+// Right-preconditioned restarted GMRES(msub), GMRES::solve
+// (src/bpmat/KSM.cpp:785-970) with a zero initial guess: Arnoldi vectors
+// W_i, Givens rotations on the Hessenberg columns, stop when the residual
+// estimate drops below atol or rtol times the first residual, x += M^{-1}
+// (sum_i y_i W_i) at the end of every cycle.  The orthogonalisation is two
+// classical Gram-Schmidt passes (two reductions per step on the GPU) where
+// the reference uses modified Gram-Schmidt (one reduction per basis vector);
+// both give an orthogonal basis to working precision.  Vectors are
+// row-ordered device vectors; pc may be NULL (no preconditioner).
+struct GmresWork {
+  DBuf<double> W, work, px, py, dH;
+  DBuf<float> w32;
+};
+
+static int gmres_pc(Mesh &m, Factor *pc, GmresWork &g, const double *src, double *dst) {
+  const size_t n6 = (size_t)m.nn * 6;
+  if (!pc) {
+    A2DS_CUDA_TRY(cudaMemcpyAsync(dst, src, n6 * sizeof(double), cudaMemcpyDeviceToDevice, m.stream));
+    return 0;
+  }
+  A2DS_CUDA_TRY(cudaMemcpyAsync(g.px.p, src, n6 * sizeof(double), cudaMemcpyDeviceToDevice, m.stream));
+  int rc;
+  if (pc->precision == 32) {
+    if ((rc = g.w32.alloc(n6))) return rc;
+    k_f64_to_f32<<<grid_for(n6), 256, 0, m.stream>>>(g.w32.p, g.px.p, n6);
+    if ((rc = solve_graph<float, float>(*pc, pc->F32.p, g.w32.p, g.w32.p, 1, m.stream, &m.launches)))
+      return rc;
+    A2DS_CUDA_TRY(cudaMemsetAsync(dst, 0, n6 * sizeof(double), m.stream));
+    k_add_f32<<<grid_for(n6), 256, 0, m.stream>>>(dst, g.w32.p, n6);
+    A2DS_CUDA_TRY(cudaGetLastError());
+    return 0;
+  }
+  if ((rc = solve_graph<double, double>(*pc, pc->F64.p, g.px.p, g.py.p, 1, m.stream, &m.launches)))
+    return rc;
+  A2DS_CUDA_TRY(cudaMemcpyAsync(dst, g.py.p, n6 * sizeof(double), cudaMemcpyDeviceToDevice, m.stream));
+  return 0;
+}
+
+static int gmres_device(Mesh &m, Factor *pc, const double *Avals, const double *b, double *x,
+                        int msub, int nrestart, double rtol, double atol, GmresWork &g, Blas &B,
+                        int *iters, double *res_norm) {
+  const size_t n6 = (size_t)m.nn * 6;
+  int rc;
+  if ((rc = g.W.alloc((size_t)(msub + 1) * n6)) || (rc = g.work.alloc(n6)) ||
+      (rc = g.px.alloc(n6)) || (rc = g.py.alloc(n6)) || (rc = g.dH.alloc((size_t)msub + 1)))
+    return rc;
+  std::vector<double> H((size_t)(msub + 1) * msub, 0.0), res(msub + 1), qc(msub), qs(msub);
+  std::vector<double> h1(msub + 1), h2(msub + 1);
+  auto Hc = [&](int row, int col) -> double & { return H[(size_t)col * (msub + 1) + row]; };
+  double rhs_norm = 0.0, resnorm = 0.0;
+  int total = 0, flag = 0;
+  for (int count = 0; count < nrestart + 1; count++) {
+    if (count == 0) {
+      A2DS_CUDA_TRY(cudaMemsetAsync(x, 0, n6 * sizeof(double), m.stream));
+      A2DS_CUDA_TRY(cudaMemcpyAsync(g.W.p, b, n6 * sizeof(double), cudaMemcpyDeviceToDevice, m.stream));
+      res[0] = sqrt(B.dot(g.W.p, g.W.p, n6));
+      if (res[0] > 0) B.scale(g.W.p, 1.0 / res[0], n6);
+    } else {
+      if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, Avals, x, g.W.p, m.stream))) return rc;
+      m.launches++;
+      B.axpby(g.W.p, -1.0, b, 1.0, n6);  // W0 = A x - b
+      res[0] = sqrt(B.dot(g.W.p, g.W.p, n6));
+      if (res[0] > 0) B.scale(g.W.p, -1.0 / res[0], n6);
+    }
+    if (count == 0) rhs_norm = res[0];
+    resnorm = res[0];
+    if (res[0] < atol) {
+      flag = 1;
+      break;
+    }
+    int niters = 0;
+    for (int i = 0; i < msub; i++) {
+      double *Wi = g.W.p + (size_t)i * n6, *Wn = g.W.p + (size_t)(i + 1) * n6;
+      if ((rc = gmres_pc(m, pc, g, Wi, g.work.p))) return rc;
+      if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, Avals, g.work.p, Wn, m.stream))) return rc;
+      m.launches++;
+      for (int pass = 0; pass < 2; pass++) {
+        std::vector<double> &h = pass ? h2 : h1;
+        if ((rc = blk_dots(g.W.p, i + 1, n6, Wn, n6, 1, g.dH.p, m.stream))) return rc;
+        if ((rc = blk_sub(Wn, g.W.p, i + 1, n6, g.dH.p, n6, 1, m.stream))) return rc;
+        m.launches += 2;
+        A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), g.dH.p, (i + 1) * sizeof(double),
+                                      cudaMemcpyDeviceToHost, m.stream));
+      }
+      const double hn = sqrt(B.dot(Wn, Wn, n6));  // synchronises: h1, h2 ready
+      for (int k = 0; k <= i; k++) Hc(k, i) = h1[k] + h2[k];
+      Hc(i + 1, i) = hn;
+      if (hn > 0) B.scale(Wn, 1.0 / hn, n6);
+      for (int k = 0; k < i; k++) {
+        const double a = Hc(k, i), c = Hc(k + 1, i);
+        Hc(k, i) = a * qc[k] + c * qs[k];
+        Hc(k + 1, i) = -a * qs[k] + c * qc[k];
+      }
+      {
+        const double a = Hc(i, i), c = Hc(i + 1, i);
+        const double sq = sqrt(a * a + c * c);
+        qc[i] = a / sq;
+        qs[i] = c / sq;
+        Hc(i, i) = a * qc[i] + c * qs[i];
+        Hc(i + 1, i) = -a * qs[i] + c * qc[i];
+        const double r = res[i];
+        res[i] = r * qc[i];
+        res[i + 1] = -r * qs[i];
+      }
+      niters++;
+      resnorm = fabs(res[i + 1]);
+      if (resnorm < atol || resnorm < rtol * rhs_norm) {
+        flag = 1;
+        break;
+      }
+    }
+    total += niters;
+    for (int i = niters - 1; i >= 0; i--) {
+      for (int j = i + 1; j < niters; j++) res[i] -= Hc(i, j) * res[j];
+      res[i] /= Hc(i, i);
+    }
+    // work = sum_i res_i W_i ; x += M^{-1} work
+    A2DS_CUDA_TRY(cudaMemsetAsync(g.work.p, 0, n6 * sizeof(double), m.stream));
+    std::vector<double> neg(niters);
+    for (int i = 0; i < niters; i++) neg[i] = -res[i];
+    if (niters > 0) {
+      A2DS_CUDA_TRY(cudaMemcpyAsync(g.dH.p, neg.data(), niters * sizeof(double),
+                                    cudaMemcpyHostToDevice, m.stream));
+      if ((rc = blk_sub(g.work.p, g.W.p, niters, n6, g.dH.p, n6, 1, m.stream))) return rc;
+      m.launches++;
+      A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // neg is pageable host memory
+    }
+    if ((rc = gmres_pc(m, pc, g, g.work.p, g.W.p))) return rc;
+    B.axpby(x, 1.0, g.W.p, 1.0, n6);
+    if (flag) break;
+  }
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  if (iters) *iters = total;
+  if (res_norm) *res_norm = resnorm;
+  return flag ? 0 : fail(A2DS_ERR_NOCONV, "GMRES did not reach the tolerance (residual " +
+                                             std::to_string(resnorm) + ")");
+}
+
 }  // namespace a2ds
 
 using namespace a2ds;
@@ -648,6 +799,28 @@ int a2ds_pc_apply_multi(a2ds_pc pc, int nrhs, const double *x, double *y) {
   return 0;
 }
 
+int a2ds_gmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rtol, double atol,
+                     const double *b, double *x, int *iters, double *res_norm) {
+  if (!A || !b || !x) return fail(A2DS_ERR_ARG, "null argument");
+  if (msub < 1 || nrestart < 0) return fail(A2DS_ERR_ARG, "need msub >= 1 and nrestart >= 0");
+  if (pc && pc->mat->mesh != A->mesh) return fail(A2DS_ERR_ARG, "preconditioner of another mesh");
+  Mesh &m = A->mesh->m;
+  DBuf<double> db, dx;
+  int rc;
+  if ((rc = m.to_rows(b, db)) || (rc = dx.alloc((size_t)m.nn * 6))) return rc;
+  GmresWork g;
+  Blas B{m.stream};
+  B.launches = &m.launches;
+  int it = 0;
+  double rn = 0.0;
+  rc = gmres_device(m, pc ? &pc->f : nullptr, A->vals.p, db.p, dx.p, msub, nrestart, rtol, atol, g,
+                    B, &it, &rn);
+  if (iters) *iters = it;
+  if (res_norm) *res_norm = rn;
+  int rc2 = m.from_rows(dx.p, x);
+  return rc ? rc : rc2;
+}
+
 int a2ds_pc_get(a2ds_pc pc, int *nrows, int *nnzb, int *rowp, int *cols, double *vals) {
   if (!pc) return fail(A2DS_ERR_ARG, "null preconditioner");
   Factor &f = pc->f;
@@ -721,7 +894,8 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     // or double-float when the shifted factor is double-float too; an FP32
     // factor of K is too coarse for this (cond(K) ~ 1e11)
     if ((rc = factor_setup(m, opts->lev_fill, opts->precision == 48 ? 48 : 64, Sp->fk))) return rc;
-    if ((rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa))) return rc;
+    if (opts->lev_fill >= m.nn && (rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa)))
+      return rc;
   }
   BucklingState &S = *Sp;
   S.sigma = opts->sigma;
@@ -773,8 +947,22 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // h is pageable and goes out of scope
   }
   int inner = 0;
-  if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.rhs.p, S.path.p, 1, 1e-13, 4, &inner)))
-    return rc;
+  // complete factors: direct solves with FP64 refinement; incomplete (ILU(k))
+  // factors: the reference's GMRES preconditioned by the factor of K, on K
+  // for the path and on K + sigma G inside the shift-invert operator
+  const bool direct = opts->lev_fill >= m.nn;
+  GmresWork gw;
+  if (direct) {
+    if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.rhs.p, S.path.p, 1, 1e-13, 4, &inner)))
+      return rc;
+  } else {
+    int it = 0;
+    double rn = 0.0;
+    if ((rc = gmres_device(m, &S.fk, S.K.p, S.rhs.p, S.path.p, opts->gmres_m, opts->gmres_restarts,
+                           opts->gmres_rtol, opts->gmres_atol, gw, B, &it, &rn)))
+      return rc;
+    inner += it;
+  }
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   double t_path = now() - ta;
 
@@ -792,9 +980,9 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     return rc;
   m.launches += 2;
   A2DS_CUDA_TRY(cudaEventRecord(S.ev[2], m.stream));
-  if ((rc = factor_numeric(m, S.fa, S.Aux.p, nullptr, 0.0))) return rc;
+  if (direct && (rc = factor_numeric(m, S.fa, S.Aux.p, nullptr, 0.0))) return rc;
   A2DS_CUDA_TRY(cudaEventRecord(S.ev[3], m.stream));
-  if ((rc = factor_check(m, S.fa))) return rc;
+  if (direct && (rc = factor_check(m, S.fa))) return rc;
   double t_fa = now() - ta;
 
   // 4. block Lanczos on A^{-1} K with the K inner product
@@ -833,7 +1021,22 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
     double *KQj = S.KQ.p + (size_t)j * bs;
     double *W = S.Q.p + (size_t)(j + 1) * bs, *KW = S.KQ.p + (size_t)(j + 1) * bs;
     // W = A^{-1} K Q_j
-    if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, 1e-10, 2, &inner))) return rc;
+    if (direct) {
+      if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, 1e-10, 2, &inner))) return rc;
+    } else {
+      for (int c = 0; c < p; c++) {  // one GMRES solve per block column
+        k_col_get<<<grid_for(n6), 256, 0, m.stream>>>(KQj, p, c, S.r.p, n6);
+        int it = 0;
+        double rn = 0.0;
+        if ((rc = gmres_device(m, &S.fk, S.Aux.p, S.r.p, S.t.p, opts->gmres_m,
+                               opts->gmres_restarts, opts->gmres_rtol, opts->gmres_atol, gw, B,
+                               &it, &rn)))
+          return rc;
+        k_col_put<<<grid_for(n6), 256, 0, m.stream>>>(W, p, c, S.t.p, n6);
+        m.launches += 2;
+        inner += it;
+      }
+    }
     if ((rc = blk_zero_bc(W, p, m.d_bc_rows.p, m.d_bc_masks.p, nbc, m.stream))) return rc;
     // full K-orthogonalisation against blocks 0..j, two classical passes
     if ((rc = blk_dots(S.KQ.p, j + 1, bs, W, n6, p, S.dH1.p, m.stream))) return rc;
@@ -942,7 +1145,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   cudaEventElapsedTime(&ms_fk, S.ev[4], S.ev[5]);
   m.stats = {total, t_k, t_g, t_fk + t_fa, t_path, t_lan, (double)mdim, (double)inner,
              (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
-             (double)S.fa.nnzb(), (double)S.fa.flv.nlevels, (double)S.fa.flops(), (double)p,
+             (double)S.fk.nnzb(), (double)S.fk.flv.nlevels, (double)S.fk.flops(), (double)p,
              (double)nsteps, S.solve_ms(), (double)(S.ntev / 2)};
   if (!converged) return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
   return 0;
@@ -955,8 +1158,80 @@ int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out) {
   return 0;
 }
 
-int a2ds_eig_sens_thickness(a2ds_mesh, int, double *) {
-  return fail(A2DS_ERR_STATE, "eigenvalue sensitivities are not available yet");
+int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt) {
+  if (!mesh || !dlam_dt) return fail(A2DS_ERR_ARG, "null argument");
+  Mesh &m = mesh->m;
+  BucklingState *Sp = (BucklingState *)m.solver;
+  if (!Sp || Sp->lam.empty())
+    return fail(A2DS_ERR_STATE, "eigenvalue sensitivities need a preceding a2ds_buckling_solve");
+  BucklingState &S = *Sp;
+  if (n < 0 || n >= (int)S.lam.size()) return fail(A2DS_ERR_ARG, "eigenvalue index out of range");
+  if (m.alpha * m.temperature != 0.0)
+    return fail(A2DS_ERR_ARG, "thickness sensitivities of thermal buckling loads are not supported");
+  const size_t n6 = (size_t)m.nn * 6;
+  const int ng = (int)m.tvals.size();
+  const double lam = S.lam[n];
+  const double *phi = S.phi.p + (size_t)n * n6;
+  const int nbc = (int)m.bc_rows.size();
+  Blas B{m.stream};
+  B.launches = &m.launches;
+  int rc;
+  // phi^T G phi (phi vanishes on the Dirichlet DOFs)
+  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, phi, S.r.p, m.stream))) return rc;
+  m.launches++;
+  const double phiGphi = B.dot(phi, S.r.p, n6);
+  if (!(phiGphi != 0.0) || !std::isfinite(phiGphi))
+    return fail(A2DS_ERR_NUMERIC, "phi^T G phi vanishes");
+  // adjoint: K psi = d(phi^T G(path) phi)/d(path) = G(phi) phi (the third
+  // derivative of the strain energy is symmetric), Dirichlet rows zeroed
+  if ((rc = m.assemble_device(MODE_G, phi, S.Aux.p, nullptr, A2DS_SCATTER_ATOMIC))) return rc;
+  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.Aux.p, phi, S.t.p, m.stream))) return rc;
+  m.launches++;
+  if (nbc) {
+    k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.t.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
+    m.launches++;
+  }
+  DBuf<double> psi, dd;
+  if ((rc = psi.alloc(n6)) || (rc = dd.alloc(ng))) return rc;
+  int inner = 0;
+  if (S.lev_fill >= m.nn) {
+    if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.t.p, psi.p, 1, 1e-13, 4, &inner))) return rc;
+  } else {
+    GmresWork gw;
+    double rn = 0.0;
+    if ((rc = gmres_device(m, &S.fk, S.K.p, S.t.p, psi.p, 30, 15, 1e-12, 1e-30, gw, B, &inner, &rn)))
+      return rc;
+  }
+  // dlam/dt_g = -[phi^T K' phi + lam phi^T G'(path) phi - lam psi^T K' path] / phi^T G phi,
+  // ' = d/dt_g (element matrices with the derivative constitutive matrix)
+  A2DS_CUDA_TRY(cudaMemsetAsync(dd.p, 0, ng * sizeof(double), m.stream));
+  ElemLaunch L = m.launch_params(MODE_K, nullptr, nullptr, nullptr);
+  L.dconst = 1;
+  L.cout = dd.p;
+  L.cx = phi;
+  L.cy = phi;
+  L.ccoef = 1.0;
+  if ((rc = launch_element_kernel(L, m.stream))) return rc;
+  L = m.launch_params(MODE_G, S.path.p, nullptr, nullptr);
+  L.dconst = 1;
+  L.cout = dd.p;
+  L.cx = phi;
+  L.cy = phi;
+  L.ccoef = lam;
+  if ((rc = launch_element_kernel(L, m.stream))) return rc;
+  L = m.launch_params(MODE_K, nullptr, nullptr, nullptr);
+  L.dconst = 1;
+  L.cout = dd.p;
+  L.cx = psi.p;
+  L.cy = S.path.p;
+  L.ccoef = -lam;
+  if ((rc = launch_element_kernel(L, m.stream))) return rc;
+  m.launches += 3;
+  std::vector<double> h(ng);
+  A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), dd.p, ng * sizeof(double), cudaMemcpyDeviceToHost, m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  for (int g = 0; g < ng; g++) dlam_dt[g] = -h[g] / phiGphi;
+  return 0;
 }
 
 }  // extern "C"

@@ -215,6 +215,17 @@ int a2ds_pc_apply_multi(a2ds_pc pc, int nrhs, const double *x, double *y);
 int a2ds_pc_get(a2ds_pc pc, int *nrows, int *nnzb, int *rowp, int *cols,
                 double *vals);
 
+/* GMRES(mat, pc, msub, nrestart, isFlexible = 0) with setTolerances(rtol,
+   atol) and solve(b, x, zero_guess = 1) (src/bpmat/KSM.cpp:547-645,
+   785-970): right-preconditioned restarted GMRES on A with the factor of pc
+   (NULL: no preconditioner).  b and x are node-ordered num_nodes x 6 host
+   vectors.  *iters receives the total inner iterations and *res_norm the
+   final residual estimate; A2DS_ERR_NOCONV if the tolerance was not met
+   (x then holds the last iterate). */
+int a2ds_gmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rtol,
+                     double atol, const double *b, double *x, int *iters,
+                     double *res_norm);
+
 /* --------------------------------------------------------- buckling solve */
 typedef struct {
   double sigma;          /* spectral shift (TACSLinearBuckling ctor) */

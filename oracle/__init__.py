@@ -189,6 +189,24 @@ def factor(rowp, cols, vals, frowp, fcols, fdiag):
     return F
 
 
+def gmres(rowp, cols, A, frowp, fcols, fdiag, F, m, nrestart, rtol, atol, b):
+    """GMRES::solve (src/bpmat/KSM.cpp:785-970) on the CPU: right
+    preconditioned by the factor F, zero initial guess.  Returns (x, iterations)."""
+    lib = load()
+    _declare_solver(lib)
+    n = rowp.size - 1
+    args = [np.ascontiguousarray(v, np.int32) for v in (rowp, cols, frowp, fcols, fdiag)]
+    A = np.ascontiguousarray(A, np.float64)
+    F = np.ascontiguousarray(F, np.float64)
+    sysA = _System(n, _pi(args[0]), _pi(args[1]), _p(A), _pi(args[2]), _pi(args[3]),
+                   _pi(args[4]), _p(F))
+    b = np.ascontiguousarray(b, np.float64).ravel()
+    x = np.zeros_like(b)
+    it = lib.orc_gmres(ctypes.byref(sysA), int(m), int(nrestart), float(rtol), float(atol),
+                       _p(b), _p(x))
+    return x, it
+
+
 class CpuBuckling:
     """The reference's buckling path on the CPU (TACSLinearBuckling::solve
     with a TACSSchurPc factor of K and GMRES on K + sigma G), timed phase by
