@@ -26,7 +26,11 @@ LIB_PATH = os.path.join(PKG, "lib", "liba2ds_gpu.so")
 A2DS_STIFFNESS_MATRIX = 0
 A2DS_GEOMETRIC_STIFFNESS_MATRIX = 2
 A2DS_NATURAL_ORDER = 0
+A2DS_RCM_ORDER = 1
+A2DS_AMD_ORDER = 2
+A2DS_ND_ORDER = 3
 A2DS_TACS_AMD_ORDER = 4
+A2DS_MULTICOLOR_ORDER = 5
 A2DS_SCATTER_ATOMIC = 0
 A2DS_SCATTER_COLORED = 1
 

@@ -146,8 +146,12 @@ int a2ds_mesh_plan(a2ds_mesh mesh, int order_type) {
   if (rc) return rc;
   Mesh &m = mesh->m;
   if (m.planned) return fail(A2DS_ERR_STATE, "mesh already planned");
-  if (order_type != A2DS_NATURAL_ORDER && order_type != A2DS_TACS_AMD_ORDER)
-    return fail(A2DS_ERR_ARG, "order_type must be A2DS_NATURAL_ORDER or A2DS_TACS_AMD_ORDER");
+  if (order_type == A2DS_ND_ORDER)
+    return fail(A2DS_ERR_ARG, "A2DS_ND_ORDER needs METIS (METIS_NodeND), which is not available");
+  if (order_type != A2DS_NATURAL_ORDER && order_type != A2DS_RCM_ORDER &&
+      order_type != A2DS_AMD_ORDER && order_type != A2DS_TACS_AMD_ORDER &&
+      order_type != A2DS_MULTICOLOR_ORDER)
+    return fail(A2DS_ERR_ARG, "unknown order_type");
   m.order_type = order_type;
   if ((rc = m.build_pattern())) return rc;
   m.planned = true;

@@ -421,4 +421,74 @@ int amd_order(int n, std::vector<int> &rowp, std::vector<int> &cols, std::vector
   return 0;
 }
 
+// ------------------------------------------------------------------ RCM
+static int rcm_pass(int nn, const std::vector<int> &rowp, const std::vector<int> &cols, int root,
+                    std::vector<int> &order, std::vector<int> &num) {
+  num.assign(nn, -1);
+  order.assign(nn, 0);
+  int head = 0, tail = 0, count = 0;
+  while (count < nn) {
+    if (head == tail) {
+      // next component: the root first, then the lowest unnumbered node
+      if (num[root] >= 0) {
+        int i = 0;
+        while (i < nn && num[i] >= 0) i++;
+        if (i == nn) return count;
+        root = i;
+      }
+      order[tail++] = root;
+      num[root] = count++;
+    }
+    while (head < tail) {
+      const int level_end = tail;
+      for (; head < level_end; head++) {
+        const int v = order[head];
+        for (int k = rowp[v]; k < rowp[v + 1]; k++) {
+          const int w = cols[k];
+          if (num[w] < 0) {
+            num[w] = count++;
+            order[tail++] = w;
+          }
+        }
+      }
+    }
+  }
+  for (int i = 0; i < count; i++) num[order[i]] = count - 1 - i;
+  return count;
+}
+
+int rcm_order(int nn, const std::vector<int> &rowp, const std::vector<int> &cols, int root,
+              int passes, std::vector<int> &new_vars) {
+  std::vector<int> order;
+  int got = 0;
+  for (int p = 0; p < std::max(passes, 1); p++) {
+    got = rcm_pass(nn, rowp, cols, root, order, new_vars);
+    if (got != nn) return got;
+    root = new_vars[0];
+  }
+  return got;
+}
+
+// -------------------------------------------------------- multicolouring
+int multicolor_order(int nn, const std::vector<int> &rowp, const std::vector<int> &cols,
+                     std::vector<int> &colors, std::vector<int> &new_vars) {
+  colors.assign(nn, -1);
+  std::vector<int> seen(nn + 1, -1);  // seen[c] == i: colour c used next to node i
+  int ncolors = 0;
+  for (int i = 0; i < nn; i++) {
+    for (int k = rowp[i]; k < rowp[i + 1]; k++)
+      if (colors[cols[k]] >= 0) seen[colors[cols[k]]] = i;
+    int c = 0;
+    while (c < ncolors && seen[c] == i) c++;
+    if (c == ncolors) ncolors++;
+    colors[i] = c;
+  }
+  std::vector<int> start(ncolors + 1, 0);
+  for (int i = 0; i < nn; i++) start[colors[i] + 1]++;
+  for (int c = 0; c < ncolors; c++) start[c + 1] += start[c];
+  new_vars.resize(nn);
+  for (int i = 0; i < nn; i++) new_vars[i] = start[colors[i]]++;
+  return ncolors;
+}
+
 }  // namespace a2ds

@@ -58,11 +58,21 @@ int Mesh::build_pattern() {
   // (TACSAssembler::computeLocalNodeToNodeCSR + TacsSortAndUniquifyCSR)
   node_csr(nn, ne, npe, conn.data(), 0, node_rowp, node_cols);
 
+  // TACSAssembler::createSchurMat(order_type) on one process (no coupling
+  // nodes) -> computeMatReordering (src/TACSAssembler.cpp:1508-1600)
   perm.resize(nn);
-  if (order_type == A2DS_TACS_AMD_ORDER) {
+  if (order_type == A2DS_TACS_AMD_ORDER || order_type == A2DS_AMD_ORDER) {
+    // AMD_ORDER without the external AMD library is the same call
     std::vector<int> rp, cl;
     node_csr(nn, ne, npe, conn.data(), 1, rp, cl);
     amd_order(nn, rp, cl, perm);
+  } else if (order_type == A2DS_RCM_ORDER || order_type == A2DS_MULTICOLOR_ORDER) {
+    std::vector<int> new_vars, colors;
+    if (order_type == A2DS_RCM_ORDER)
+      rcm_order(nn, node_rowp, node_cols, 0, 1, new_vars);
+    else
+      multicolor_order(nn, node_rowp, node_cols, colors, new_vars);
+    for (int k = 0; k < nn; k++) perm[new_vars[k]] = k;
   } else {
     std::iota(perm.begin(), perm.end(), 0);
   }

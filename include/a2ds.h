@@ -41,9 +41,16 @@ extern "C" {
 #define A2DS_GEOMETRIC_STIFFNESS_MATRIX 2
 
 /* Node orderings for the matrix, numbered as TACSAssembler::OrderingType
-   (src/TACSAssembler.h:64-71). */
+   (src/TACSAssembler.h:64-71).  RCM: TacsComputeRCMOrder from node 0, one
+   pass; AMD and TACS_AMD: amd_order_interface (one process, no coupling
+   nodes); MULTICOLOR: TacsComputeSerialMultiColor.  ND needs METIS, which is
+   not available (a2ds_mesh_plan returns A2DS_ERR_ARG). */
 #define A2DS_NATURAL_ORDER 0
+#define A2DS_RCM_ORDER 1
+#define A2DS_AMD_ORDER 2
+#define A2DS_ND_ORDER 3
 #define A2DS_TACS_AMD_ORDER 4
+#define A2DS_MULTICOLOR_ORDER 5
 
 /* Scatter strategies for element-to-BCSR assembly. */
 #define A2DS_SCATTER_ATOMIC 0   /* FP64 atomic adds (fastest, order-dependent rounding) */
@@ -109,8 +116,7 @@ int a2ds_mesh_ilu_pattern(a2ds_mesh mesh, int lev_fill, int *nnzb, int *rowp, in
 /* TACSAssembler::initialize (src/TACSAssembler.cpp:2459) plus the matrix
    ordering of createSchurMat(order_type) (src/TACSAssembler.cpp:3453):
    builds the node-to-node pattern, the ordering, the element-slot map and
-   uploads everything.  order_type: A2DS_NATURAL_ORDER or
-   A2DS_TACS_AMD_ORDER. */
+   uploads everything.  order_type: one of the A2DS_*_ORDER values above. */
 int a2ds_mesh_initialize(a2ds_mesh mesh, int order_type);
 
 /* perm[i] = node in row i of every matrix of this mesh (the reference's

@@ -29,6 +29,7 @@
 #include "TACSSchurMat.h"
 #include "TACSShellElementDefs.h"
 #include "TACSShellElementTransform.h"
+#include "TacsUtilities.h"
 
 #ifdef TACS_USE_COMPLEX
 static const char *SUFFIX = "_cs";
@@ -465,11 +466,51 @@ static void run_assembly(const std::string &in, const std::string &out) {
   printf("assembly fixture: nn=%d ne=%d nnzb=%d\n", nn, ne, browp[nrows]);
 }
 
+// Orderings of the node graph (TACSAssembler::computeMatReordering,
+// src/TACSAssembler.cpp:1508-1600): RCM from root 0 with one pass and the
+// serial greedy multicolouring, on the node-to-node CSR with the diagonal.
+static void run_orderings(const std::string &in, const std::string &out) {
+  std::vector<long> xs, cs;
+  std::vector<double> X = read_npy<double>(in + "/X.npy", &xs);
+  std::vector<int> conn = read_npy<int>(in + "/conn.npy", &cs);
+  const int nn = (int)xs[0], ne = (int)cs[0], npe = (int)cs[1];
+  TACSShellTransform *tr = new TACSShellNaturalTransform();
+  tr->incref();
+  TACSMaterialProperties *props =
+      new TACSMaterialProperties(2700.0, 921.0, 70e9, 0.3, 270e6, 0.0, 230.0);
+  props->incref();
+  TACSIsoShellConstitutive *con = new TACSIsoShellConstitutive(props, 1e-2, 0);
+  TACSElement *el = make_element(npe == 4 ? "TACSQuad4Shell" : "TACSQuad9Shell", tr, con);
+  el->incref();
+  std::vector<TACSElement *> elems(ne, el);
+  TACSAssembler *assembler = new TACSAssembler(MPI_COMM_WORLD, 6, nn, ne);
+  assembler->incref();
+  std::vector<int> ptr(ne + 1);
+  for (int e = 0; e <= ne; e++) ptr[e] = npe * e;
+  assembler->setElementConnectivity(ptr.data(), conn.data());
+  assembler->setElements(elems.data());
+  assembler->initialize();
+  int *rowp, *cols;
+  assembler->computeLocalNodeToNodeCSR(&rowp, &cols, 0);
+  std::vector<int> rcm(nn), colors(nn), mc(nn);
+  TacsComputeRCMOrder(nn, rowp, cols, rcm.data(), 0, 1);
+  int ncolors = TacsComputeSerialMultiColor(nn, rowp, cols, colors.data(), mc.data());
+  save_i(out, "rcm_new_vars", rcm.data(), {nn});
+  save_i(out, "mc_colors", colors.data(), {nn});
+  save_i(out, "mc_new_vars", mc.data(), {nn});
+  save_i(out, "mc_ncolors", &ncolors, {1});
+  delete[] rowp;
+  delete[] cols;
+  assembler->decref();
+}
+
 int main(int argc, char **argv) {
   MPI_Init(&argc, &argv);
   TacsInitialize();
   if (argc >= 3 && strcmp(argv[1], "element") == 0) {
     run_elements(argv[2]);
+  } else if (argc >= 4 && strcmp(argv[1], "orderings") == 0) {
+    run_orderings(argv[2], argv[3]);
   } else if (argc >= 4 && strcmp(argv[1], "assembly") == 0) {
     run_assembly(argv[2], argv[3]);
   } else {

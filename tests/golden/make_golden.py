@@ -136,8 +136,34 @@ def run_case(name, m, lev, gm_m, gm_restarts, lanczos, neig, sigma=None, nonline
           "dense", lam_dense[:3], "rel", rel)
 
 
+def make_orderings():
+    """Orderings of the three fixture meshes' node graphs by the reference's
+    own routines (RCM, serial multicolouring, AMD with the diagonal)."""
+    cases = {"cyl_q4_4x8": meshgen.cylinder(4, 8, order=2),
+             "cyl_q4_8x16": meshgen.cylinder(8, 16, order=2),
+             "cyl_q9_2x4": meshgen.cylinder(2, 4, order=3),
+             "cyl_q4_16x32": meshgen.cylinder(16, 32, order=2)}
+    out = {}
+    for name, m in cases.items():
+        with tempfile.TemporaryDirectory() as d:
+            ind, outd = os.path.join(d, "in"), os.path.join(d, "out")
+            os.makedirs(ind)
+            os.makedirs(outd)
+            np.save(os.path.join(ind, "X.npy"), np.ascontiguousarray(m.X, np.float64))
+            np.save(os.path.join(ind, "conn.npy"), np.ascontiguousarray(m.conn, np.int32))
+            subprocess.run([os.path.join(REF_OUT, "golden_gen"), "orderings", ind, outd],
+                           check=True)
+            for k, v in load_dir(outd).items():
+                out[f"{name}__{k}"] = v
+            out[f"{name}__X"] = m.X
+            out[f"{name}__conn"] = m.conn
+    np.savez_compressed(os.path.join(HERE, "orderings.npz"), **out)
+    print("wrote orderings.npz")
+
+
 def main():
     build_reference()
+    make_orderings()
     make_elements()
     run_case("cyl_q4_4x8_lu", meshgen.cylinder(4, 8, order=2), lev=1000000, gm_m=10,
              gm_restarts=15, lanczos=100, neig=50)

@@ -70,3 +70,32 @@ def test_bad_inputs_are_rejected():
         capi.Assembler(X, np.array([[0, 1, 2, 7]]))      # node out of range
     with pytest.raises(capi.A2dsError):
         capi.Assembler(X, np.array([[0, 1, 2]]))         # 3-node element
+
+
+ORDER_CASES = ["cyl_q4_4x8", "cyl_q4_8x16", "cyl_q9_2x4", "cyl_q4_16x32"]
+
+
+@pytest.mark.parametrize("case", ORDER_CASES)
+@pytest.mark.parametrize("order,key", [(capi.A2DS_RCM_ORDER, "rcm_new_vars"),
+                                       (capi.A2DS_MULTICOLOR_ORDER, "mc_new_vars")])
+def test_rcm_and_multicolor_orderings_match_reference(case, order, key):
+    """createSchurMat(RCM_ORDER / MULTICOLOR_ORDER) on one process: the
+    permutation from TacsComputeRCMOrder (root 0, one pass) and
+    TacsComputeSerialMultiColor on the node graph with its diagonal
+    (tests/golden/orderings.npz, written by the reference's own routines)."""
+    f = np.load(os.path.join(GOLDEN, "orderings.npz"))
+    a = capi.Assembler(f[f"{case}__X"], f[f"{case}__conn"])
+    a.plan(order)
+    new_vars = f[f"{case}__{key}"]
+    expect = np.empty_like(new_vars)
+    expect[new_vars] = np.arange(new_vars.size, dtype=new_vars.dtype)
+    assert np.array_equal(a.get_ordering(), expect)
+
+
+def test_amd_order_type_equals_tacs_amd_and_nd_is_refused():
+    f = np.load(os.path.join(GOLDEN, "cyl_q4_8x16_ilu1.npz"))
+    a = _planned(f, capi.A2DS_AMD_ORDER)
+    assert np.array_equal(a.get_ordering(), f["amd_perm"])
+    b = capi.Assembler(f["X"], f["conn"])
+    with pytest.raises(capi.A2dsError, match="METIS"):
+        b.plan(capi.A2DS_ND_ORDER)
