@@ -49,7 +49,7 @@ EXPORTS = [
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
     "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
-    "a2ds_buckling_stats", "a2ds_eig_sens_thickness",
+    "a2ds_buckling_stats", "a2ds_eig_sens_thickness", "a2ds_eigen_shift_invert",
 ]
 
 
@@ -129,6 +129,8 @@ def load(build: bool = False):
     lib.a2ds_buckling_default_opts.restype = None
     lib.a2ds_buckling_solve.argtypes = [VP, ctypes.POINTER(BucklingOpts), P_D, P_D, P_D, P_D, P_D]
     lib.a2ds_buckling_stats.argtypes = [VP, ctypes.c_int, P_D]
+    lib.a2ds_eigen_shift_invert.argtypes = [VP, ctypes.POINTER(BucklingOpts), VP, VP, P_D, P_D,
+                                            P_D]
     lib.a2ds_eig_sens_thickness.argtypes = [VP, ctypes.c_int, P_D]
     _lib = lib
     return lib
@@ -404,6 +406,18 @@ class LinearBuckling:
                                           _d(err), _d(vecs), _d(path))
         # on A2DS_ERR_NOCONV the current Ritz pairs are still returned
         self.eigvals, self.errors, self.eigvecs, self.path = lam, err, vecs, path
+        _check(rc)
+        return lam
+
+    def solve_matrices(self, K: "BCSRMat", G: "BCSRMat", want_vectors=True):
+        """SEP::solve with EPBucklingShiftInvert(sigma, K, G) on given
+        matrices (e.g. K_T(u) and G(u) about a preloaded state)."""
+        n, k = self.a.num_nodes, self.opts.num_eigvals
+        lam, err = np.zeros(k), np.zeros(k)
+        vecs = np.zeros((k, n, 6)) if want_vectors else None
+        rc = self.lib.a2ds_eigen_shift_invert(self.a.h, ctypes.byref(self.opts), K.h, G.h,
+                                              _d(lam), _d(err), _d(vecs))
+        self.eigvals, self.errors, self.eigvecs = lam, err, vecs
         _check(rc)
         return lam
 

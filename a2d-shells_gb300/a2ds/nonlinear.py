@@ -1,0 +1,78 @@
+"""Nonlinear preload and buckling about the preloaded state.
+
+The reference builds no Newton or continuation solver (TACSContinuation and
+TACSIntegrator live only in its archive/); its building blocks are
+TACSAssembler::assembleRes / assembleJacobian (src/TACSAssembler.cpp:4000,
+4084), TACSSchurPc and the nonlinear shell elements
+(TACSQuad4NonlinearShell, src/elements/shell/TACSShellElementDefs.h:27).
+This module is the driver on top of the GB300 library:
+
+* `newton_preload`: equal load increments s_k = load * k / nsteps; at each,
+  full Newton on R(u) = s_k f with the exact tangent K_T(u) (assembleJacobian)
+  factored on the GPU each step;
+* `preload_buckling`: the eigenproblem K_T(u) x + lam G(u) x = 0 about the
+  converged preload u, with G(u) the geometric stiffness along u (stated
+  definition), solved by the library's shift-invert Lanczos.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import capi
+
+
+def _bc_mask_vector(assembler: capi.Assembler, bc_nodes, bc_mask):
+    fixed = np.zeros((assembler.num_nodes, 6), bool)
+    for node, mask in zip(np.asarray(bc_nodes), np.asarray(bc_mask)):
+        for k in range(6):
+            if int(mask) >> k & 1:
+                fixed[node, k] = True
+    return fixed
+
+
+def newton_preload(assembler: capi.Assembler, rhs, bc_nodes, bc_mask, load: float,
+                   nsteps: int = 10, rtol: float = 1e-10, max_newton: int = 25,
+                   precision: int = 64):
+    """Newton load stepping to `load` times the nodal load vector `rhs`
+    (node-major num_nodes x 6).  Returns (u, iterations per step, final
+    relative residual).  Raises RuntimeError if a step does not converge."""
+    f = np.asarray(rhs, float).reshape(-1, 6).copy()
+    fixed = _bc_mask_vector(assembler, bc_nodes, bc_mask)
+    f[fixed] = 0.0
+    u = np.zeros_like(f)
+    KT = assembler.create_mat()
+    pc = None
+    its = []
+    rel = 0.0
+    for k in range(1, nsteps + 1):
+        fk = load * k / nsteps * f
+        fn = max(np.linalg.norm(fk), 1e-300)
+        for it in range(max_newton + 1):
+            res = assembler.assemble_jacobian(KT, u)  # R(u); Dirichlet rows u - u_bc
+            r = res - fk
+            rel = np.linalg.norm(r) / fn
+            if rel <= rtol:
+                its.append(it)
+                break
+            if it == max_newton:
+                raise RuntimeError(f"Newton did not converge in load step {k}: "
+                                   f"relative residual {rel:.3e}")
+            if pc is None:
+                pc = capi.SchurPc(KT, 1000000, precision)
+            pc.factor(KT)
+            u = u - pc.apply_factor(r)
+    return u, its, rel
+
+
+def preload_buckling(assembler: capi.Assembler, u, sigma: float, num_eigvals: int = 5,
+                     max_lanczos: int = 120, eig_tol: float = 1e-10, precision: int = 64,
+                     block_size: int = 8):
+    """Lowest buckling multipliers about the preloaded state u:
+    K_T(u) x + lam G(u) x = 0.  Returns (lam, LinearBuckling handle)."""
+    KT, G = assembler.create_mat(), assembler.create_mat()
+    assembler.assemble_jacobian(KT, u, want_res=False)
+    assembler.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, u)
+    b = capi.LinearBuckling(assembler, sigma, max_lanczos=max_lanczos, num_eigvals=num_eigvals,
+                            eig_tol=eig_tol, precision=precision, block_size=block_size)
+    lam = b.solve_matrices(KT, G)
+    return lam, b, KT, G

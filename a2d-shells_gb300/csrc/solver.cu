@@ -712,6 +712,243 @@ static int gmres_device(Mesh &m, Factor *pc, const double *Avals, const double *
 
 using namespace a2ds;
 
+// Checks of the options and the per-mesh solver state (factor set-up on the
+// first call or when the fill level or precision change) and buffers.
+static int prepare_solve(Mesh &m, const a2ds_buckling_opts *opts, BucklingState **out) {
+  if (!m.initialized) return fail(A2DS_ERR_STATE, "mesh not initialized");
+  const int nev = opts->num_eigvals, mmax = opts->max_lanczos, p = opts->block_size;
+  if (p != 1 && p != 2 && p != 4 && p != 8 && p != 16)
+    return fail(A2DS_ERR_ARG, "block_size must be 1, 2, 4, 8 or 16");
+  const int nbmax = mmax / p;  // block steps; basis dimension <= max_lanczos
+  if (nev <= 0 || nbmax < 1 || nbmax * p < nev)
+    return fail(A2DS_ERR_ARG, "need 0 < num_eigvals <= max_lanczos and block_size <= max_lanczos");
+  // any nonzero shift (negative shifts target the negative side of a
+  // two-sided spectrum, e.g. thermal buckling)
+  if (!(opts->sigma != 0.0) || !std::isfinite(opts->sigma))
+    return fail(A2DS_ERR_ARG, "sigma must be nonzero and finite");
+  if (opts->precision != 64 && opts->precision != 48 && opts->precision != 32)
+    return fail(A2DS_ERR_ARG, "precision must be 64, 48 or 32");
+  const size_t n6 = (size_t)m.nn * 6;
+  const size_t nv = (size_t)m.nnzb * 36;
+  const size_t bs = n6 * p;  // doubles per basis block
+  int rc;
+
+  BucklingState *Sp = (BucklingState *)m.solver;
+  if (!Sp || Sp->lev_fill != opts->lev_fill || Sp->precision != opts->precision) {
+    delete Sp;
+    Sp = new BucklingState();
+    m.solver = Sp;
+    Sp->lev_fill = opts->lev_fill;
+    Sp->precision = opts->precision;
+    // K's factor serves the load-path solve (FP64 refinement to 1e-13): FP64,
+    // or double-float when the shifted factor is double-float too; an FP32
+    // factor of K is too coarse for this (cond(K) ~ 1e11)
+    if ((rc = factor_setup(m, opts->lev_fill, opts->precision == 48 ? 48 : 64, Sp->fk))) return rc;
+    if (opts->lev_fill >= m.nn && (rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa)))
+      return rc;
+  }
+  BucklingState &S = *Sp;
+  S.sigma = opts->sigma;
+  S.ntev = 0;
+  if ((rc = S.K.alloc(nv)) || (rc = S.G.alloc(nv)) || (rc = S.Aux.alloc(nv))) return rc;
+  if ((rc = S.Q.alloc((size_t)(nbmax + 1) * bs)) || (rc = S.KQ.alloc((size_t)(nbmax + 1) * bs)))
+    return rc;
+  if ((rc = S.Xb.alloc(bs)) || (rc = S.Yb.alloc(bs)) || (rc = S.dH1.alloc((size_t)nbmax * p * p)) ||
+      (rc = S.dH2.alloc((size_t)nbmax * p * p)) || (rc = S.dN.alloc((size_t)p * p)) ||
+      (rc = S.dM.alloc((size_t)p * p)) || (rc = S.phi.alloc((size_t)nev * n6)) ||
+      (rc = S.r.alloc(n6)) || (rc = S.t.alloc(n6)) || (rc = S.path.alloc(n6)) ||
+      (rc = S.rhs.alloc(n6)))
+    return rc;
+  (void)S;
+  *out = Sp;
+  return 0;
+}
+
+// A = K + sigma G (identity Dirichlet rows), its factor (complete fill) and
+// the block shift-invert Lanczos on A^{-1} K with the K inner product
+// (EPBucklingShiftInvert + SEP::solve, src/bpmat/GSEP.cpp:200-244,485-596);
+// S.K and S.G hold the matrices.  Fills eigvals / errors / eigvecs (host,
+// node order) and the Ritz vectors in S.phi.
+struct PhaseOut {
+  double t_fa = 0.0, t_lan = 0.0;
+  int mdim = 0, nsteps = 0, converged = 0;
+};
+static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opts *opts,
+                              Blas &B, bool direct, GmresWork &gw, int &inner, double *eigvals,
+                              double *errors, double *eigvecs, PhaseOut &out) {
+  const int nev = opts->num_eigvals, p = opts->block_size, nbmax = opts->max_lanczos / p;
+  const size_t n6 = (size_t)m.nn * 6, nv = (size_t)m.nnzb * 36, bs = n6 * p;
+  int rc;
+  double ta;
+  ta = now();
+  A2DS_CUDA_TRY(cudaMemcpyAsync(S.Aux.p, S.K.p, nv * sizeof(double), cudaMemcpyDeviceToDevice,
+                                m.stream));
+  if ((rc = launch_axpy(S.Aux.p, S.sigma, S.G.p, nv, m.stream))) return rc;
+  if ((rc = launch_apply_bc_rows(S.Aux.p, m.d_rowp.p, m.d_cols.p, m.d_bc_rows.p, m.d_bc_masks.p,
+                                 (int)m.bc_rows.size(), m.stream)))
+    return rc;
+  m.launches += 2;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[2], m.stream));
+  if (direct && (rc = factor_numeric(m, S.fa, S.Aux.p, nullptr, 0.0))) return rc;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[3], m.stream));
+  if (direct && (rc = factor_check(m, S.fa))) return rc;
+  out.t_fa = now() - ta;
+
+  // 4. block Lanczos on A^{-1} K with the K inner product
+  ta = now();
+  const int nbc = (int)m.bc_rows.size();
+  {
+    // seeded start block (splitmix64), BC DOFs zeroed, K-orthonormalised
+    std::vector<double> h(bs);
+    uint64_t st = 0x9E3779B97F4A7C15ull * (uint64_t)(opts->seed + 1);
+    for (size_t i = 0; i < bs; i++) {
+      uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      z ^= z >> 31;
+      h[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    }
+    A2DS_CUDA_TRY(cudaMemcpyAsync(S.Q.p, h.data(), bs * sizeof(double), cudaMemcpyHostToDevice,
+                                  m.stream));
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  }
+  if ((rc = blk_zero_bc(S.Q.p, p, m.d_bc_rows.p, m.d_bc_masks.p, nbc, m.stream))) return rc;
+  if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, S.Q.p, nullptr, S.KQ.p, p, m.stream)))
+    return rc;
+  m.launches += 2;
+  std::vector<double> Bj;
+  if ((rc = cholqr2(m, S, S.Q.p, S.KQ.p, p, Bj))) return rc;
+
+  const int tdim = (nbmax + 1) * p;
+  std::vector<double> T((size_t)tdim * tdim, 0.0), h1((size_t)p * p), h2((size_t)p * p);
+  std::vector<double> Tw, TV, Tm;
+  std::vector<int> order;
+  auto lamof = [&](double mu) { return -mu * S.sigma / (1.0 - mu); };
+  int nsteps = 0, mdim = 0, converged = 0;
+  std::vector<double> lastB;
+  for (int j = 0; j < nbmax; j++) {
+    double *KQj = S.KQ.p + (size_t)j * bs;
+    double *W = S.Q.p + (size_t)(j + 1) * bs, *KW = S.KQ.p + (size_t)(j + 1) * bs;
+    // W = A^{-1} K Q_j
+    if (direct) {
+      if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, 1e-10, 2, &inner))) return rc;
+    } else {
+      for (int c = 0; c < p; c++) {  // one GMRES solve per block column
+        k_col_get<<<grid_for(n6), 256, 0, m.stream>>>(KQj, p, c, S.r.p, n6);
+        int it = 0;
+        double rn = 0.0;
+        if ((rc = gmres_device(m, &S.fk, S.Aux.p, S.r.p, S.t.p, opts->gmres_m,
+                               opts->gmres_restarts, opts->gmres_rtol, opts->gmres_atol, gw, B,
+                               &it, &rn)))
+          return rc;
+        k_col_put<<<grid_for(n6), 256, 0, m.stream>>>(W, p, c, S.t.p, n6);
+        m.launches += 2;
+        inner += it;
+      }
+    }
+    if ((rc = blk_zero_bc(W, p, m.d_bc_rows.p, m.d_bc_masks.p, nbc, m.stream))) return rc;
+    // full K-orthogonalisation against blocks 0..j, two classical passes
+    if ((rc = blk_dots(S.KQ.p, j + 1, bs, W, n6, p, S.dH1.p, m.stream))) return rc;
+    if ((rc = blk_sub(W, S.Q.p, j + 1, bs, S.dH1.p, n6, p, m.stream))) return rc;
+    if ((rc = blk_dots(S.KQ.p, j + 1, bs, W, n6, p, S.dH2.p, m.stream))) return rc;
+    if ((rc = blk_sub(W, S.Q.p, j + 1, bs, S.dH2.p, n6, p, m.stream))) return rc;
+    m.launches += 5;
+    A2DS_CUDA_TRY(cudaMemcpyAsync(h1.data(), S.dH1.p + (size_t)j * p * p, p * p * sizeof(double),
+                                  cudaMemcpyDeviceToHost, m.stream));
+    A2DS_CUDA_TRY(cudaMemcpyAsync(h2.data(), S.dH2.p + (size_t)j * p * p, p * p * sizeof(double),
+                                  cudaMemcpyDeviceToHost, m.stream));
+    if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, W, nullptr, KW, p, m.stream)))
+      return rc;
+    m.launches++;
+    if ((rc = cholqr2(m, S, W, KW, p, Bj))) return rc;  // synchronises: h1, h2 are ready
+    // T: diagonal block j (symmetrised), sub/super-diagonal blocks from B_j
+    for (int a = 0; a < p; a++)
+      for (int b = 0; b < p; b++) {
+        const double v = 0.5 * (h1[(size_t)a * p + b] + h2[(size_t)a * p + b] +
+                                h1[(size_t)b * p + a] + h2[(size_t)b * p + a]);
+        T[(size_t)(j * p + a) * tdim + j * p + b] = v;
+        T[(size_t)((j + 1) * p + a) * tdim + j * p + b] = Bj[(size_t)a * p + b];
+        T[(size_t)(j * p + b) * tdim + (j + 1) * p + a] = Bj[(size_t)a * p + b];
+      }
+    nsteps = j + 1;
+    mdim = nsteps * p;
+    lastB = Bj;
+    if (mdim < nev) continue;
+    // Ritz values of the leading mdim x mdim block of T
+    Tm.assign((size_t)mdim * mdim, 0.0);
+    for (int a = 0; a < mdim; a++)
+      for (int b = 0; b < mdim; b++) Tm[(size_t)a * mdim + b] = T[(size_t)a * tdim + b];
+    if (sym_eig(mdim, Tm, Tw, TV)) return fail(A2DS_ERR_NUMERIC, "tridiagonal eigensolver failed");
+    order.resize(mdim);
+    for (int k = 0; k < mdim; k++) order[k] = k;
+    std::sort(order.begin(), order.end(),
+              [&](int a, int c) { return fabs(lamof(Tw[a])) < fabs(lamof(Tw[c])); });
+    converged = 1;
+    for (int k = 0; k < nev; k++) {
+      const int idx = order[k];
+      // residual estimate ||B_j y_j||, y_j = last p entries of the Ritz vector
+      double est2 = 0.0;
+      for (int a = 0; a < p; a++) {
+        double s = 0.0;
+        for (int b = 0; b < p; b++)
+          s += Bj[(size_t)a * p + b] * TV[(size_t)(j * p + b) * mdim + idx];
+        est2 += s * s;
+      }
+      if (!(sqrt(est2) <= opts->eig_tol * fabs(Tw[idx]))) {
+        converged = 0;
+        break;
+      }
+    }
+    if (converged) break;
+  }
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  out.t_lan = now() - ta;
+  if (mdim < nev || order.empty()) return fail(A2DS_ERR_NOCONV, "Lanczos produced too few vectors");
+
+  // eigenvalues; eigenvectors phi = Q y; residual ||K phi + lam G phi|| / ||K phi||
+  S.lam.assign(nev, 0.0);
+  S.err.assign(nev, 0.0);
+  S.ritz.assign((size_t)mdim * nev, 0.0);
+  for (int k = 0; k < nev; k++) {
+    const int idx = order[k];
+    S.lam[k] = lamof(Tw[idx]);
+    for (int j = 0; j < mdim; j++) S.ritz[(size_t)j * nev + k] = TV[(size_t)j * mdim + idx];
+  }
+  {
+    DBuf<double> dC;
+    if ((rc = dC.upload(S.ritz.data(), S.ritz.size(), m.stream))) return rc;
+    if ((rc = blk_combine(S.Q.p, nsteps, bs, p, dC.p, nev, n6, S.phi.p, m.stream))) return rc;
+    m.launches++;
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  }
+  for (int k = 0; k < nev; k++) {
+    double *phik = S.phi.p + (size_t)k * n6;
+    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, phik, S.r.p, m.stream))) return rc;
+    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, phik, S.t.p, m.stream))) return rc;
+    m.launches += 2;
+    if (nbc) {
+      k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.r.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
+      k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.t.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
+      m.launches += 2;
+    }
+    double kn = sqrt(B.dot(S.r.p, S.r.p, n6));
+    B.axpby(S.r.p, S.lam[k], S.t.p, 1.0, n6);
+    double rn = sqrt(B.dot(S.r.p, S.r.p, n6));
+    S.err[k] = kn > 0 ? rn / kn : rn;
+    if (eigvecs) {
+      if ((rc = m.from_rows(phik, eigvecs + (size_t)k * n6))) return rc;
+    }
+  }
+  for (int k = 0; k < nev; k++) {
+    eigvals[k] = S.lam[k];
+    if (errors) errors[k] = S.err[k];
+  }
+  out.mdim = mdim;
+  out.nsteps = nsteps;
+  out.converged = converged;
+  return 0;
+}
+
 extern "C" {
 
 int a2ds_pc_create(a2ds_bcsr A, int lev_fill, int precision, a2ds_pc *out) {
@@ -866,49 +1103,15 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
                         double *eigvals, double *errors, double *eigvecs, double *path_out) {
   if (!mesh || !opts || !eigvals) return fail(A2DS_ERR_ARG, "null argument");
   Mesh &m = mesh->m;
-  if (!m.initialized) return fail(A2DS_ERR_STATE, "mesh not initialized");
-  const int nev = opts->num_eigvals, mmax = opts->max_lanczos, p = opts->block_size;
-  if (p != 1 && p != 2 && p != 4 && p != 8 && p != 16)
-    return fail(A2DS_ERR_ARG, "block_size must be 1, 2, 4, 8 or 16");
-  const int nbmax = mmax / p;  // block steps; basis dimension <= max_lanczos
-  if (nev <= 0 || nbmax < 1 || nbmax * p < nev)
-    return fail(A2DS_ERR_ARG, "need 0 < num_eigvals <= max_lanczos and block_size <= max_lanczos");
-  if (!(opts->sigma > 0.0)) return fail(A2DS_ERR_ARG, "sigma must be positive");
-  if (opts->precision != 64 && opts->precision != 48 && opts->precision != 32)
-    return fail(A2DS_ERR_ARG, "precision must be 64, 48 or 32");
-  const size_t n6 = (size_t)m.nn * 6;
-  const size_t nv = (size_t)m.nnzb * 36;
-  const size_t bs = n6 * p;  // doubles per basis block
-  int rc;
   double t0 = now();
   long long launches0 = m.launches;
-
-  BucklingState *Sp = (BucklingState *)m.solver;
-  if (!Sp || Sp->lev_fill != opts->lev_fill || Sp->precision != opts->precision) {
-    delete Sp;
-    Sp = new BucklingState();
-    m.solver = Sp;
-    Sp->lev_fill = opts->lev_fill;
-    Sp->precision = opts->precision;
-    // K's factor serves the load-path solve (FP64 refinement to 1e-13): FP64,
-    // or double-float when the shifted factor is double-float too; an FP32
-    // factor of K is too coarse for this (cond(K) ~ 1e11)
-    if ((rc = factor_setup(m, opts->lev_fill, opts->precision == 48 ? 48 : 64, Sp->fk))) return rc;
-    if (opts->lev_fill >= m.nn && (rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa)))
-      return rc;
-  }
+  BucklingState *Sp = nullptr;
+  int rc;
+  if ((rc = prepare_solve(m, opts, &Sp))) return rc;
   BucklingState &S = *Sp;
-  S.sigma = opts->sigma;
-  S.ntev = 0;
-  if ((rc = S.K.alloc(nv)) || (rc = S.G.alloc(nv)) || (rc = S.Aux.alloc(nv))) return rc;
-  if ((rc = S.Q.alloc((size_t)(nbmax + 1) * bs)) || (rc = S.KQ.alloc((size_t)(nbmax + 1) * bs)))
-    return rc;
-  if ((rc = S.Xb.alloc(bs)) || (rc = S.Yb.alloc(bs)) || (rc = S.dH1.alloc((size_t)nbmax * p * p)) ||
-      (rc = S.dH2.alloc((size_t)nbmax * p * p)) || (rc = S.dN.alloc((size_t)p * p)) ||
-      (rc = S.dM.alloc((size_t)p * p)) || (rc = S.phi.alloc((size_t)nev * n6)) ||
-      (rc = S.r.alloc(n6)) || (rc = S.t.alloc(n6)) || (rc = S.path.alloc(n6)) ||
-      (rc = S.rhs.alloc(n6)))
-    return rc;
+  const int nev = opts->num_eigvals, p = opts->block_size;
+  const size_t n6 = (size_t)m.nn * 6;
+  const size_t nv = (size_t)m.nnzb * 36;
   Blas B{m.stream};
   B.launches = &m.launches;
 
@@ -971,169 +1174,11 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   if ((rc = m.assemble_device(MODE_G, S.path.p, S.G.p, nullptr, A2DS_SCATTER_ATOMIC))) return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   double t_g = now() - ta;
-  ta = now();
-  A2DS_CUDA_TRY(cudaMemcpyAsync(S.Aux.p, S.K.p, nv * sizeof(double), cudaMemcpyDeviceToDevice,
-                                m.stream));
-  if ((rc = launch_axpy(S.Aux.p, S.sigma, S.G.p, nv, m.stream))) return rc;
-  if ((rc = launch_apply_bc_rows(S.Aux.p, m.d_rowp.p, m.d_cols.p, m.d_bc_rows.p, m.d_bc_masks.p,
-                                 (int)m.bc_rows.size(), m.stream)))
+  PhaseOut po;
+  if ((rc = shift_invert_phase(m, S, opts, B, direct, gw, inner, eigvals, errors, eigvecs, po)))
     return rc;
-  m.launches += 2;
-  A2DS_CUDA_TRY(cudaEventRecord(S.ev[2], m.stream));
-  if (direct && (rc = factor_numeric(m, S.fa, S.Aux.p, nullptr, 0.0))) return rc;
-  A2DS_CUDA_TRY(cudaEventRecord(S.ev[3], m.stream));
-  if (direct && (rc = factor_check(m, S.fa))) return rc;
-  double t_fa = now() - ta;
-
-  // 4. block Lanczos on A^{-1} K with the K inner product
-  ta = now();
-  const int nbc = (int)m.bc_rows.size();
-  {
-    // seeded start block (splitmix64), BC DOFs zeroed, K-orthonormalised
-    std::vector<double> h(bs);
-    uint64_t st = 0x9E3779B97F4A7C15ull * (uint64_t)(opts->seed + 1);
-    for (size_t i = 0; i < bs; i++) {
-      uint64_t z = (st += 0x9E3779B97F4A7C15ull);
-      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-      z ^= z >> 31;
-      h[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
-    }
-    A2DS_CUDA_TRY(cudaMemcpyAsync(S.Q.p, h.data(), bs * sizeof(double), cudaMemcpyHostToDevice,
-                                  m.stream));
-    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
-  }
-  if ((rc = blk_zero_bc(S.Q.p, p, m.d_bc_rows.p, m.d_bc_masks.p, nbc, m.stream))) return rc;
-  if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, S.Q.p, nullptr, S.KQ.p, p, m.stream)))
-    return rc;
-  m.launches += 2;
-  std::vector<double> Bj;
-  if ((rc = cholqr2(m, S, S.Q.p, S.KQ.p, p, Bj))) return rc;
-
-  const int tdim = (nbmax + 1) * p;
-  std::vector<double> T((size_t)tdim * tdim, 0.0), h1((size_t)p * p), h2((size_t)p * p);
-  std::vector<double> Tw, TV, Tm;
-  std::vector<int> order;
-  auto lamof = [&](double mu) { return -mu * S.sigma / (1.0 - mu); };
-  int nsteps = 0, mdim = 0, converged = 0;
-  std::vector<double> lastB;
-  for (int j = 0; j < nbmax; j++) {
-    double *KQj = S.KQ.p + (size_t)j * bs;
-    double *W = S.Q.p + (size_t)(j + 1) * bs, *KW = S.KQ.p + (size_t)(j + 1) * bs;
-    // W = A^{-1} K Q_j
-    if (direct) {
-      if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, 1e-10, 2, &inner))) return rc;
-    } else {
-      for (int c = 0; c < p; c++) {  // one GMRES solve per block column
-        k_col_get<<<grid_for(n6), 256, 0, m.stream>>>(KQj, p, c, S.r.p, n6);
-        int it = 0;
-        double rn = 0.0;
-        if ((rc = gmres_device(m, &S.fk, S.Aux.p, S.r.p, S.t.p, opts->gmres_m,
-                               opts->gmres_restarts, opts->gmres_rtol, opts->gmres_atol, gw, B,
-                               &it, &rn)))
-          return rc;
-        k_col_put<<<grid_for(n6), 256, 0, m.stream>>>(W, p, c, S.t.p, n6);
-        m.launches += 2;
-        inner += it;
-      }
-    }
-    if ((rc = blk_zero_bc(W, p, m.d_bc_rows.p, m.d_bc_masks.p, nbc, m.stream))) return rc;
-    // full K-orthogonalisation against blocks 0..j, two classical passes
-    if ((rc = blk_dots(S.KQ.p, j + 1, bs, W, n6, p, S.dH1.p, m.stream))) return rc;
-    if ((rc = blk_sub(W, S.Q.p, j + 1, bs, S.dH1.p, n6, p, m.stream))) return rc;
-    if ((rc = blk_dots(S.KQ.p, j + 1, bs, W, n6, p, S.dH2.p, m.stream))) return rc;
-    if ((rc = blk_sub(W, S.Q.p, j + 1, bs, S.dH2.p, n6, p, m.stream))) return rc;
-    m.launches += 5;
-    A2DS_CUDA_TRY(cudaMemcpyAsync(h1.data(), S.dH1.p + (size_t)j * p * p, p * p * sizeof(double),
-                                  cudaMemcpyDeviceToHost, m.stream));
-    A2DS_CUDA_TRY(cudaMemcpyAsync(h2.data(), S.dH2.p + (size_t)j * p * p, p * p * sizeof(double),
-                                  cudaMemcpyDeviceToHost, m.stream));
-    if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, W, nullptr, KW, p, m.stream)))
-      return rc;
-    m.launches++;
-    if ((rc = cholqr2(m, S, W, KW, p, Bj))) return rc;  // synchronises: h1, h2 are ready
-    // T: diagonal block j (symmetrised), sub/super-diagonal blocks from B_j
-    for (int a = 0; a < p; a++)
-      for (int b = 0; b < p; b++) {
-        const double v = 0.5 * (h1[(size_t)a * p + b] + h2[(size_t)a * p + b] +
-                                h1[(size_t)b * p + a] + h2[(size_t)b * p + a]);
-        T[(size_t)(j * p + a) * tdim + j * p + b] = v;
-        T[(size_t)((j + 1) * p + a) * tdim + j * p + b] = Bj[(size_t)a * p + b];
-        T[(size_t)(j * p + b) * tdim + (j + 1) * p + a] = Bj[(size_t)a * p + b];
-      }
-    nsteps = j + 1;
-    mdim = nsteps * p;
-    lastB = Bj;
-    if (mdim < nev) continue;
-    // Ritz values of the leading mdim x mdim block of T
-    Tm.assign((size_t)mdim * mdim, 0.0);
-    for (int a = 0; a < mdim; a++)
-      for (int b = 0; b < mdim; b++) Tm[(size_t)a * mdim + b] = T[(size_t)a * tdim + b];
-    if (sym_eig(mdim, Tm, Tw, TV)) return fail(A2DS_ERR_NUMERIC, "tridiagonal eigensolver failed");
-    order.resize(mdim);
-    for (int k = 0; k < mdim; k++) order[k] = k;
-    std::sort(order.begin(), order.end(),
-              [&](int a, int c) { return fabs(lamof(Tw[a])) < fabs(lamof(Tw[c])); });
-    converged = 1;
-    for (int k = 0; k < nev; k++) {
-      const int idx = order[k];
-      // residual estimate ||B_j y_j||, y_j = last p entries of the Ritz vector
-      double est2 = 0.0;
-      for (int a = 0; a < p; a++) {
-        double s = 0.0;
-        for (int b = 0; b < p; b++)
-          s += Bj[(size_t)a * p + b] * TV[(size_t)(j * p + b) * mdim + idx];
-        est2 += s * s;
-      }
-      if (!(sqrt(est2) <= opts->eig_tol * fabs(Tw[idx]))) {
-        converged = 0;
-        break;
-      }
-    }
-    if (converged) break;
-  }
-  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
-  double t_lan = now() - ta;
-  if (mdim < nev || order.empty()) return fail(A2DS_ERR_NOCONV, "Lanczos produced too few vectors");
-
-  // eigenvalues; eigenvectors phi = Q y; residual ||K phi + lam G phi|| / ||K phi||
-  S.lam.assign(nev, 0.0);
-  S.err.assign(nev, 0.0);
-  S.ritz.assign((size_t)mdim * nev, 0.0);
-  for (int k = 0; k < nev; k++) {
-    const int idx = order[k];
-    S.lam[k] = lamof(Tw[idx]);
-    for (int j = 0; j < mdim; j++) S.ritz[(size_t)j * nev + k] = TV[(size_t)j * mdim + idx];
-  }
-  {
-    DBuf<double> dC;
-    if ((rc = dC.upload(S.ritz.data(), S.ritz.size(), m.stream))) return rc;
-    if ((rc = blk_combine(S.Q.p, nsteps, bs, p, dC.p, nev, n6, S.phi.p, m.stream))) return rc;
-    m.launches++;
-    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
-  }
-  for (int k = 0; k < nev; k++) {
-    double *phik = S.phi.p + (size_t)k * n6;
-    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.K.p, phik, S.r.p, m.stream))) return rc;
-    if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, phik, S.t.p, m.stream))) return rc;
-    m.launches += 2;
-    if (nbc) {
-      k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.r.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
-      k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.t.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
-      m.launches += 2;
-    }
-    double kn = sqrt(B.dot(S.r.p, S.r.p, n6));
-    B.axpby(S.r.p, S.lam[k], S.t.p, 1.0, n6);
-    double rn = sqrt(B.dot(S.r.p, S.r.p, n6));
-    S.err[k] = kn > 0 ? rn / kn : rn;
-    if (eigvecs) {
-      if ((rc = m.from_rows(phik, eigvecs + (size_t)k * n6))) return rc;
-    }
-  }
-  for (int k = 0; k < nev; k++) {
-    eigvals[k] = S.lam[k];
-    if (errors) errors[k] = S.err[k];
-  }
+  const double t_fa = po.t_fa, t_lan = po.t_lan;
+  const int mdim = po.mdim, nsteps = po.nsteps, converged = po.converged;
   if (path_out && (rc = m.from_rows(S.path.p, path_out))) return rc;
   S.nconv = converged ? nev : 0;
   A2DS_CUDA_TRY(cudaEventRecord(S.ev[1], m.stream));
@@ -1148,6 +1193,63 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
              (double)S.fk.nnzb(), (double)S.fk.flv.nlevels, (double)S.fk.flops(), (double)p,
              (double)nsteps, S.solve_ms(), (double)(S.ntev / 2)};
   if (!converged) return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
+  return 0;
+}
+
+
+int a2ds_eigen_shift_invert(a2ds_mesh mesh, const a2ds_buckling_opts *opts, a2ds_bcsr K,
+                            a2ds_bcsr G, double *eigvals, double *errors, double *eigvecs) {
+  if (!K || !G) return fail(A2DS_ERR_ARG, "null matrix");
+  if (K->mesh != mesh || G->mesh != mesh) return fail(A2DS_ERR_ARG, "matrices of another mesh");
+  if (!mesh || !opts || !eigvals) return fail(A2DS_ERR_ARG, "null argument");
+  Mesh &m = mesh->m;
+  double t0 = now();
+  long long launches0 = m.launches;
+  BucklingState *Sp = nullptr;
+  int rc;
+  if ((rc = prepare_solve(m, opts, &Sp))) return rc;
+  BucklingState &S = *Sp;
+  const int nev = opts->num_eigvals, p = opts->block_size;
+  const size_t n6 = (size_t)m.nn * 6;
+  const size_t nv = (size_t)m.nnzb * 36;
+  Blas B{m.stream};
+  B.launches = &m.launches;
+  (void)nev;
+  (void)p;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[0], m.stream));
+  A2DS_CUDA_TRY(cudaMemcpyAsync(S.K.p, K->vals.p, nv * sizeof(double), cudaMemcpyDeviceToDevice,
+                                m.stream));
+  A2DS_CUDA_TRY(cudaMemcpyAsync(S.G.p, G->vals.p, nv * sizeof(double), cudaMemcpyDeviceToDevice,
+                                m.stream));
+  A2DS_CUDA_TRY(cudaMemsetAsync(S.path.p, 0, n6 * sizeof(double), m.stream));
+  int inner = 0;
+  const bool direct = opts->lev_fill >= m.nn;
+  GmresWork gw;
+  double ta = now();
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[4], m.stream));
+  if (!direct) {  // GMRES inside the operator is preconditioned by the factor of K
+    if ((rc = factor_numeric(m, S.fk, S.K.p, nullptr, 0.0)) || (rc = factor_check(m, S.fk)))
+      return rc;
+  }
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[5], m.stream));
+  const double t_fk = now() - ta;
+  PhaseOut po;
+  if ((rc = shift_invert_phase(m, S, opts, B, direct, gw, inner, eigvals, errors, eigvecs, po)))
+    return rc;
+  S.nconv = po.converged ? opts->num_eigvals : 0;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[1], m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  const double total = now() - t0;
+  float ms_solve = 0.f, ms_fa = 0.f, ms_fk = 0.f;
+  cudaEventElapsedTime(&ms_solve, S.ev[0], S.ev[1]);
+  cudaEventElapsedTime(&ms_fa, S.ev[2], S.ev[3]);
+  cudaEventElapsedTime(&ms_fk, S.ev[4], S.ev[5]);
+  m.stats = {total, 0.0, 0.0, t_fk + po.t_fa, 0.0, po.t_lan, (double)po.mdim, (double)inner,
+             (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
+             (double)S.fk.nnzb(), (double)S.fk.flv.nlevels, (double)S.fk.flops(),
+             (double)opts->block_size, (double)po.nsteps, S.solve_ms(), (double)(S.ntev / 2)};
+  if (!po.converged)
+    return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
   return 0;
 }
 

@@ -267,6 +267,18 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts,
                         const double *rhs, double *eigvals, double *errors,
                         double *eigvecs, double *path);
 
+/* SEP::solve with EPBucklingShiftInvert(sigma, K, G)
+   (src/bpmat/GSEP.cpp:200-244, 485-596) on matrices the caller assembled:
+   the num_eigvals smallest-magnitude lambda of K x + lambda G x = 0 by the
+   same block shift-invert Lanczos as a2ds_buckling_solve (K and G in this
+   mesh's pattern, Dirichlet rows applied).  Used, for example, for
+   buckling about a nonlinear preloaded state with K = K_T(u) from
+   a2ds_assemble_jacobian and G from a2ds_assemble_mat along u.  Outputs as
+   a2ds_buckling_solve (no path). */
+int a2ds_eigen_shift_invert(a2ds_mesh mesh, const a2ds_buckling_opts *opts, a2ds_bcsr K,
+                            a2ds_bcsr G, double *eigvals, double *errors,
+                            double *eigvecs);
+
 /* Timings and counters of the last a2ds_buckling_solve on this mesh:
    fills up to n doubles {total_s, assemble_k_s, assemble_g_s, factor_s,
    path_s, lanczos_s, lanczos_vectors, inner_iters, kernel_launches,

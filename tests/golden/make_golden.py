@@ -103,13 +103,15 @@ def dense_eigs(fx, neig):
     return lam[:neig]
 
 
-def run_case(name, m, lev, gm_m, gm_restarts, lanczos, neig, sigma=None, nonlinear=0):
+def run_case(name, m, lev, gm_m, gm_restarts, lanczos, neig, sigma=None, nonlinear=0,
+             temperature=0.0, alpha_t=0.0):
     with tempfile.TemporaryDirectory() as d:
         ind, outd = os.path.join(d, "in"), os.path.join(d, "out")
         os.makedirs(ind)
         os.makedirs(outd)
         s0 = sigma if sigma is not None else 1e4
-        write_inputs(ind, m, s0, lev, gm_m, gm_restarts, lanczos, neig, nonlinear)
+        write_inputs(ind, m, s0, lev, gm_m, gm_restarts, lanczos, neig, nonlinear,
+                     temperature=temperature, alpha_t=alpha_t)
         subprocess.run([os.path.join(REF_OUT, "golden_gen"), "assembly", ind, outd], check=True)
         fx = load_dir(outd)
         fx.update(bc_nodes=m.bc_nodes, bc_mask=m.bc_mask)
@@ -117,7 +119,8 @@ def run_case(name, m, lev, gm_m, gm_restarts, lanczos, neig, sigma=None, nonline
         if sigma is None:
             # Second pass with the shift just below the lowest dense eigenvalue
             sigma = 0.95 * lam_dense[0]
-            write_inputs(ind, m, sigma, lev, gm_m, gm_restarts, lanczos, neig, nonlinear)
+            write_inputs(ind, m, sigma, lev, gm_m, gm_restarts, lanczos, neig, nonlinear,
+                         temperature=temperature, alpha_t=alpha_t)
             subprocess.run([os.path.join(REF_OUT, "golden_gen"), "assembly", ind, outd],
                            check=True)
         subprocess.run([os.path.join(REF_OUT, "golden_gen_cplx"), "assembly", ind, outd],
@@ -129,6 +132,7 @@ def run_case(name, m, lev, gm_m, gm_restarts, lanczos, neig, sigma=None, nonline
                sigma=np.float64(sigma), lev=np.int32(lev), gm_m=np.int32(gm_m),
                gm_restarts=np.int32(gm_restarts), lanczos=np.int32(lanczos),
                neig=np.int32(neig), nonlinear=np.int32(nonlinear),
+               temperature=np.float64(temperature), alpha_t=np.float64(alpha_t),
                eigvals_dense=lam_dense)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     rel = np.abs(out["eigvals"][:3] - lam_dense[:3]) / lam_dense[:3]
@@ -161,8 +165,28 @@ def make_orderings():
     print("wrote orderings.npz")
 
 
+def thermal_cylinder(nx, ny):
+    """Both ends clamped, no mechanical load: uniform heating (temperature
+    with a thermal expansion coefficient) compresses the shell axially, as in
+    the reference's thermal buckling example."""
+    m = meshgen.cylinder(nx, ny, order=2)
+    x = m.X[:, 0]
+    ends = np.where((np.abs(x) < 1e-12) | (np.abs(x - x.max()) < 1e-12))[0].astype(np.int32)
+    m.bc_nodes = ends
+    m.bc_mask = np.full(ends.size, 63, np.int32)
+    m.bc_vals = np.zeros((ends.size, 6))
+    m.rhs = np.zeros_like(m.rhs)
+    return m
+
+
+def make_thermal():
+    run_case("cyl_q4_4x8_thermal", thermal_cylinder(4, 8), lev=1000000, gm_m=10,
+             gm_restarts=15, lanczos=100, neig=50, temperature=10.0, alpha_t=1e-5)
+
+
 def main():
     build_reference()
+    make_thermal()
     make_orderings()
     make_elements()
     run_case("cyl_q4_4x8_lu", meshgen.cylinder(4, 8, order=2), lev=1000000, gm_m=10,

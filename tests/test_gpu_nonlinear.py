@@ -1,0 +1,58 @@
+"""Buckling about a nonlinear preloaded state (the nonlinear-preload row of
+the scope: Newton load stepping on the nonlinear shell model with the exact
+tangent, then K_T(u) x + lam G(u) x = 0).  Equilibrium of the GPU Newton
+solution is checked with the CPU oracle's element residuals (restated from
+TACSShellElement::addResidual with the nonlinear strain model); the
+eigenvalues against a dense FP64 eigensolve of the same matrices."""
+import numpy as np
+import pytest
+
+import oracle
+from a2ds import capi
+from a2ds import mesh as meshgen
+from a2ds import nonlinear
+
+
+def cpu_residual(m, u, t):
+    """Assembled nonlinear residual R(u) from the oracle's element residuals."""
+    mat = oracle.Material.iso(m.E, m.nu, t)
+    R = np.zeros((m.num_nodes, 6))
+    for e in range(m.num_elements):
+        nodes = m.conn[e]
+        re = oracle.element_residual(2, 1, mat, m.X[nodes], u[nodes].ravel())
+        R[nodes] += re.reshape(-1, 6)
+    return R
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64, 48])
+def test_newton_preload_and_buckling(precision):
+    m = meshgen.cylinder(8, 16)
+    t = m.meta["t"]
+    a = capi.Assembler(m.X, m.conn, nonlinear=True)
+    a.set_material(m.E, m.nu)
+    a.set_thickness([t])
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    load = 0.3 * meshgen.classical_cylinder_load(m.E, m.nu, t, 1.0)
+    u, its, rel = nonlinear.newton_preload(a, m.rhs, m.bc_nodes, m.bc_mask, load, nsteps=4,
+                                           rtol=1e-10, precision=precision)
+    assert rel <= 1e-10
+    assert max(its) <= 8, its  # Newton with the exact tangent converges fast
+    # equilibrium on the free DOFs, by the CPU restatement of the element residual
+    fixed = nonlinear._bc_mask_vector(a, m.bc_nodes, m.bc_mask)
+    f = load * m.rhs
+    R = cpu_residual(m, u, t)
+    r = (R - f)[~fixed]
+    assert np.linalg.norm(r) <= 1e-8 * np.linalg.norm(f[~fixed])
+    assert np.abs(u[fixed]).max() == 0.0
+    # buckling about the preloaded state
+    KT, G = a.create_mat(), a.create_mat()
+    a.assemble_jacobian(KT, u, want_res=False)
+    a.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, u)
+    from test_gpu_solve import dense_buckling
+    dense = dense_buckling(KT.to_dense_nodes(), G.to_dense_nodes(), m.bc_nodes, m.bc_mask)
+    nev = 4
+    lam, b, _, _ = nonlinear.preload_buckling(a, u, 0.95 * dense[0], num_eigvals=nev,
+                                              eig_tol=1e-12, precision=precision, block_size=4)
+    assert np.max(np.abs(lam - dense[:nev]) / np.abs(dense[:nev])) < 1e-8, (lam, dense[:nev])

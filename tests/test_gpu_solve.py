@@ -291,3 +291,50 @@ def test_eigenvalue_thickness_sensitivity_vs_finite_difference(precision):
         tm[g] -= h
         fd = (solve(tp)[2][0] - solve(tm)[2][0]) / (2 * h)
         assert abs(dl[g] - fd) <= 1e-4 * abs(fd), (g, dl[g], fd)
+
+
+@pytest.mark.gpu
+def test_thermal_buckling_matches_reference():
+    """Thermal buckling (both ends clamped, uniform temperature with thermal
+    expansion, no mechanical load; tests/golden/cyl_q4_4x8_thermal.npz from
+    the reference).  G follows the reference's default getMatType, whose
+    central difference perturbs the temperature with the state
+    (TACSShellElement.h:700-767), so G carries the thermal prestress term;
+    the reference's complex-step G (setComplexStepGmatrix) omits that term
+    (it equals the GPU G at zero temperature).  The buckling temperature
+    multiplier of smallest magnitude (negative: heating compresses the
+    shell) matches a dense FP64 eigensolve (negative shift next to it) and
+    the reference's own Lanczos value."""
+    f = np.load(os.path.join(GOLDEN, "cyl_q4_4x8_thermal.npz"))
+
+    def assembler(temperature, alpha):
+        a = capi.Assembler(f["X"], f["conn"])
+        a.set_material(float(f["E"]), float(f["nu"]), alpha, temperature)
+        a.set_thickness(f["thickness"][:1])
+        a.add_bcs(f["bc_nodes"], f["bc_mask"], f["bc_vals"])
+        a.initialize(capi.A2DS_TACS_AMD_ORDER)
+        return a
+
+    a = assembler(float(f["temperature"]), float(f["alpha_t"]))
+    a0 = assembler(0.0, 0.0)
+    K, G, G0 = a.create_mat(), a.create_mat(), a0.create_mat()
+    a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
+    assert rel(K.get_arrays()[2], f["K_after"]) < 1e-12
+    a.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, f["path"])
+    a0.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G0, f["path_cs"])
+    # real-mode reference G (central difference, FD noise ~1e-7 here)
+    assert rel(G.get_arrays()[2], f["G"]) < 1e-6
+    # its mechanical part equals the reference's complex-step G
+    assert rel(G0.get_arrays()[2], f["G_cs"]) < 1e-12
+    dense = dense_buckling(K.to_dense_nodes(), G.to_dense_nodes(), f["bc_nodes"], f["bc_mask"])
+    sigma = 0.95 * dense[0]
+    b = capi.LinearBuckling(a, sigma, max_lanczos=60, num_eigvals=1, eig_tol=1e-12,
+                            block_size=1)
+    lam = b.solve(f["rhs"])
+    assert rel(b.path, f["path"].reshape(b.path.shape)) < 1e-8
+    assert abs(lam[0] - dense[0]) <= 1e-8 * abs(dense[0]), (lam, dense[:3])
+    # the reference's own Lanczos value: it stops after num_eigvals steps (not
+    # a converged value, F3 of the reference) and uses the central-difference
+    # G, so it agrees only to a few 1e-6 here
+    ref = f["eigvals"][np.argmin(np.abs(f["eigvals"]))]
+    assert abs(lam[0] - ref) <= 1e-5 * abs(ref), (lam[0], ref)
