@@ -831,7 +831,11 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
     double *W = S.Q.p + (size_t)(j + 1) * bs, *KW = S.KQ.p + (size_t)(j + 1) * bs;
     // W = A^{-1} K Q_j
     if (direct) {
-      if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, 1e-10, 2, &inner))) return rc;
+      // solves accurate to a tenth of the eigenvalue tolerance (within
+      // [1e-12, 1e-9]): the Ritz values of the exact operator are then
+      // unaffected at that tolerance
+      const double rtol = std::max(1e-12, std::min(1e-9, 0.1 * opts->eig_tol));
+      if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, rtol, 2, &inner))) return rc;
     } else {
       for (int c = 0; c < p; c++) {  // one GMRES solve per block column
         k_col_get<<<grid_for(n6), 256, 0, m.stream>>>(KQj, p, c, S.r.p, n6);
