@@ -283,49 +283,48 @@ __global__ void __launch_bounds__(288) k_factor_lcol(const int *__restrict__ jps
 // Six threads share one block update, thread b owning column b: the six
 // threads read each 48-byte row of U and C together (coalesced), and a
 // thread holds only 18 values, so many warps fit on an SM to hide the
-// memory latency of the scattered U and target blocks.
-__device__ __forceinline__ void blk_col_update(double *C, const double *L, const double *U,
-                                               int b) {
-  double u[6], c[6];
-#pragma unroll
-  for (int k = 0; k < 6; k++) u[k] = U[6 * k + b];
-#pragma unroll
-  for (int a = 0; a < 6; a++) c[a] = C[6 * a + b];
+// memory latency of the scattered U and target blocks.  blk_col_sub is the
+// register form (c = C[:, b], u = U[:, b]) shared by both update paths.
+__device__ __forceinline__ void blk_col_sub(double (&c)[6], const double *L, const double (&u)[6]) {
 #pragma unroll
   for (int a = 0; a < 6; a++) {
     double s = 0.0;
 #pragma unroll
     for (int k = 0; k < 6; k++) s += L[6 * a + k] * u[k];
-    C[6 * a + b] = c[a] - s;
+    c[a] = c[a] - s;
   }
 }
-__device__ __forceinline__ void blk_col_update(float *C, const float *L, const float *U, int b) {
-  float u[6], c[6];
-#pragma unroll
-  for (int k = 0; k < 6; k++) u[k] = U[6 * k + b];
-#pragma unroll
-  for (int a = 0; a < 6; a++) c[a] = C[6 * a + b];
+__device__ __forceinline__ void blk_col_sub(float (&c)[6], const float *L, const float (&u)[6]) {
 #pragma unroll
   for (int a = 0; a < 6; a++) {
     float s = 0.0f;
 #pragma unroll
     for (int k = 0; k < 6; k++) s += L[6 * a + k] * u[k];
-    C[6 * a + b] = c[a] - s;
+    c[a] = c[a] - s;
   }
 }
-__device__ __forceinline__ void blk_col_update(df64 *C, const df64 *L, const df64 *U, int b) {
-  df64 u[6], c[6];
-#pragma unroll
-  for (int k = 0; k < 6; k++) u[k] = U[6 * k + b];
-#pragma unroll
-  for (int a = 0; a < 6; a++) c[a] = C[6 * a + b];
+__device__ __forceinline__ void blk_col_sub(df64 (&c)[6], const df64 *L, const df64 (&u)[6]) {
 #pragma unroll
   for (int a = 0; a < 6; a++) {
     float hi = c[a].hi, lo = c[a].lo;
 #pragma unroll
     for (int k = 0; k < 6; k++) df_sub_prod(hi, lo, L[6 * a + k], u[k]);
-    C[6 * a + b] = df_norm(hi, lo);
+    c[a] = df_norm(hi, lo);
   }
+}
+template <typename T>
+__device__ __forceinline__ void blk_col_load(T (&v)[6], const T *B, int b) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) v[k] = B[6 * k + b];
+}
+template <typename T>
+__device__ __forceinline__ void blk_col_update(T *C, const T *L, const T *U, int b) {
+  T u[6], c[6];
+  blk_col_load(u, U, b);
+  blk_col_load(c, C, b);
+  blk_col_sub(c, L, u);
+#pragma unroll
+  for (int a = 0; a < 6; a++) C[6 * a + b] = c[a];
 }
 
 // Long target rows: one 384-thread CTA per task (64 block updates at a
@@ -411,6 +410,94 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
   }
 }
 
+// Phase 2 of a panel (runs of narrow levels whose pivot rows P are
+// factored together): one 384-thread CTA per target row i outside P.
+// (a) Row i's L blocks in P's columns, in pivot order: L_ik = A_ik D_k^{-1}
+// (A_ik is final once the earlier pivots of P have been applied to it), kept
+// in shared memory, written back, and applied to row i's later P columns.
+// (b) Every other block of row i that a U row of P reaches (uc, the union of
+// P's U columns outside P) is held in registers while all of P's pivots are
+// applied to it in pivot order, so the trailing blocks are read and written
+// once per panel instead of once per level.  tab[k nuc + u] / tp[k PM + k2]
+// are the U positions of pivot k at column uc[u] / at P's column k2 (-1:
+// none); task_jpk holds row i's L positions in P's columns (-1: none).
+template <typename T>
+__global__ void __launch_bounds__(384, 2) k_update_panel(
+    const int *__restrict__ task_row, const int *__restrict__ task_jpk, int ntasks,
+    const int *__restrict__ prow, int np, const int *__restrict__ uc, int nuc,
+    const int *__restrict__ tab, const int *__restrict__ tp, const int *__restrict__ frowp,
+    const int *__restrict__ fcols, const int *__restrict__ fdiag, T *__restrict__ F) {
+  constexpr int PM = PANEL_MAX_ROWS;
+  extern __shared__ int s_cols[];
+  __shared__ T s_L[PM][36];
+  __shared__ int s_jp[PM];
+  const int t = blockIdx.x;
+  if (t >= ntasks) return;
+  const int tid = threadIdx.x;
+  const int slot = tid / 6, b = tid - 6 * (tid / 6);
+  const int nslots = blockDim.x / 6;
+  const int i = task_row[t];
+  const int rs = frowp[i], len = frowp[i + 1] - rs;
+  const bool staged = len <= FACTOR_CTA_COLS;
+  if (staged)
+    for (int k = tid; k < len; k += blockDim.x) s_cols[k] = fcols[rs + k];
+  if (tid < PM) s_jp[tid] = task_jpk[(size_t)t * PM + tid];
+  const int *cols = staged ? s_cols : fcols + rs;
+  __syncthreads();
+  // (a) L blocks in P's columns
+  for (int k = 0; k < np; k++) {
+    const int jp = s_jp[k];
+    if (jp < 0) continue;  // uniform over the CTA
+    T v{};
+    if (tid < 36) v = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[prow[k]] * 36, tid);
+    __syncthreads();  // every read of A_ik done before the in-place write
+    if (tid < 36) {
+      s_L[k][tid] = v;
+      F[(size_t)jp * 36 + tid] = v;
+    }
+    __syncthreads();
+    const int k2 = k + 1 + slot;
+    if (k2 < np) {
+      const int jp2 = s_jp[k2], pu = tp[k * PM + k2];
+      if (jp2 >= 0 && pu >= 0)
+        blk_col_update(F + (size_t)jp2 * 36, &s_L[k][0], F + (size_t)pu * 36, b);
+    }
+    __syncthreads();  // before pivot k + 1 reads its (updated) A_ik
+  }
+  // (b) the other blocks: positions after row i's first L block in P
+  int lo0 = len;
+#pragma unroll
+  for (int k = 0; k < PM; k++)
+    if (s_jp[k] >= 0) lo0 = min(lo0, s_jp[k] - rs + 1);
+#pragma unroll 1
+  for (int u = slot; u < nuc; u += nslots) {
+    const int pos = find_col(cols, lo0, len, uc[u]);
+    if (pos < 0) continue;  // no such block in row i (dropped fill)
+    T *C = F + (size_t)(rs + pos) * 36;
+    T c[6];
+    blk_col_load(c, C, b);
+    // pivots four at a time: their U positions loaded together
+#pragma unroll 1
+    for (int k0 = 0; k0 < np; k0 += 4) {
+      int pus[4];
+#pragma unroll
+      for (int d = 0; d < 4; d++) {
+        const int k = k0 + d;
+        pus[d] = (k < np && s_jp[k] >= 0) ? tab[(size_t)k * nuc + u] : -1;
+      }
+#pragma unroll
+      for (int d = 0; d < 4; d++)
+        if (pus[d] >= 0) {
+          T uu[6];
+          blk_col_load(uu, F + (size_t)pus[d] * 36, b);
+          blk_col_sub(c, &s_L[k0 + d][0], uu);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 6; a++) C[6 * a + b] = c[a];
+  }
+}
+
 // df64 factor values -> FP64, in place (same 8 bytes per value).
 __global__ void k_df64_to_f64(double *F, size_t n) {
   df64 *D = reinterpret_cast<df64 *>(F);
@@ -439,21 +526,29 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
   if (!configured) {
     A2DS_CUDA_TRY(cudaFuncSetAttribute(k_update_long<T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    A2DS_CUDA_TRY(cudaFuncSetAttribute(k_update_panel<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     configured = true;
   }
   long long nl = 0;
+  const PanelSchedule &pn = f.pn;
+  constexpr int PM = PANEL_MAX_ROWS;
   for (int lv = 0; lv < L.nlevels; lv++) {
     const int cnt = L.ptr[lv + 1] - L.ptr[lv];
     k_factor_pivot<T><<<(cnt + 19) / 20, 128, 0, s>>>(L.d_rows.p + L.ptr[lv], cnt, f.d_fdiag.p, F,
                                                       status);
     nl++;
-    const int t0 = f.task_level_ptr[lv], nt = f.task_level_ptr[lv + 1] - t0;
-    if (nt <= 0) continue;
-    const int q0 = f.task_ptr[t0], nq = f.task_ptr[t0 + nt] - q0;
-    k_factor_lcol<T><<<(nq + 7) / 8, 288, 0, s>>>(f.d_task_jp.p + q0, nq, f.d_fcols.p,
-                                                  f.d_fdiag.p, F);
-    nl++;
-    const int nlong = f.task_nlong[lv], ns = nt - nlong;
+    const int pk = pn.level_panel[lv];
+    const int t0 = f.task_level_ptr[lv];
+    // panel levels: only the tasks with targets in the panel (phase 1)
+    const int nt = pk >= 0 ? pn.task_np[lv] : f.task_level_ptr[lv + 1] - t0;
+    if (nt > 0) {
+      const int q0 = f.task_ptr[t0], nq = f.task_ptr[t0 + nt] - q0;
+      k_factor_lcol<T><<<(nq + 7) / 8, 288, 0, s>>>(f.d_task_jp.p + q0, nq, f.d_fcols.p,
+                                                    f.d_fdiag.p, F);
+      nl++;
+    }
+    const int nlong = pk >= 0 ? nt : f.task_nlong[lv], ns = nt - nlong;
     if (nlong > 0) {
       k_update_long<T><<<nlong, 384, smem, s>>>(f.d_task_row.p + t0, f.d_task_ptr.p + t0,
                                                 f.d_task_jp.p, nlong, f.d_frowp.p, f.d_fcols.p,
@@ -474,6 +569,18 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
         k_update_group<T, 5><<<grid, 256, 0, s>>>(tr, tp, f.d_task_jp.p, ns, f.d_frowp.p,
                                                   f.d_fcols.p, f.d_fdiag.p, F);
       nl++;
+    }
+    if (pk >= 0 && lv + 1 == pn.l1[pk]) {  // phase 2 of the panel
+      const int a = pn.task_ptr[pk], ntk = pn.task_ptr[pk + 1] - a;
+      const int u0 = pn.uc_ptr[pk], nuc = pn.uc_ptr[pk + 1] - u0;
+      if (ntk > 0) {
+        k_update_panel<T><<<ntk, 384, smem, s>>>(
+            f.d_pn_task_row.p + a, f.d_pn_task_jpk.p + (size_t)a * PM, ntk,
+            f.d_pn_prow.p + (size_t)pk * PM, pn.np[pk], f.d_pn_uc.p + u0, nuc,
+            f.d_pn_tab.p + pn.tab_off[pk], f.d_pn_tp.p + (size_t)pk * PM * PM, f.d_frowp.p,
+            f.d_fcols.p, f.d_fdiag.p, F);
+        nl++;
+      }
     }
   }
   if (launches) *launches += nl;

@@ -2,6 +2,8 @@
 // triangular solves: dependency levels, right-looking update tasks and the
 // head / dense-tail split of the solves.  The kernels are in factor.cu and
 // trisolve.cu.
+#include <algorithm>
+
 #include "a2ds_internal.h"
 #include "ilu.h"
 
@@ -78,22 +80,78 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
   f.task_ptr.assign(1, 0);
   f.task_jp.clear();
   f.task_jp.reserve(bucket_jp.size());
+  // Panels: runs of consecutive narrow levels (at most PANEL_LEVEL_ROWS rows
+  // each, PANEL_MAX_ROWS rows together, at least two levels).  A panel's
+  // own rows P are factored level by level (phase 1, tasks with targets in
+  // P); every other target row receives all the panel's pivots in one task
+  // (phase 2), so its trailing blocks are read and written once per panel
+  // instead of once per level.
+  PanelSchedule &pn = f.pn;
+  pn = PanelSchedule();
+  pn.level_panel.assign(nl, -1);
+  {
+    // the tables hold at most PANEL_MAX_ROWS entries per U block of P; keep
+    // their offsets within int range
+    long long tab_bound = 0;
+    int l = 0;
+    while (l < nl) {
+      int l1 = l, rows = 0;
+      long long ublocks = 0;
+      while (l1 < nl) {
+        const int r = f.flv.ptr[l1 + 1] - f.flv.ptr[l1];
+        if (r > PANEL_LEVEL_ROWS || rows + r > PANEL_MAX_ROWS) break;
+        for (int k = f.flv.ptr[l1]; k < f.flv.ptr[l1 + 1]; k++) {
+          const int j = f.flv.rows[k];
+          ublocks += f.frowp[j + 1] - f.fdiag[j] - 1;
+        }
+        rows += r;
+        l1++;
+      }
+      if (l1 - l >= 2 && tab_bound + PANEL_MAX_ROWS * ublocks < (1LL << 30)) {
+        tab_bound += PANEL_MAX_ROWS * ublocks;
+        for (int k = l; k < l1; k++) pn.level_panel[k] = (int)pn.l0.size();
+        pn.l0.push_back(l);
+        pn.l1.push_back(l1);
+        pn.np.push_back(rows);
+        l = l1;
+      } else {
+        l++;
+      }
+    }
+  }
+  std::vector<char> in_panel_rows(n, 0);
+  pn.task_np.assign(nl, 0);
   for (int l = 0; l < nl; l++) {
     // tasks of this level: runs of equal rows in [cnt[l], cnt[l+1])
-    for (int pass = 0; pass < 2; pass++) {  // 0: long rows, 1: short rows
+    const int pk = pn.level_panel[l];
+    if (pk >= 0 && l == pn.l0[pk]) {  // mark the panel's rows
+      for (int k = f.flv.ptr[l]; k < f.flv.ptr[pn.l1[pk]]; k++) in_panel_rows[f.flv.rows[k]] = 1;
+    }
+    // panel levels: 0 = targets in the panel (phase 1), 1 = the others (phase 2);
+    // other levels: 0 = long rows, 1 = short rows
+    for (int pass = 0; pass < 2; pass++) {
       for (long long p = cnt[l]; p < cnt[l + 1];) {
         long long e = p;
         while (e < cnt[l + 1] && bucket_row[e] == bucket_row[p]) e++;
         const int i = bucket_row[p];
-        const bool is_long = f.frowp[i + 1] - f.frowp[i] > FACTOR_WARP_COLS;
-        if (is_long == (pass == 0)) {
+        const bool first = pk >= 0 ? in_panel_rows[i] != 0
+                                   : f.frowp[i + 1] - f.frowp[i] > FACTOR_WARP_COLS;
+        if (first == (pass == 0)) {
           f.task_row.push_back(i);
           for (long long q = p; q < e; q++) f.task_jp.push_back(bucket_jp[q]);
           f.task_ptr.push_back((int)f.task_jp.size());
-          if (pass == 0) f.task_nlong[l]++;
+          if (pass == 0) {
+            if (pk >= 0)
+              pn.task_np[l]++;
+            else
+              f.task_nlong[l]++;
+          }
         }
         p = e;
       }
+    }
+    if (pk >= 0 && l + 1 == pn.l1[pk]) {  // unmark
+      for (int k = f.flv.ptr[pn.l0[pk]]; k < f.flv.ptr[l + 1]; k++) in_panel_rows[f.flv.rows[k]] = 0;
     }
     f.task_level_ptr[l + 1] = (int)f.task_row.size();
     // block updates in flight per short task (6 lanes each): from the
@@ -107,6 +165,66 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
       }
     const double mean = entries > 0 ? ublocks / entries : 0.0;
     f.task_group.push_back(mean <= 2.0 ? 1 : mean <= 8.0 ? 2 : 5);
+  }
+  // phase-2 tables and tasks of every panel
+  const int PM = PANEL_MAX_ROWS;
+  pn.uc_ptr.assign(1, 0);
+  pn.tab_off.assign(1, 0);
+  pn.task_ptr.assign(1, 0);
+  std::vector<int> kof(n, -1), slot(n, -1), mark(n, -1);
+  for (int pk = 0; pk < (int)pn.l0.size(); pk++) {
+    const int r0 = f.flv.ptr[pn.l0[pk]], np = pn.np[pk];
+    for (int k = 0; k < PM; k++) pn.prow.push_back(k < np ? f.flv.rows[r0 + k] : -1);
+    const int *prow = pn.prow.data() + (size_t)pk * PM;
+    for (int k = 0; k < np; k++) kof[prow[k]] = k;
+    // union of the U columns outside P, and both U position tables
+    std::vector<int> uc;
+    for (int k = 0; k < np; k++) {
+      const int j = prow[k];
+      for (int q = f.fdiag[j] + 1; q < f.frowp[j + 1]; q++) {
+        const int c = f.fcols[q];
+        if (kof[c] < 0 && mark[c] != pk) {
+          mark[c] = pk;
+          uc.push_back(c);
+        }
+      }
+    }
+    std::sort(uc.begin(), uc.end());
+    const int nuc = (int)uc.size();
+    for (int u = 0; u < nuc; u++) slot[uc[u]] = u;
+    const size_t t0 = pn.tab.size();
+    pn.tab.resize(t0 + (size_t)np * nuc, -1);
+    const size_t p0 = pn.tp.size();
+    pn.tp.resize(p0 + (size_t)PM * PM, -1);
+    for (int k = 0; k < np; k++) {
+      const int j = prow[k];
+      for (int q = f.fdiag[j] + 1; q < f.frowp[j + 1]; q++) {
+        const int c = f.fcols[q];
+        if (kof[c] >= 0)
+          pn.tp[p0 + (size_t)k * PM + kof[c]] = q;
+        else
+          pn.tab[t0 + (size_t)k * nuc + slot[c]] = q;
+      }
+    }
+    pn.uc.insert(pn.uc.end(), uc.begin(), uc.end());
+    pn.uc_ptr.push_back((int)pn.uc.size());
+    pn.tab_off.push_back((int)pn.tab.size());
+    // target rows outside P with L entries in P's columns
+    std::vector<int> rows;
+    for (int l = pn.l0[pk]; l < pn.l1[pk]; l++)
+      for (int t = f.task_level_ptr[l] + pn.task_np[l]; t < f.task_level_ptr[l + 1]; t++)
+        rows.push_back(f.task_row[t]);
+    std::sort(rows.begin(), rows.end());
+    rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+    for (int i : rows) {
+      pn.task_row.push_back(i);
+      const size_t b0 = pn.task_jpk.size();
+      pn.task_jpk.resize(b0 + PM, -1);
+      for (int q = f.frowp[i]; q < f.fdiag[i]; q++)
+        if (kof[f.fcols[q]] >= 0) pn.task_jpk[b0 + kof[f.fcols[q]]] = q;
+    }
+    pn.task_ptr.push_back((int)pn.task_row.size());
+    for (int k = 0; k < np; k++) kof[prow[k]] = -1;
   }
 }
 
@@ -318,6 +436,13 @@ int upload_schedules(Factor &f, cudaStream_t s) {
   if ((rc = f.d_td_row.upload(f.td_row.data(), f.td_row.size(), s))) return rc;
   if ((rc = f.d_td_pos.upload(f.td_pos.data(), f.td_pos.size(), s))) return rc;
   if ((rc = f.d_td_col.upload(f.td_col.data(), f.td_col.size(), s))) return rc;
+  const PanelSchedule &pn = f.pn;
+  if ((rc = f.d_pn_prow.upload(pn.prow.data(), pn.prow.size(), s))) return rc;
+  if ((rc = f.d_pn_uc.upload(pn.uc.data(), pn.uc.size(), s))) return rc;
+  if ((rc = f.d_pn_tab.upload(pn.tab.data(), pn.tab.size(), s))) return rc;
+  if ((rc = f.d_pn_tp.upload(pn.tp.data(), pn.tp.size(), s))) return rc;
+  if ((rc = f.d_pn_task_row.upload(pn.task_row.data(), pn.task_row.size(), s))) return rc;
+  if ((rc = f.d_pn_task_jpk.upload(pn.task_jpk.data(), pn.task_jpk.size(), s))) return rc;
   return 0;
 }
 

@@ -24,6 +24,27 @@ struct SolveGraph {
   long long nlaunch;  // kernels in the graph
 };
 
+// Panels: runs of consecutive narrow factor levels whose pivot rows P (at
+// most PANEL_MAX_ROWS) are factored together.  Phase 1 runs the panel's
+// levels restricted to target rows in P; phase 2 updates every other target
+// row with all of P's pivots in one pass (one task per row).
+struct PanelSchedule {
+  std::vector<int> level_panel;  // per factor level: its panel, -1 if none
+  std::vector<int> l0, l1;       // level range [l0, l1) of each panel
+  std::vector<int> np;           // pivot rows of each panel
+  std::vector<int> task_np;      // per level: leading tasks with targets in P
+  std::vector<int> prow;         // PANEL_MAX_ROWS per panel: P in level order (-1 pad)
+  // union of the U columns of P outside P, sorted, per panel
+  std::vector<int> uc_ptr, uc;
+  // per panel np x nuc: U position of pivot k at column uc[u] (-1: none)
+  std::vector<int> tab_off, tab;
+  // PANEL_MAX_ROWS^2 per panel: U position of pivot k at column prow[k2]
+  std::vector<int> tp;
+  // phase-2 tasks: per panel a range of target rows; PANEL_MAX_ROWS L
+  // positions per task (L block of the row in column prow[k], -1: none)
+  std::vector<int> task_ptr, task_row, task_jpk;
+};
+
 // A factorization handle (the TACSSchurPc role on one GPU).
 struct Factor {
   int n = 0, lev_fill = 0, precision = 64;
@@ -39,6 +60,9 @@ struct Factor {
   // of long target rows (> FACTOR_WARP_COLS blocks) come first
   std::vector<int> task_level_ptr, task_nlong, task_row, task_ptr, task_jp;
   std::vector<int> task_group;  // block updates in flight per short task, per level (1, 2, 5)
+  // panels of narrow levels (blocked trailing updates, see build_update_tasks)
+  PanelSchedule pn;
+  DBuf<int> d_pn_prow, d_pn_uc, d_pn_tab, d_pn_tp, d_pn_task_row, d_pn_task_jpk;
   DBuf<int> d_task_row, d_task_ptr, d_task_jp;
   // dense tail rows [tail_s, n): head pull split and column push lists
   int tail_s = 0;
@@ -82,6 +106,10 @@ int dense_build(Factor &f, const void *F, cudaStream_t s, long long *launches);
 // indices staged in shared memory up to FACTOR_CTA_COLS).
 constexpr int FACTOR_WARP_COLS = 512;
 constexpr int FACTOR_CTA_COLS = 10240;
+// Panels of the factorization: runs of levels with at most PANEL_LEVEL_ROWS
+// rows each, PANEL_MAX_ROWS rows in total.
+constexpr int PANEL_LEVEL_ROWS = 2;
+constexpr int PANEL_MAX_ROWS = 16;
 
 // Dense trailing block of the solves: panels of DENSE_PANEL block rows,
 // between DENSE_MIN and DENSE_MAX block rows, used when the factor fills at

@@ -192,6 +192,7 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   f.task_level_ptr = src.task_level_ptr;
   f.task_nlong = src.task_nlong;
   f.task_group = src.task_group;
+  f.pn = src.pn;
   f.task_row = src.task_row;
   f.task_ptr = src.task_ptr;
   f.task_jp = src.task_jp;
