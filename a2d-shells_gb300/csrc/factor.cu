@@ -415,12 +415,15 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
 // (a) Row i's L blocks in P's columns, in pivot order: L_ik = A_ik D_k^{-1}
 // (A_ik is final once the earlier pivots of P have been applied to it), kept
 // in shared memory, written back, and applied to row i's later P columns.
-// (b) Every other block of row i that a U row of P reaches (uc, the union of
-// P's U columns outside P) is held in registers while all of P's pivots are
-// applied to it in pivot order, so the trailing blocks are read and written
-// once per panel instead of once per level.  tab[k nuc + u] / tp[k PM + k2]
-// are the U positions of pivot k at column uc[u] / at P's column k2 (-1:
-// none); task_jpk holds row i's L positions in P's columns (-1: none).
+// (b) Every other block of row i that a U row of P reaches (its column is in
+// uc, the union of P's U columns outside P) is held in registers while all
+// of row i's pivots in P are applied to it in pivot order, so the trailing
+// blocks are read and written once per panel instead of once per level.
+// tab[k nuc + u] / tp[k PM + k2] are the U positions of pivot k at column
+// uc[u] / at P's column k2 (-1: none); task_jpk holds row i's L positions in
+// P's columns (-1: none).  Dynamic shared memory: row i's columns
+// (FACTOR_CTA_COLS ints) and uc (PANEL_UC_SMEM ints), each read from global
+// memory instead when longer.
 template <typename T>
 __global__ void __launch_bounds__(384, 2) k_update_panel(
     const int *__restrict__ task_row, const int *__restrict__ task_jpk, int ntasks,
@@ -428,9 +431,9 @@ __global__ void __launch_bounds__(384, 2) k_update_panel(
     const int *__restrict__ tab, const int *__restrict__ tp, const int *__restrict__ frowp,
     const int *__restrict__ fcols, const int *__restrict__ fdiag, T *__restrict__ F) {
   constexpr int PM = PANEL_MAX_ROWS;
-  extern __shared__ int s_cols[];
+  extern __shared__ int s_dyn[];
   __shared__ T s_L[PM][36];
-  __shared__ int s_jp[PM];
+  __shared__ int s_jp[PM], s_kk[PM], s_nk;
   const int t = blockIdx.x;
   if (t >= ntasks) return;
   const int tid = threadIdx.x;
@@ -438,16 +441,27 @@ __global__ void __launch_bounds__(384, 2) k_update_panel(
   const int nslots = blockDim.x / 6;
   const int i = task_row[t];
   const int rs = frowp[i], len = frowp[i + 1] - rs;
-  const bool staged = len <= FACTOR_CTA_COLS;
+  int *s_cols = s_dyn, *s_uc = s_dyn + FACTOR_CTA_COLS;
+  const bool staged = len <= FACTOR_CTA_COLS, uc_staged = nuc <= PANEL_UC_SMEM;
   if (staged)
     for (int k = tid; k < len; k += blockDim.x) s_cols[k] = fcols[rs + k];
+  if (uc_staged)
+    for (int k = tid; k < nuc; k += blockDim.x) s_uc[k] = uc[k];
   if (tid < PM) s_jp[tid] = task_jpk[(size_t)t * PM + tid];
-  const int *cols = staged ? s_cols : fcols + rs;
   __syncthreads();
+  if (tid == 0) {  // row i's pivots in P, in pivot order
+    int nk = 0;
+    for (int k = 0; k < np; k++)
+      if (s_jp[k] >= 0) s_kk[nk++] = k;
+    s_nk = nk;
+  }
+  const int *cols = staged ? s_cols : fcols + rs;
+  const int *ucs = uc_staged ? s_uc : uc;
+  __syncthreads();
+  const int nk = s_nk;
   // (a) L blocks in P's columns
-  for (int k = 0; k < np; k++) {
-    const int jp = s_jp[k];
-    if (jp < 0) continue;  // uniform over the CTA
+  for (int kk = 0; kk < nk; kk++) {
+    const int k = s_kk[kk], jp = s_jp[k];
     T v{};
     if (tid < 36) v = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[prow[k]] * 36, tid);
     __syncthreads();  // every read of A_ik done before the in-place write
@@ -456,41 +470,39 @@ __global__ void __launch_bounds__(384, 2) k_update_panel(
       F[(size_t)jp * 36 + tid] = v;
     }
     __syncthreads();
-    const int k2 = k + 1 + slot;
-    if (k2 < np) {
-      const int jp2 = s_jp[k2], pu = tp[k * PM + k2];
-      if (jp2 >= 0 && pu >= 0)
-        blk_col_update(F + (size_t)jp2 * 36, &s_L[k][0], F + (size_t)pu * 36, b);
+    if (kk + 1 + slot < nk) {
+      const int k2 = s_kk[kk + 1 + slot];
+      const int pu = tp[k * PM + k2];
+      if (pu >= 0) blk_col_update(F + (size_t)s_jp[k2] * 36, &s_L[k][0], F + (size_t)pu * 36, b);
     }
-    __syncthreads();  // before pivot k + 1 reads its (updated) A_ik
+    __syncthreads();  // before the next pivot reads its (updated) A_ik
   }
-  // (b) the other blocks: positions after row i's first L block in P
+  // (b) the other blocks: positions after row i's first L block in P (the
+  // pivot order of P is its level order, not its column order)
   int lo0 = len;
-#pragma unroll
-  for (int k = 0; k < PM; k++)
-    if (s_jp[k] >= 0) lo0 = min(lo0, s_jp[k] - rs + 1);
+  for (int kk = 0; kk < nk; kk++) lo0 = min(lo0, s_jp[s_kk[kk]] - rs + 1);
 #pragma unroll 1
-  for (int u = slot; u < nuc; u += nslots) {
-    const int pos = find_col(cols, lo0, len, uc[u]);
-    if (pos < 0) continue;  // no such block in row i (dropped fill)
+  for (int pos = lo0 + slot; pos < len; pos += nslots) {
+    const int u = find_col(ucs, 0, nuc, cols[pos]);
+    if (u < 0) continue;  // no U row of P reaches this block
     T *C = F + (size_t)(rs + pos) * 36;
     T c[6];
     blk_col_load(c, C, b);
     // pivots four at a time: their U positions loaded together
 #pragma unroll 1
-    for (int k0 = 0; k0 < np; k0 += 4) {
-      int pus[4];
+    for (int k0 = 0; k0 < nk; k0 += 4) {
+      int pus[4], ks[4];
 #pragma unroll
       for (int d = 0; d < 4; d++) {
-        const int k = k0 + d;
-        pus[d] = (k < np && s_jp[k] >= 0) ? tab[(size_t)k * nuc + u] : -1;
+        ks[d] = k0 + d < nk ? s_kk[k0 + d] : 0;
+        pus[d] = k0 + d < nk ? tab[(size_t)ks[d] * nuc + u] : -1;
       }
 #pragma unroll
       for (int d = 0; d < 4; d++)
         if (pus[d] >= 0) {
           T uu[6];
           blk_col_load(uu, F + (size_t)pus[d] * 36, b);
-          blk_col_sub(c, &s_L[k0 + d][0], uu);
+          blk_col_sub(c, &s_L[ks[d]][0], uu);
         }
     }
 #pragma unroll
@@ -523,11 +535,12 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
   const LevelSchedule &L = f.flv;
   static bool configured = false;
   const int smem = FACTOR_CTA_COLS * (int)sizeof(int);
+  const int psmem = (FACTOR_CTA_COLS + PANEL_UC_SMEM) * (int)sizeof(int);
   if (!configured) {
     A2DS_CUDA_TRY(cudaFuncSetAttribute(k_update_long<T>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     A2DS_CUDA_TRY(cudaFuncSetAttribute(k_update_panel<T>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, psmem));
     configured = true;
   }
   long long nl = 0;
@@ -574,7 +587,7 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
       const int a = pn.task_ptr[pk], ntk = pn.task_ptr[pk + 1] - a;
       const int u0 = pn.uc_ptr[pk], nuc = pn.uc_ptr[pk + 1] - u0;
       if (ntk > 0) {
-        k_update_panel<T><<<ntk, 384, smem, s>>>(
+        k_update_panel<T><<<ntk, 384, psmem, s>>>(
             f.d_pn_task_row.p + a, f.d_pn_task_jpk.p + (size_t)a * PM, ntk,
             f.d_pn_prow.p + (size_t)pk * PM, pn.np[pk], f.d_pn_uc.p + u0, nuc,
             f.d_pn_tab.p + pn.tab_off[pk], f.d_pn_tp.p + (size_t)pk * PM * PM, f.d_frowp.p,

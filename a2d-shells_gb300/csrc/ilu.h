@@ -108,8 +108,10 @@ constexpr int FACTOR_WARP_COLS = 512;
 constexpr int FACTOR_CTA_COLS = 10240;
 // Panels of the factorization: runs of levels with at most PANEL_LEVEL_ROWS
 // rows each, PANEL_MAX_ROWS rows in total.
-constexpr int PANEL_LEVEL_ROWS = 2;
-constexpr int PANEL_MAX_ROWS = 16;
+constexpr int PANEL_LEVEL_ROWS = 16;
+constexpr int PANEL_MAX_ROWS = 32;
+// union U columns of a panel staged in shared memory by its phase-2 kernel
+constexpr int PANEL_UC_SMEM = 8192;
 
 // Dense trailing block of the solves: panels of DENSE_PANEL block rows,
 // between DENSE_MIN and DENSE_MAX block rows, used when the factor fills at
