@@ -18,14 +18,18 @@
 //
 // Schedule: rows are grouped by dependency level.  For level l,
 // (1) k_factor_pivot inverts the diagonal blocks of the level's rows (final
-// once every lower level has been applied), (2) k_factor_lcol forms every
-// L_ij = A_ij D_j^{-1} with j in level l, (3) the update kernels process one
-// task per target row i with L entries in level-l columns and apply
-// -L_ij U_j* to row i.  Pivots of one level never update each other's rows
-// or L entries, and one task owns its target row, so no atomics are needed.
-// Six threads share each 6x6 block update (one output column each).  Long
-// rows: one 384-thread CTA per task.  Short rows: a group of 6, 12 or 30
-// lanes per task within a warp, sized to the level's U-row lengths.
+// once every lower level has been applied), (2) the update kernels process
+// one task per target row i with L entries in level-l columns: form each
+// L_ij = A_ij D_j^{-1} (j in level l) and apply -L_ij U_j* to row i.
+// Pivots of one level never update each other's rows or L entries, and one
+// task owns its target row, so no atomics are needed.  Six threads share
+// each 6x6 block update (one output column each).  Long rows: one 384-thread
+// CTA per task (or several CTAs per single-pivot task when a level has few,
+// with k_factor_lcol forming the L blocks first).  Short rows: a group of 6,
+// 12 or 30 lanes per task within a warp, sized to the level's U-row lengths.
+// Runs of narrow levels are grouped into panels (k_update_panel).
+#include <type_traits>
+
 #include "a2ds_internal.h"
 #include "ilu.h"
 
@@ -241,6 +245,109 @@ __global__ void __launch_bounds__(128) k_factor_pivot(const int *__restrict__ ro
   }
 }
 
+// Double-float version for df64 factors: the same Gauss-Jordan steps and
+// lane layout with every operation on the FP32 pipe (the FP64 version's
+// ~30 FP64 instructions per column run at ~1/64 rate and set a latency
+// floor of several microseconds per level).  The pivot search compares the
+// leading parts; 1/pivot is the FP32 reciprocal refined by one Newton step,
+// x1 = x0 + x0 (1 - p x0), in double-float (~48 bits).
+__device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
+  const float ph = __fmul_rn(a.hi, b.hi);
+  float pe = fmaf(a.hi, b.hi, -ph);
+  pe = fmaf(a.hi, b.lo, pe);
+  pe = fmaf(a.lo, b.hi, pe);
+  return df_norm(ph, pe);
+}
+__device__ __forceinline__ df64 df_recip(df64 p) {
+  const float q = __frcp_rn(p.hi);
+  float hi = 1.0f, lo = 0.0f;
+  df_sub_prod(hi, lo, p, df64{q, 0.0f});  // e = 1 - p q
+  const float qe = __fmul_rn(q, __fadd_rn(hi, lo));
+  return df_norm(q, qe);
+}
+__device__ __forceinline__ df64 df_shfl(unsigned mask, df64 v, int src) {
+  return df64{__shfl_sync(mask, v.hi, src), __shfl_sync(mask, v.lo, src)};
+}
+__global__ void __launch_bounds__(128) k_factor_pivot_df(const int *__restrict__ rows, int nrows,
+                                                         const int *__restrict__ fdiag,
+                                                         df64 *__restrict__ F,
+                                                         int *__restrict__ status) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp * 5 >= nrows) return;  // whole warp
+  const int sub = lane / 6, r = lane - 6 * (lane / 6);
+  const int idx = warp * 5 + sub;
+  const bool live = sub < 5 && idx < nrows;
+  const int base = sub < 5 ? 6 * sub : 0;
+  const int j = live ? rows[idx] : 0;
+  df64 *D = F + (size_t)(live ? fdiag[j] : 0) * 36;
+  df64 m[6], v[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    m[k] = live ? D[6 * r + k] : df64{0.0f, 0.0f};
+    v[k] = df64{(k == r) ? 1.0f : 0.0f, 0.0f};
+  }
+  int fail = 0;
+#pragma unroll
+  for (int c = 0; c < 6; c++) {
+    float bv = -1.0f;
+    int bp = c;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+      const float vq = __shfl_sync(full, fabsf(m[c].hi), base + q);
+      if (q >= c && vq > bv) {
+        bv = vq;
+        bp = q;
+      }
+    }
+    if (bv == 0.0f && !fail) fail = c + 1;  // singular; result unused
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const df64 mc = df_shfl(full, m[k], base + c), mp = df_shfl(full, m[k], base + bp);
+      const df64 vc = df_shfl(full, v[k], base + c), vp = df_shfl(full, v[k], base + bp);
+      if (r == c) {
+        m[k] = mp;
+        v[k] = vp;
+      } else if (r == bp) {
+        m[k] = mc;
+        v[k] = vc;
+      }
+    }
+    const df64 piv = df_shfl(full, m[c], base + c);
+    const df64 inv = piv.hi != 0.0f ? df_recip(piv) : df64{0.0f, 0.0f};
+    if (r == c) {
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        m[k] = df_mul(m[k], inv);
+        v[k] = df_mul(v[k], inv);
+      }
+    }
+    df64 pm[6], pv[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      pm[k] = df_shfl(full, m[k], base + c);
+      pv[k] = df_shfl(full, v[k], base + c);
+    }
+    if (r != c) {
+      const df64 f = m[c];
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        float mh = m[k].hi, ml = m[k].lo, vh = v[k].hi, vl = v[k].lo;
+        df_sub_prod(mh, ml, f, pm[k]);
+        df_sub_prod(vh, vl, f, pv[k]);
+        m[k] = df_norm(mh, ml);
+        v[k] = df_norm(vh, vl);
+      }
+    }
+  }
+  if (live) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) D[6 * r + k] = v[k];
+    if (fail && r == 0) atomicMax(status, j + 1);
+  }
+}
+
 // ------------------------------------------------------------- updates
 // Position of column c in cols[lo, hi) (sorted), or -1.
 __device__ __forceinline__ int find_col(const int *cols, int lo, int hi, int c) {
@@ -331,42 +438,58 @@ __device__ __forceinline__ void blk_col_update(T *C, const T *L, const T *U, int
 // time, six threads each); every pivot's U blocks are strided over the
 // slots (a pivot's U columns are distinct, so no two slots touch one target
 // block), one barrier between pivots.  The row's column indices are staged
-// in shared memory.
+// in shared memory.  With nsplit == 1 the CTA also forms its L blocks
+// L_ij = A_ij D_j^{-1} (it owns them: no other task reads them in this
+// level).  With nsplit > 1 (levels whose tasks have one pivot each) nsplit
+// CTAs share a task, each taking every nsplit-th stride of the pivot's U
+// blocks, and k_factor_lcol has formed the L blocks beforehand.
 template <typename T>
 __global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ task_row,
                                                         const int *__restrict__ task_ptr,
                                                         const int *__restrict__ task_jp,
-                                                        int ntasks, const int *__restrict__ frowp,
+                                                        int ntasks, int nsplit,
+                                                        const int *__restrict__ frowp,
                                                         const int *__restrict__ fcols,
                                                         const int *__restrict__ fdiag,
                                                         T *__restrict__ F) {
   extern __shared__ int s_cols[];
   __shared__ T s_L[36];
-  const int t = blockIdx.x;
+  const int t = blockIdx.x / nsplit, sidx = blockIdx.x - nsplit * t;
   if (t >= ntasks) return;
-  const int slot = threadIdx.x / 6, b = threadIdx.x - 6 * (threadIdx.x / 6);
+  const int tid = threadIdx.x;
+  const int slot = tid / 6, b = tid - 6 * (tid / 6);
   const int nslots = blockDim.x / 6;
   const int i = task_row[t];
   const int rs = frowp[i], len = frowp[i + 1] - rs;
   const bool staged = len <= FACTOR_CTA_COLS;
   if (staged)
-    for (int k = threadIdx.x; k < len; k += blockDim.x) s_cols[k] = fcols[rs + k];
+    for (int k = tid; k < len; k += blockDim.x) s_cols[k] = fcols[rs + k];
   const int *cols = staged ? s_cols : fcols + rs;
   for (int q = task_ptr[t]; q < task_ptr[t + 1]; q++) {
     const int jp = task_jp[q];
     const int j = fcols[jp];
-    if (threadIdx.x < 36) s_L[threadIdx.x] = F[(size_t)jp * 36 + threadIdx.x];
+    if (nsplit == 1) {
+      T v{};
+      if (tid < 36) v = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[j] * 36, tid);
+      __syncthreads();  // every read of A_ij done before the in-place write
+      if (tid < 36) {
+        s_L[tid] = v;
+        F[(size_t)jp * 36 + tid] = v;
+      }
+    } else if (tid < 36) {
+      s_L[tid] = F[(size_t)jp * 36 + tid];
+    }
     __syncthreads();  // s_L (and, first time, s_cols) ready
     const int ue = frowp[j + 1], lo0 = jp + 1 - rs;
-    if (slot < nslots)
+    const int stride = nslots * nsplit;
 #pragma unroll 1
-      for (int pu = fdiag[j] + 1 + slot; pu < ue; pu += nslots) {
-        // re-read s_L each block (cheap) rather than pinning 36 values in
-        // registers for the whole loop, which would halve the resident warps
-        asm volatile("" ::: "memory");
-        const int pos = find_col(cols, lo0, len, fcols[pu]);
-        if (pos >= 0) blk_col_update(F + (size_t)(rs + pos) * 36, s_L, F + (size_t)pu * 36, b);
-      }
+    for (int pu = fdiag[j] + 1 + sidx * nslots + slot; pu < ue; pu += stride) {
+      // re-read s_L each block (cheap) rather than pinning 36 values in
+      // registers for the whole loop, which would halve the resident warps
+      asm volatile("" ::: "memory");
+      const int pos = find_col(cols, lo0, len, fcols[pu]);
+      if (pos >= 0) blk_col_update(F + (size_t)(rs + pos) * 36, s_L, F + (size_t)pu * 36, b);
+    }
     __syncthreads();  // this pivot's updates done before the next pivot's
   }
 }
@@ -374,7 +497,9 @@ __global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ 
 // Short target rows: a group of 6 S lanes per task inside one warp (S block
 // updates at a time; S = 1, 2 or 5 gives 5, 2 or 1 groups per warp, chosen
 // per level from the mean U-row length of its pivots); the task's pivots
-// are applied in order, each pivot's U blocks strided over the S slots.
+// are applied in order, each pivot's U blocks strided over the S slots.  The
+// group first forms each L block L_ij = A_ij D_j^{-1} in place (the task
+// owns it).
 template <typename T, int S>
 __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ task_row,
                                                       const int *__restrict__ task_ptr,
@@ -383,7 +508,7 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
                                                       const int *__restrict__ fcols,
                                                       const int *__restrict__ fdiag,
                                                       T *__restrict__ F) {
-  constexpr int G = 6 * S, GW = 32 / G;
+  constexpr int G = 6 * S, GW = 32 / G, NE = (36 + G - 1) / G;
   __shared__ T s_L[8][GW][36];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gw = lane / G, gl = lane - G * (lane / G);
@@ -398,7 +523,18 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
   for (int q = task_ptr[t]; q < task_ptr[t + 1]; q++) {
     const int jp = task_jp[q];
     const int j = fcols[jp];
-    for (int e = gl; e < 36; e += G) L[e] = F[(size_t)jp * 36 + e];
+    T v[NE];
+#pragma unroll
+    for (int d = 0; d < NE; d++)
+      if (gl + d * G < 36)
+        v[d] = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[j] * 36, gl + d * G);
+    __syncwarp(gmask);  // every read of A_ij done before the in-place write
+#pragma unroll
+    for (int d = 0; d < NE; d++)
+      if (gl + d * G < 36) {
+        L[gl + d * G] = v[d];
+        F[(size_t)jp * 36 + gl + d * G] = v[d];
+      }
     __syncwarp(gmask);
     const int ue = frowp[j + 1], lo0 = jp + 1 - rs;
 #pragma unroll 1
@@ -543,29 +679,43 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, psmem));
     configured = true;
   }
+  static int num_sms = 0;
+  if (!num_sms) {
+    int dev = 0;
+    A2DS_CUDA_TRY(cudaGetDevice(&dev));
+    A2DS_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+  }
   long long nl = 0;
   const PanelSchedule &pn = f.pn;
   constexpr int PM = PANEL_MAX_ROWS;
   for (int lv = 0; lv < L.nlevels; lv++) {
     const int cnt = L.ptr[lv + 1] - L.ptr[lv];
-    k_factor_pivot<T><<<(cnt + 19) / 20, 128, 0, s>>>(L.d_rows.p + L.ptr[lv], cnt, f.d_fdiag.p, F,
-                                                      status);
+    if constexpr (std::is_same<T, df64>::value)
+      k_factor_pivot_df<<<(cnt + 19) / 20, 128, 0, s>>>(L.d_rows.p + L.ptr[lv], cnt, f.d_fdiag.p, F,
+                                                       status);
+    else
+      k_factor_pivot<T><<<(cnt + 19) / 20, 128, 0, s>>>(L.d_rows.p + L.ptr[lv], cnt, f.d_fdiag.p,
+                                                        F, status);
     nl++;
     const int pk = pn.level_panel[lv];
     const int t0 = f.task_level_ptr[lv];
     // panel levels: only the tasks with targets in the panel (phase 1)
     const int nt = pk >= 0 ? pn.task_np[lv] : f.task_level_ptr[lv + 1] - t0;
-    if (nt > 0) {
-      const int q0 = f.task_ptr[t0], nq = f.task_ptr[t0 + nt] - q0;
-      k_factor_lcol<T><<<(nq + 7) / 8, 288, 0, s>>>(f.d_task_jp.p + q0, nq, f.d_fcols.p,
-                                                    f.d_fdiag.p, F);
-      nl++;
-    }
     const int nlong = pk >= 0 ? nt : f.task_nlong[lv], ns = nt - nlong;
     if (nlong > 0) {
-      k_update_long<T><<<nlong, 384, smem, s>>>(f.d_task_row.p + t0, f.d_task_ptr.p + t0,
-                                                f.d_task_jp.p, nlong, f.d_frowp.p, f.d_fcols.p,
-                                                f.d_fdiag.p, F);
+      // few single-pivot long tasks: several CTAs per task
+      const int q0 = f.task_ptr[t0], nq = f.task_ptr[t0 + nlong] - q0;
+      const int nsplit = (nq == nlong && nlong < 2 * num_sms)
+                             ? std::min(FACTOR_MAX_SPLIT, (2 * num_sms + nlong - 1) / nlong)
+                             : 1;
+      if (nsplit > 1) {
+        k_factor_lcol<T><<<(nq + 7) / 8, 288, 0, s>>>(f.d_task_jp.p + q0, nq, f.d_fcols.p,
+                                                      f.d_fdiag.p, F);
+        nl++;
+      }
+      k_update_long<T><<<nlong * nsplit, 384, smem, s>>>(
+          f.d_task_row.p + t0, f.d_task_ptr.p + t0, f.d_task_jp.p, nlong, nsplit, f.d_frowp.p,
+          f.d_fcols.p, f.d_fdiag.p, F);
       nl++;
     }
     if (ns > 0) {

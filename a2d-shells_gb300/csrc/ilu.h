@@ -106,6 +106,8 @@ int dense_build(Factor &f, const void *F, cudaStream_t s, long long *launches);
 // indices staged in shared memory up to FACTOR_CTA_COLS).
 constexpr int FACTOR_WARP_COLS = 512;
 constexpr int FACTOR_CTA_COLS = 10240;
+// at most this many CTAs share one single-pivot long update task
+constexpr int FACTOR_MAX_SPLIT = 8;
 // Panels of the factorization: runs of levels with at most PANEL_LEVEL_ROWS
 // rows each, PANEL_MAX_ROWS rows in total.
 constexpr int PANEL_LEVEL_ROWS = 16;
