@@ -262,70 +262,110 @@ __global__ void k_tail_finalize(int s, int d, const int *__restrict__ fdiag,
 // the whole GPU.
 constexpr int PB6 = 6 * DENSE_PANEL;
 
+// Sum of v[r] over the warp for every r, spread over the lanes: halving
+// exchanges (offsets 16, 8, ...) leave each lane one partial sum for RHS
+// `rhs` (from its high lane bits), then the remaining offsets complete it;
+// lanes with (lane & (32 / R - 1)) == 0 hold the R distinct totals.  R + 4
+// shuffles per warp instead of 5 R.
 template <typename TV, int R>
-__device__ __forceinline__ void warp_sum(TV (&acc)[R]) {
+__device__ __forceinline__ TV warp_reduce_scatter(TV (&v)[R], int lane, int &rhs) {
+  static_assert(R >= 1 && R <= 32 && (R & (R - 1)) == 0, "R must be a power of two <= 32");
+  const unsigned full = 0xffffffffu;
+  int base = 0;
 #pragma unroll
-  for (int r = 0; r < R; r++)
+  for (int h = R / 2, o = 16; h >= 1; h /= 2, o /= 2) {
+    const bool up = (lane & o) != 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+    for (int k = 0; k < h; k++) {
+      const TV send = up ? v[k] : v[k + h];
+      const TV keep = up ? v[k + h] : v[k];
+      v[k] = keep + __shfl_xor_sync(full, send, o);
+    }
+    if (up) base += h;
+  }
+  TV sum = v[0];
+#pragma unroll
+  for (int o = 16 / R; o >= 1; o /= 2) sum += __shfl_xor_sync(full, sum, o);
+  rhs = base;
+  return sum;
+}
+
+// Stage a PB6 x R vector (row-major, [c][r]) in shared memory as [r][c], so
+// that lanes reading consecutive c hit consecutive banks.
+template <typename TV, int R>
+__device__ __forceinline__ void stage_panel_vec(TV *sv, const TV *v) {
+  for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) sv[(k % R) * PB6 + k / R] = v[k];
+}
+
+// acc[q][r] = sum_c row_q[c] sv[r][c] over this lane's columns (lane + 32 j).
+template <typename T, typename TV, int R, int NQ>
+__device__ __forceinline__ void panel_rows_dot(const T *const (&rows)[NQ], const TV *sv, int lane,
+                                               TV (&acc)[NQ][R]) {
+  T m[NQ][6];
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+#pragma unroll
+    for (int j = 0; j < 6; j++) m[q][j] = rows[q] ? rows[q][lane + 32 * j] : T(0);
+#pragma unroll
+  for (int q = 0; q < NQ; q++)
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      TV s = 0;
+#pragma unroll
+      for (int j = 0; j < 6; j++) s += (TV)m[q][j] * sv[r * PB6 + lane + 32 * j];
+      acc[q][r] = s;
+    }
 }
 
 // w = P v, P = PB6 x PB6 row-major, v and w PB6 x R; one warp per row of P.
 template <typename T, typename TV, int R>
 __global__ void __launch_bounds__(256) k_dense_panel_apply(const T *__restrict__ P, const TV *v,
                                                            TV *__restrict__ w) {
+  static_assert(PB6 == 6 * 32, "a panel row is six warp-wide segments");
   __shared__ TV sv[PB6 * R];
-  for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) sv[k] = v[k];
+  stage_panel_vec<TV, R>(sv, v);
   __syncthreads();
   const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (row >= PB6) return;
-  TV acc[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) acc[r] = 0;
-  const T *prow = P + (size_t)row * PB6;
-  for (int c = lane; c < PB6; c += 32) {
-    const TV m = (TV)prow[c];
-#pragma unroll
-    for (int r = 0; r < R; r++) acc[r] += m * sv[c * R + r];
-  }
-  warp_sum<TV, R>(acc);
-  TV out = 0;
-#pragma unroll
-  for (int r = 0; r < R; r++)
-    if (lane == r) out = acc[r];
-  if (lane < R) w[(size_t)row * R + lane] = out;
+  const T *rows[1] = {P + (size_t)row * PB6};
+  TV acc[1][R];
+  panel_rows_dot<T, TV, R, 1>(rows, sv, lane, acc);
+  int rhs;
+  const TV sum = warp_reduce_scatter<TV, R>(acc[0], lane, rhs);
+  if ((lane & (32 / R - 1)) == 0) w[(size_t)row * R + rhs] = sum;
 }
 
 // Rows [r0, r0 + nrows) of the dense segment yD: y -= M[rows, c0 : c0 + PB6] w;
-// CTA 0 also stores w as the panel's final values (yD rows c0 ..).  One warp
-// per row; M is the dense block, leading dimension ld.
+// CTA 0 also stores w as the panel's final values (yD rows c0 ..).  Each
+// warp takes DENSE_ROWS_PER_WARP rows, two at a time (their twelve loads
+// issued together); M is the dense block, leading dimension ld.
+constexpr int DENSE_ROWS_PER_WARP = 4;
 template <typename T, typename TV, int R>
 __global__ void __launch_bounds__(256) k_dense_panel_update(const T *__restrict__ M, int ld,
                                                             int r0, int nrows, int c0,
                                                             const TV *__restrict__ w, TV *yD) {
   __shared__ TV sw[PB6 * R];
-  for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) sw[k] = w[k];
-  __syncthreads();
+  stage_panel_vec<TV, R>(sw, w);
   if (blockIdx.x == 0)
-    for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) yD[(size_t)c0 * R + k] = sw[k];
-  const int rr = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (rr >= nrows) return;
-  const int row = r0 + rr;
-  TV acc[R];
+    for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) yD[(size_t)c0 * R + k] = w[k];
+  __syncthreads();
+  const int warp = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+#pragma unroll 1
+  for (int q = 0; q < DENSE_ROWS_PER_WARP; q += 2) {
+    const int rr = warp * DENSE_ROWS_PER_WARP + q;
+    if (rr >= nrows) break;
+    const T *rows[2] = {M + (size_t)(r0 + rr) * ld + c0,
+                        rr + 1 < nrows ? M + (size_t)(r0 + rr + 1) * ld + c0 : nullptr};
+    TV acc[2][R];
+    panel_rows_dot<T, TV, R, 2>(rows, sw, lane, acc);
 #pragma unroll
-  for (int r = 0; r < R; r++) acc[r] = 0;
-  const T *mrow = M + (size_t)row * ld + c0;
-  for (int c = lane; c < PB6; c += 32) {
-    const TV m = (TV)mrow[c];
-#pragma unroll
-    for (int r = 0; r < R; r++) acc[r] += m * sw[c * R + r];
+    for (int d = 0; d < 2; d++) {
+      int rhs;
+      const TV sum = warp_reduce_scatter<TV, R>(acc[d], lane, rhs);
+      if (rr + d < nrows && (lane & (32 / R - 1)) == 0)
+        yD[(size_t)(r0 + rr + d) * R + rhs] -= sum;
+    }
   }
-  warp_sum<TV, R>(acc);
-  TV out = 0;
-#pragma unroll
-  for (int r = 0; r < R; r++)
-    if (lane == r) out = acc[r];
-  if (lane < R) yD[(size_t)row * R + lane] -= out;
 }
 
 // Copy the factor's blocks of the dense block rows into the dense array
@@ -440,6 +480,11 @@ int dense_build(Factor &f, const void *F, cudaStream_t s, long long *launches) {
   return dense_build_t<double>(f, (const double *)F, s, launches);
 }
 
+static int dense_update_grid(int nrows) {
+  const int per_cta = 8 * DENSE_ROWS_PER_WARP;
+  return std::max(1, (nrows + per_cta - 1) / per_cta);
+}
+
 template <typename T, typename TV, int R>
 static void dense_solve(const Factor &f, TV *y, cudaStream_t s, long long &nl) {
   const int nd = f.dense_n, ld = 6 * nd, np = nd / DENSE_PANEL;
@@ -450,16 +495,16 @@ static void dense_solve(const Factor &f, TV *y, cudaStream_t s, long long &nl) {
     k_dense_panel_apply<T, TV, R><<<PB6 / 8, 256, 0, s>>>(
         DenseBufs<T>::L(f) + (size_t)p * PB6 * PB6, yD + (size_t)p * PB6 * R, w);
     const int r0 = (p + 1) * PB6, nr = ld - r0;
-    k_dense_panel_update<T, TV, R><<<std::max(1, (nr + 7) / 8), 256, 0, s>>>(M, ld, r0, nr,
-                                                                             p * PB6, w, yD);
+    k_dense_panel_update<T, TV, R><<<dense_update_grid(nr), 256, 0, s>>>(M, ld, r0, nr,
+                                                                         p * PB6, w, yD);
     nl += 2;
   }
   for (int p = np - 1; p >= 0; p--) {  // D + U: backward
     k_dense_panel_apply<T, TV, R><<<PB6 / 8, 256, 0, s>>>(
         DenseBufs<T>::U(f) + (size_t)p * PB6 * PB6, yD + (size_t)p * PB6 * R, w);
     const int nr = p * PB6;
-    k_dense_panel_update<T, TV, R><<<std::max(1, (nr + 7) / 8), 256, 0, s>>>(M, ld, 0, nr,
-                                                                             p * PB6, w, yD);
+    k_dense_panel_update<T, TV, R><<<dense_update_grid(nr), 256, 0, s>>>(M, ld, 0, nr,
+                                                                         p * PB6, w, yD);
     nl += 2;
   }
 }
