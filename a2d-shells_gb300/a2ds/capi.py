@@ -50,6 +50,9 @@ EXPORTS = [
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
     "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
     "a2ds_buckling_stats", "a2ds_eig_sens_thickness", "a2ds_eigen_shift_invert",
+    "a2ds_bdf_scan", "a2ds_bdf_destroy", "a2ds_bdf_get_sizes", "a2ds_bdf_get_connectivity",
+    "a2ds_bdf_get_bcs", "a2ds_bdf_get_element_descript", "a2ds_bdf_get_component_descript",
+    "a2ds_write_f5",
 ]
 
 
@@ -132,6 +135,16 @@ def load(build: bool = False):
     lib.a2ds_eigen_shift_invert.argtypes = [VP, ctypes.POINTER(BucklingOpts), VP, VP, P_D, P_D,
                                             P_D]
     lib.a2ds_eig_sens_thickness.argtypes = [VP, ctypes.c_int, P_D]
+    lib.a2ds_bdf_scan.argtypes = [ctypes.c_char_p, ctypes.POINTER(VP)]
+    lib.a2ds_bdf_destroy.argtypes = [VP]
+    lib.a2ds_bdf_get_sizes.argtypes = [VP, P_I, P_I, P_I, P_I, P_I, P_I]
+    lib.a2ds_bdf_get_connectivity.argtypes = [VP, P_I, P_I, P_I, P_D]
+    lib.a2ds_bdf_get_bcs.argtypes = [VP, P_I, P_I, P_I, P_D]
+    lib.a2ds_bdf_get_element_descript.argtypes = [VP, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+    lib.a2ds_bdf_get_component_descript.argtypes = [VP, ctypes.c_int, ctypes.c_char_p,
+                                                    ctypes.c_int]
+    lib.a2ds_write_f5.argtypes = [VP, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_char_p), P_I, P_D, ctypes.c_double]
     _lib = lib
     return lib
 
@@ -436,3 +449,131 @@ class LinearBuckling:
         out = np.zeros(num_groups)
         _check(self.lib.a2ds_eig_sens_thickness(self.a.h, int(n), _d(out)))
         return out
+
+
+A2DS_F5_CONNECTIVITY, A2DS_F5_NODES, A2DS_F5_DISPLACEMENTS = 1, 2, 4
+
+
+class ToFH5:
+    """TACSToFH5 for shell meshes (src/io/TACSToFH5.h): the connectivity,
+    node and displacement output classes written as a .f5 file."""
+
+    def __init__(self, assembler: "Assembler",
+                 write_flag=A2DS_F5_CONNECTIVITY | A2DS_F5_NODES | A2DS_F5_DISPLACEMENTS,
+                 elem_component=None):
+        self.a, self.lib = assembler, assembler.lib
+        self.write_flag = write_flag
+        self.elem_component = _i32(elem_component)
+        ncomp = 1 if elem_component is None else int(np.max(elem_component)) + 1
+        self.names = [None] * ncomp
+
+    def set_component_name(self, comp, name):
+        if 0 <= comp < len(self.names):
+            self.names[comp] = name
+
+    def write_to_file(self, file_name, vars=None, time=0.0):
+        vars = _f64(vars)
+        arr = (ctypes.c_char_p * len(self.names))(
+            *[None if n is None else n.encode() for n in self.names])
+        _check(self.lib.a2ds_write_f5(self.a.h, os.fsencode(file_name), self.write_flag,
+                                      len(self.names), arr, _i(self.elem_component), _d(vars),
+                                      float(time)))
+
+
+class MeshLoader:
+    """TACSMeshLoader (src/io/TACSMeshLoader.h) on one process: scan a
+    Nastran BDF file, then read back its connectivity and SPC entries or
+    build an Assembler from it (createTACS, TACSMeshLoader.cpp:1133, with
+    the one-shell-type-per-mesh restriction of this library)."""
+
+    def __init__(self):
+        self.lib = load()
+        self.h = None
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.a2ds_bdf_destroy(self.h)
+            self.h = None
+
+    def scan_bdf_file(self, file_name):
+        if self.h:
+            self.lib.a2ds_bdf_destroy(self.h)
+            self.h = None
+        h = VP()
+        _check(self.lib.a2ds_bdf_scan(os.fsencode(file_name), ctypes.byref(h)))
+        self.h = h
+        sz = [ctypes.c_int() for _ in range(6)]
+        _check(self.lib.a2ds_bdf_get_sizes(self.h, *[ctypes.byref(v) for v in sz]))
+        (self.num_nodes, self.num_elements, self._conn_size, self.num_bcs, self._bc_size,
+         self.num_components) = [v.value for v in sz]
+
+    def get_num_nodes(self):
+        return self.num_nodes
+
+    def get_num_elements(self):
+        return self.num_elements
+
+    def get_num_components(self):
+        return self.num_components
+
+    def get_connectivity(self):
+        """(elem_node_ptr, elem_node_conn, elem_component, Xpts)"""
+        ptr = np.zeros(self.num_elements + 1, np.int32)
+        conn = np.zeros(self._conn_size, np.int32)
+        comp = np.zeros(self.num_elements, np.int32)
+        X = np.zeros((self.num_nodes, 3))
+        _check(self.lib.a2ds_bdf_get_connectivity(self.h, _i(ptr), _i(conn), _i(comp), _d(X)))
+        return ptr, conn, comp, X
+
+    def get_bcs(self):
+        """(bc_nodes, bc_vars, bc_ptr, bc_vals)"""
+        nodes = np.zeros(self.num_bcs, np.int32)
+        ptr = np.zeros(self.num_bcs + 1, np.int32)
+        var = np.zeros(self._bc_size, np.int32)
+        vals = np.zeros(self._bc_size)
+        _check(self.lib.a2ds_bdf_get_bcs(self.h, _i(nodes), _i(var), _i(ptr), _d(vals)))
+        return nodes, var, ptr, vals
+
+    def get_element_descript(self, comp):
+        buf = ctypes.create_string_buffer(16)
+        _check(self.lib.a2ds_bdf_get_element_descript(self.h, comp, buf, 16))
+        return buf.value.decode()
+
+    def get_component_descript(self, comp):
+        buf = ctypes.create_string_buffer(40)
+        _check(self.lib.a2ds_bdf_get_component_descript(self.h, comp, buf, 40))
+        return buf.value.decode()
+
+    def bc_masks(self):
+        """The SPC entries as add_bcs arrays (nodes, 6-bit masks, num x 6
+        values); variables beyond the six shell DOFs are dropped."""
+        nodes, var, ptr, vals = self.get_bcs()
+        masks = np.zeros(self.num_bcs, np.int32)
+        v6 = np.zeros((self.num_bcs, 6))
+        for b in range(self.num_bcs):
+            for q in range(ptr[b], ptr[b + 1]):
+                if var[q] < 6:
+                    masks[b] |= 1 << int(var[q])
+                    v6[b, var[q]] = vals[q]
+        return nodes, masks, v6
+
+    def create_assembler(self, nonlinear=False):
+        """An Assembler on the scanned mesh with its SPC entries added; every
+        element must be CQUAD4/CQUADR (Quad4 shell) or every element
+        CQUAD9/CQUAD (Quad9 shell).  Material, thickness (per component:
+        set_thickness(t, elem_group=elem_component)) and initialize() are
+        left to the caller."""
+        ptr, conn, comp, X = self.get_connectivity()
+        npe = np.diff(ptr)
+        if self.num_elements == 0 or not (np.all(npe == 4) or np.all(npe == 9)):
+            raise A2dsError(-1, "the shell assembler needs all Quad4 or all Quad9 elements")
+        types = {self.get_element_descript(c) for c in np.unique(comp)}
+        allowed = {"CQUAD4", "CQUADR"} if npe[0] == 4 else {"CQUAD9", "CQUAD"}
+        if not types <= allowed:
+            raise A2dsError(-1, f"element types {sorted(types)} are not shell quads")
+        a = Assembler(X, conn.reshape(-1, int(npe[0])), nonlinear=nonlinear)
+        nodes, masks, v6 = self.bc_masks()
+        if nodes.size:
+            a.add_bcs(nodes, masks, v6)
+        self.elem_component = comp
+        return a

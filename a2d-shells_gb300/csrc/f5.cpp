@@ -1,0 +1,126 @@
+// .f5 output: the binary layout TACSToFH5::writeToFile writes through
+// TACSFH5File (src/io/TACSToFH5.cpp:126-358, src/io/TACSFH5.cpp:64-210) for
+// one process, restricted to the connectivity, node and displacement
+// classes (TACS_OUTPUT_CONNECTIVITY | NODES | DISPLACEMENTS).
+//
+// File = header + zones, native byte order.
+//   header: int num_components; per component: int length (with the NUL),
+//           the name and its NUL ("Component k" when no name is given).
+//   zone:   int {type (0 int, 2 float), dim1, dim2, len(zone)+1,
+//           len(vars)+1}, zone name + NUL, variable names + NUL, then
+//           dim1 x dim2 values (4-byte int or float).
+// Zones, in order: with CONNECTIVITY "components" (component of each
+// element), "ltypes" (element layout: 8 = Quad4, 9 = Quad9), "ptr"
+// (num_elements + 1 offsets), "connectivity"; with NODES and/or
+// DISPLACEMENTS one float zone "continuous data t=<time %.10e>" with
+// variables "X,Y,Z" then "u,v,w,rotx,roty,rotz", one row per node.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "a2ds.h"
+#include "a2ds_internal.h"
+#include "runtime.h"
+
+namespace {
+
+constexpr int kF5Int = 0, kF5Float = 2;
+constexpr int kLayoutQuad = 8, kLayoutQuadQuadratic = 9;
+
+void put_int(std::vector<char> &b, int v) {
+  const char *p = reinterpret_cast<const char *>(&v);
+  b.insert(b.end(), p, p + sizeof(int));
+}
+
+void put_str(std::vector<char> &b, const std::string &s) {
+  b.insert(b.end(), s.begin(), s.end());
+  b.push_back('\0');
+}
+
+template <typename T>
+void put_zone(std::vector<char> &b, int type, const std::string &zone, const std::string &vars,
+              int dim1, int dim2, const T *data) {
+  put_int(b, type);
+  put_int(b, dim1);
+  put_int(b, dim2);
+  put_int(b, (int)zone.size() + 1);
+  put_int(b, (int)vars.size() + 1);
+  put_str(b, zone);
+  put_str(b, vars);
+  const char *p = reinterpret_cast<const char *>(data);
+  b.insert(b.end(), p, p + sizeof(T) * (size_t)dim1 * dim2);
+}
+
+}  // namespace
+
+extern "C" int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_flag,
+                             int num_components, const char *const *component_names,
+                             const int *elem_component, const double *vars, double time) {
+  try {
+    using a2ds::fail;
+    if (!mesh || !file_name) return fail(A2DS_ERR_ARG, "mesh and file_name are required");
+    const int allowed = A2DS_F5_CONNECTIVITY | A2DS_F5_NODES | A2DS_F5_DISPLACEMENTS;
+    if (write_flag & ~allowed)
+      return fail(A2DS_ERR_ARG, "write_flag: only connectivity, nodes and displacements");
+    const a2ds::Mesh &m = mesh->m;
+    const int ne = m.ne, nn = m.nn, npe = m.npe;
+    int maxc = 0;
+    if (elem_component)
+      for (int e = 0; e < ne; e++) {
+        if (elem_component[e] < 0) return fail(A2DS_ERR_ARG, "negative component number");
+        maxc = std::max(maxc, elem_component[e]);
+      }
+    // TACSAssembler::getNumComponents: largest component number + 1
+    if (num_components < maxc + 1) num_components = maxc + 1;
+    std::vector<char> b;
+    put_int(b, num_components);
+    for (int k = 0; k < num_components; k++) {
+      std::string name = (component_names && component_names[k])
+                             ? std::string(component_names[k])
+                             : "Component " + std::to_string(k);
+      put_int(b, (int)name.size() + 1);
+      put_str(b, name);
+    }
+    if (write_flag & A2DS_F5_CONNECTIVITY) {
+      std::vector<int> comp(ne, 0), lt(ne, npe == 4 ? kLayoutQuad : kLayoutQuadQuadratic),
+          ptr(ne + 1);
+      if (elem_component) std::copy(elem_component, elem_component + ne, comp.begin());
+      for (int e = 0; e <= ne; e++) ptr[e] = npe * e;
+      put_zone(b, kF5Int, "components", "components", ne, 1, comp.data());
+      put_zone(b, kF5Int, "ltypes", "ltypes", ne, 1, lt.data());
+      put_zone(b, kF5Int, "ptr", "ptr", ne + 1, 1, ptr.data());
+      put_zone(b, kF5Int, "connectivity", "connectivity", ne * npe, 1, m.conn.data());
+    }
+    const bool nodes = write_flag & A2DS_F5_NODES, disp = write_flag & A2DS_F5_DISPLACEMENTS;
+    if (nodes || disp) {
+      std::string names = nodes ? "X,Y,Z" : "";
+      if (disp) names += std::string(nodes ? "," : "") + "u,v,w,rotx,roty,rotz";
+      const int dim2 = (nodes ? 3 : 0) + (disp ? 6 : 0), off = nodes ? 3 : 0;
+      std::vector<float> v((size_t)nn * dim2, 0.0f);
+      for (int i = 0; i < nn; i++) {
+        if (nodes)
+          for (int j = 0; j < 3; j++) v[(size_t)i * dim2 + j] = (float)m.X[(size_t)i * 3 + j];
+        if (disp)
+          for (int j = 0; j < 6; j++)
+            v[(size_t)i * dim2 + off + j] = vars ? (float)vars[(size_t)i * 6 + j] : 0.0f;
+      }
+      char zone[128];
+      snprintf(zone, sizeof(zone), "continuous data t=%.10e", time);
+      put_zone(b, kF5Float, zone, names, nn, dim2, v.data());
+    }
+    FILE *fp = fopen(file_name, "wb");
+    if (!fp) return fail(A2DS_ERR_ARG, std::string("cannot create ") + file_name);
+    const size_t w = fwrite(b.data(), 1, b.size(), fp);
+    const int c = fclose(fp);
+    if (w != b.size() || c != 0) return fail(A2DS_ERR_STATE, std::string("short write to ") + file_name);
+    return 0;
+  } catch (const std::bad_alloc &) {
+    return a2ds::fail(A2DS_ERR_NOMEM, "host allocation failed");
+  } catch (...) {
+    return a2ds::fail(A2DS_ERR_STATE, "unexpected host exception");
+  }
+}

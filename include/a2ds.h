@@ -295,6 +295,55 @@ int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out);
    commented out).  Needs a preceding a2ds_buckling_solve on this mesh. */
 int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt);
 
+/* ------------------------------------------------------ BDF mesh input
+   Replaces: TACSMeshLoader::scanBDFFile (src/io/TACSMeshLoader.cpp:569-1098),
+   getConnectivity (:1247), getBCs (:1272), getElementDescript and
+   getComponentDescript (src/io/TACSMeshLoader.h:73-74) on one process.
+   Reads GRID / GRID*, SPC / SPC* and the element cards CBAR, CQUADR,
+   CQUAD4, CQUAD9, CQUAD, CHEXA (8 nodes), CTRIA3 and CTETRA, with the same
+   field widths, continuation rules, Nastran real formats, node-order
+   conversion (CQUAD4/CQUADR, CQUAD9/CQUAD, CHEXA) and renumbering (nodes by
+   sorted file node number, elements by sorted file element number).  Where
+   the reference aborts (unreadable file, empty bulk line, bad element
+   card, undefined node) the scan fails with A2DS_ERR_ARG.  Arrays:
+   elem_node_ptr num_elements + 1, elem_node_conn conn_size,
+   elem_component num_elements (0-based), Xpts num_nodes x 3; bc_nodes
+   num_bcs, bc_ptr num_bcs + 1, bc_vars / bc_vals bc_vars_size (variable
+   0..7 per entry).  Host only: no GPU needed. */
+typedef struct a2ds_bdf_s *a2ds_bdf;
+int a2ds_bdf_scan(const char *file_name, a2ds_bdf *out);
+int a2ds_bdf_destroy(a2ds_bdf bdf);
+int a2ds_bdf_get_sizes(a2ds_bdf bdf, int *num_nodes, int *num_elements, int *conn_size,
+                       int *num_bcs, int *bc_vars_size, int *num_components);
+int a2ds_bdf_get_connectivity(a2ds_bdf bdf, int *elem_node_ptr, int *elem_node_conn,
+                              int *elem_component, double *Xpts);
+int a2ds_bdf_get_bcs(a2ds_bdf bdf, int *bc_nodes, int *bc_vars, int *bc_ptr, double *bc_vals);
+/* Element type name of a component (first card seen for it, "CTETRA10" for
+   10-node tetrahedra) and its "$       Shell" comment name ("" if none),
+   copied into name[len] with a terminating NUL. */
+int a2ds_bdf_get_element_descript(a2ds_bdf bdf, int comp, char *name, int len);
+int a2ds_bdf_get_component_descript(a2ds_bdf bdf, int comp, char *descript, int len);
+
+/* ------------------------------------------------------------ .f5 output
+   Replaces: TACSToFH5(assembler, TACS_BEAM_OR_SHELL_ELEMENT, write_flag)
+   with setComponentName and writeToFile (src/io/TACSToFH5.cpp:35-358;
+   file layout of TACSFH5File, src/io/TACSFH5.cpp:64-210) on one process,
+   for the connectivity, node and displacement output classes: the same
+   bytes as the reference for the same mesh, names and variables.
+   write_flag: A2DS_F5_* bits (strain, stress, extra and load output
+   classes are not written: A2DS_ERR_ARG).  component_names: NULL or
+   num_components entries (NULL entries give "Component k");
+   num_components is raised to 1 + the largest elem_component value;
+   elem_component: NULL (all 0) or num_elements values; vars: NULL (zeros)
+   or num_nodes x 6 in the caller's node numbering (a load path or an
+   eigenvector); time: the zone time stamp (getSimulationTime). */
+#define A2DS_F5_CONNECTIVITY 1
+#define A2DS_F5_NODES 2
+#define A2DS_F5_DISPLACEMENTS 4
+int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_flag, int num_components,
+                  const char *const *component_names, const int *elem_component,
+                  const double *vars, double time);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,8 @@
 #include "TACSSchurMat.h"
 #include "TACSShellElementDefs.h"
 #include "TACSShellElementTransform.h"
+#include "TACSMeshLoader.h"
+#include "TACSToFH5.h"
 #include "TacsUtilities.h"
 
 #ifdef TACS_USE_COMPLEX
@@ -504,6 +506,102 @@ static void run_orderings(const std::string &in, const std::string &out) {
   assembler->decref();
 }
 
+// The reference's BDF loader (TACSMeshLoader::scanBDFFile,
+// src/io/TACSMeshLoader.cpp:569-1098) on one file: connectivity, nodes,
+// SPC entries and the per-component names, as the loader returns them.
+static void run_bdf(const std::string &file, const std::string &out) {
+  TACSMeshLoader *loader = new TACSMeshLoader(MPI_COMM_WORLD);
+  loader->incref();
+  const int fail = loader->scanBDFFile(file.c_str());
+  int nn = 0, ne = 0, nbcs = 0;
+  const int *ptr, *conn, *comp, *bc_nodes, *bc_vars, *bc_ptr;
+  const TacsScalar *X, *bc_vals;
+  loader->getConnectivity(&nn, &ne, &ptr, &conn, &comp, &X);
+  loader->getBCs(&nbcs, &bc_nodes, &bc_vars, &bc_ptr, &bc_vals);
+  const int ncomp = loader->getNumComponents();
+  int sizes[5] = {fail, nn, ne, nbcs, ncomp};
+  save_i(out, "sizes", sizes, {5});
+  save_i(out, "elem_node_ptr", ptr, {ne + 1});
+  save_i(out, "elem_node_conn", conn, {ptr[ne]});
+  save_i(out, "elem_component", comp, {ne});
+  save_d(out, "Xpts", X, {nn, 3});
+  save_i(out, "bc_nodes", bc_nodes, {nbcs});
+  save_i(out, "bc_ptr", bc_ptr, {nbcs + 1});
+  save_i(out, "bc_vars", bc_vars, {bc_ptr[nbcs]});
+  save_d(out, "bc_vals", bc_vals, {bc_ptr[nbcs]});
+  // component names, NUL-padded to 40 characters each
+  std::vector<char> names((size_t)2 * ncomp * 40, 0);
+  for (int c = 0; c < ncomp; c++) {
+    strncpy(&names[(size_t)c * 40], loader->getElementDescript(c), 39);
+    strncpy(&names[(size_t)(ncomp + c) * 40], loader->getComponentDescript(c), 39);
+  }
+  write_npy(out + "/names" + SUFFIX + ".npy", "|u1", names.data(), 1, {2 * ncomp, 40});
+  printf("bdf fixture: nn=%d ne=%d nbcs=%d ncomp=%d\n", nn, ne, nbcs, ncomp);
+  loader->decref();
+}
+
+// TACSToFH5::writeToFile (src/io/TACSToFH5.cpp:126) for a shell mesh with
+// per-element components, named components 0 and 1, the given variables
+// and each of four output-class flags: in/X, conn, comp, vars ->
+// out/f5_<flag>.f5.
+static void run_f5(const std::string &in, const std::string &out) {
+  std::vector<long> xs, cs;
+  std::vector<double> X = read_npy<double>(in + "/X.npy", &xs);
+  std::vector<int> conn = read_npy<int>(in + "/conn.npy", &cs);
+  std::vector<int> comp = read_npy<int>(in + "/comp.npy");
+  std::vector<double> vars = read_npy<double>(in + "/vars.npy");
+  const int nn = (int)xs[0], ne = (int)cs[0], npe = (int)cs[1];
+  int ncomp = 0;
+  for (int e = 0; e < ne; e++) ncomp = comp[e] + 1 > ncomp ? comp[e] + 1 : ncomp;
+  TACSShellTransform *tr = new TACSShellNaturalTransform();
+  tr->incref();
+  TACSMaterialProperties *props =
+      new TACSMaterialProperties(2700.0, 921.0, 70e9, 0.3, 270e6, 0.0, 230.0);
+  props->incref();
+  std::vector<TACSElement *> per_comp(ncomp);
+  for (int c = 0; c < ncomp; c++) {
+    TACSIsoShellConstitutive *con = new TACSIsoShellConstitutive(props, 1e-2, c);
+    per_comp[c] = make_element(npe == 4 ? "TACSQuad4Shell" : "TACSQuad9Shell", tr, con);
+    per_comp[c]->incref();
+    per_comp[c]->setComponentNum(c);
+  }
+  std::vector<TACSElement *> elems(ne);
+  for (int e = 0; e < ne; e++) elems[e] = per_comp[comp[e]];
+  TACSAssembler *assembler = new TACSAssembler(MPI_COMM_WORLD, 6, nn, ne);
+  assembler->incref();
+  std::vector<int> ptr(ne + 1);
+  for (int e = 0; e <= ne; e++) ptr[e] = npe * e;
+  assembler->setElementConnectivity(ptr.data(), conn.data());
+  assembler->setElements(elems.data());
+  assembler->initialize();
+  TACSBVec *Xv = assembler->createNodeVec();
+  Xv->incref();
+  TacsScalar *xa;
+  Xv->getArray(&xa);
+  for (int i = 0; i < 3 * nn; i++) xa[i] = X[i];
+  assembler->setNodes(Xv);
+  TACSBVec *q = assembler->createVec();
+  q->incref();
+  TacsScalar *qa;
+  q->getArray(&qa);
+  for (int i = 0; i < 6 * nn; i++) qa[i] = vars[i];
+  assembler->setVariables(q);
+  const int flags[4] = {TACS_OUTPUT_CONNECTIVITY | TACS_OUTPUT_NODES | TACS_OUTPUT_DISPLACEMENTS,
+                        TACS_OUTPUT_NODES, TACS_OUTPUT_DISPLACEMENTS, TACS_OUTPUT_CONNECTIVITY};
+  for (int f = 0; f < 4; f++) {
+    TACSToFH5 *f5 = new TACSToFH5(assembler, TACS_BEAM_OR_SHELL_ELEMENT, flags[f]);
+    f5->incref();
+    f5->setComponentName(0, "skin");
+    if (ncomp > 1) f5->setComponentName(1, "stiffener panel");
+    const std::string path = out + "/f5_" + std::to_string(flags[f]) + ".f5";
+    remove(path.c_str());
+    f5->writeToFile(path.c_str());
+    f5->decref();
+  }
+  printf("f5 fixture: nn=%d ne=%d ncomp=%d\n", nn, ne, ncomp);
+  assembler->decref();
+}
+
 int main(int argc, char **argv) {
   MPI_Init(&argc, &argv);
   TacsInitialize();
@@ -513,6 +611,10 @@ int main(int argc, char **argv) {
     run_orderings(argv[2], argv[3]);
   } else if (argc >= 4 && strcmp(argv[1], "assembly") == 0) {
     run_assembly(argv[2], argv[3]);
+  } else if (argc >= 4 && strcmp(argv[1], "bdf") == 0) {
+    run_bdf(argv[2], argv[3]);
+  } else if (argc >= 4 && strcmp(argv[1], "f5") == 0) {
+    run_f5(argv[2], argv[3]);
   } else {
     fprintf(stderr, "usage: golden_gen element <out> | assembly <in> <out>\n");
     return 2;

@@ -248,19 +248,43 @@ static inline int MPI_Waitany(int, MPI_Request *, int *index, MPI_Status *) {
   return 0;
 }
 
+/* MPI-IO over stdio.  A file view's displacement (bytes) is kept per open
+   file: MPI_File_write / read continue from the view start, and the
+   explicit-offset calls take their offset in elements from it. */
+static inline MPI_Offset *a2ds_mpi_view_disp(MPI_File fp, int release) {
+  static MPI_File files[16];
+  static MPI_Offset disp[16];
+  for (int k = 0; k < 16; k++)
+    if (files[k] == fp) {
+      if (release) files[k] = NULL;
+      return &disp[k];
+    }
+  for (int k = 0; k < 16; k++)
+    if (!files[k]) {
+      files[k] = fp;
+      disp[k] = 0;
+      return &disp[k];
+    }
+  return &disp[0];
+}
 static inline int MPI_File_open(MPI_Comm, const char *name, int mode, MPI_Info,
                                 MPI_File *fp) {
   *fp = fopen(name, (mode & MPI_MODE_WRONLY) ? "wb" : "rb");
+  if (*fp) *a2ds_mpi_view_disp(*fp, 0) = 0;
   return *fp ? 0 : 1;
 }
 static inline int MPI_File_close(MPI_File *fp) {
-  if (*fp) fclose(*fp);
+  if (*fp) {
+    a2ds_mpi_view_disp(*fp, 1);
+    fclose(*fp);
+  }
   *fp = NULL;
   return 0;
 }
 static inline int MPI_File_set_size(MPI_File, MPI_Offset) { return 0; }
 static inline int MPI_File_set_view(MPI_File fp, MPI_Offset disp, MPI_Datatype,
                                     MPI_Datatype, const char *, MPI_Info) {
+  *a2ds_mpi_view_disp(fp, 0) = disp;
   return fseek(fp, (long)disp, SEEK_SET);
 }
 static inline int MPI_File_write(MPI_File fp, const void *b, int n,
@@ -276,13 +300,13 @@ static inline int MPI_File_read(MPI_File fp, void *b, int n, MPI_Datatype t,
 static inline int MPI_File_write_at_all(MPI_File fp, MPI_Offset off,
                                         const void *b, int n, MPI_Datatype t,
                                         MPI_Status *) {
-  fseek(fp, (long)off, SEEK_SET);
+  fseek(fp, (long)(*a2ds_mpi_view_disp(fp, 0) + off * (MPI_Offset)a2ds_mpi_tsize(t)), SEEK_SET);
   fwrite(b, a2ds_mpi_tsize(t), (size_t)n, fp);
   return 0;
 }
 static inline int MPI_File_read_at_all(MPI_File fp, MPI_Offset off, void *b,
                                        int n, MPI_Datatype t, MPI_Status *) {
-  fseek(fp, (long)off, SEEK_SET);
+  fseek(fp, (long)(*a2ds_mpi_view_disp(fp, 0) + off * (MPI_Offset)a2ds_mpi_tsize(t)), SEEK_SET);
   size_t r = fread(b, a2ds_mpi_tsize(t), (size_t)n, fp);
   return r == (size_t)n ? 0 : 1;
 }

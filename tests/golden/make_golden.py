@@ -12,6 +12,10 @@ builds) and packs inputs and outputs into small .npz files:
                         reference's node CSR, AMD permutation, BCSR pattern,
                         assembled K and G, ILU pattern and factor, load path
                         and buckling eigenpairs
+  bdf_*.bdf, bdf.npz    synthetic Nastran decks (bdf_cases.py) and the
+                        reference loader's arrays for each
+  f5.npz                .f5 files of the reference's TACSToFH5 (raw bytes)
+                        for two seeded meshes and four output-class flags
 
 Only this container has the reference sources; the fixtures are committed so
 the tests never need them.  Run:  python tests/golden/make_golden.py
@@ -28,6 +32,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(REPO, "a2d-shells_gb300"))
+sys.path.insert(0, HERE)
 
 from a2ds import mesh as meshgen  # noqa: E402
 
@@ -184,8 +189,82 @@ def make_thermal():
              gm_restarts=15, lanczos=100, neig=50, temperature=10.0, alpha_t=1e-5)
 
 
+def parse_bdf_reference(path):
+    """The reference loader's arrays for one deck (golden_gen bdf)."""
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run([os.path.join(REF_OUT, "golden_gen"), "bdf", path, d], check=True)
+        return load_dir(d)
+
+
+def make_bdf():
+    """Synthetic decks (bdf_cases.py) written here, the reference loader's
+    arrays for each in bdf.npz, and a buckling case on the cylinder deck's
+    parsed mesh (displacement control through nonzero SPC values)."""
+    import bdf_cases
+    decks = {"bdf_mixed": bdf_cases.mixed_deck(),
+             "bdf_cyl_q4_8x16": bdf_cases.cylinder_deck(meshgen.cylinder(8, 16, order=2))}
+    out = {}
+    for name, text in decks.items():
+        path = os.path.join(HERE, name + ".bdf")
+        with open(path, "w") as f:
+            f.write(text)
+        for k, v in parse_bdf_reference(path).items():
+            out[f"{name}__{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "bdf.npz"), **out)
+    print("wrote bdf.npz")
+    # the cylinder deck's mesh as the reference loader returns it
+    pre = "bdf_cyl_q4_8x16__"
+    ptr, conn = out[pre + "elem_node_ptr"], out[pre + "elem_node_conn"]
+    X = out[pre + "Xpts"]
+    nodes, var, bptr, vals = (out[pre + "bc_nodes"], out[pre + "bc_vars"], out[pre + "bc_ptr"],
+                              out[pre + "bc_vals"])
+    mask = np.zeros(nodes.size, np.int32)
+    v6 = np.zeros((nodes.size, 6))
+    for b in range(nodes.size):
+        for q in range(bptr[b], bptr[b + 1]):
+            if var[q] < 6:
+                mask[b] |= 1 << int(var[q])
+                v6[b, var[q]] = vals[q]
+    ne = ptr.size - 1
+    m = meshgen.ShellMesh(X=X, conn=conn.reshape(ne, 4), bc_nodes=nodes.astype(np.int32),
+                          bc_mask=mask, bc_vals=v6, rhs=np.zeros((X.shape[0], 6)),
+                          thickness=np.full(ne, 2e-3), dv_group=np.zeros(ne, np.int32))
+    run_case("bdf_cyl_q4_8x16_lu", m, lev=1000000, gm_m=10, gm_restarts=15, lanczos=100,
+             neig=20)
+
+
+def make_f5():
+    """.f5 files written by the reference's TACSToFH5 for a Quad4 and a Quad9
+    cylinder with two components and a seeded variable vector, for four
+    output-class flags; stored as raw bytes in f5.npz with the inputs."""
+    rng = np.random.default_rng(11)
+    out = {}
+    for name, m in {"q4": meshgen.cylinder(4, 8, order=2),
+                    "q9": meshgen.cylinder(2, 4, order=3)}.items():
+        comp = (np.arange(m.num_elements) % 3 == 1).astype(np.int32)
+        vars_ = rng.standard_normal((m.num_nodes, 6)) * 1e-3
+        with tempfile.TemporaryDirectory() as d:
+            ind, outd = os.path.join(d, "in"), os.path.join(d, "out")
+            os.makedirs(ind)
+            os.makedirs(outd)
+            np.save(os.path.join(ind, "X.npy"), np.ascontiguousarray(m.X, np.float64))
+            np.save(os.path.join(ind, "conn.npy"), np.ascontiguousarray(m.conn, np.int32))
+            np.save(os.path.join(ind, "comp.npy"), comp)
+            np.save(os.path.join(ind, "vars.npy"), vars_)
+            subprocess.run([os.path.join(REF_OUT, "golden_gen"), "f5", ind, outd], check=True)
+            for f in sorted(os.listdir(outd)):
+                with open(os.path.join(outd, f), "rb") as fh:
+                    out[f"{name}__{f[:-3]}"] = np.frombuffer(fh.read(), np.uint8)
+        out.update({f"{name}__X": m.X, f"{name}__conn": m.conn, f"{name}__comp": comp,
+                    f"{name}__vars": vars_})
+    np.savez_compressed(os.path.join(HERE, "f5.npz"), **out)
+    print("wrote f5.npz", sorted(k for k in out if "f5_" in k))
+
+
 def main():
     build_reference()
+    make_f5()
+    make_bdf()
     make_thermal()
     make_orderings()
     make_elements()
