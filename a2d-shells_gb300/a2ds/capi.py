@@ -396,7 +396,7 @@ class LinearBuckling:
     eig_tol): solve(rhs) then extract_eigenvalue / extract_eigenvector."""
 
     def __init__(self, assembler: Assembler, sigma, max_lanczos=100, num_eigvals=10,
-                 eig_tol=1e-10, lev_fill=1000000, precision=64, seed=0, block_size=8,
+                 eig_tol=1e-10, lev_fill=1000000, precision=64, seed=0, block_size=4,
                  gmres_m=30, gmres_restarts=15, gmres_rtol=1e-12, gmres_atol=1e-30):
         self.a = assembler
         self.lib = assembler.lib

@@ -66,7 +66,7 @@ def newton_preload(assembler: capi.Assembler, rhs, bc_nodes, bc_mask, load: floa
 
 def preload_buckling(assembler: capi.Assembler, u, sigma: float, num_eigvals: int = 5,
                      max_lanczos: int = 120, eig_tol: float = 1e-10, precision: int = 64,
-                     block_size: int = 8):
+                     block_size: int = 4):
     """Lowest buckling multipliers about the preloaded state u:
     K_T(u) x + lam G(u) x = 0.  Returns (lam, LinearBuckling handle)."""
     KT, G = assembler.create_mat(), assembler.create_mat()

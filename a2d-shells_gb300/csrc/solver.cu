@@ -1101,7 +1101,7 @@ void a2ds_buckling_default_opts(a2ds_buckling_opts *o) {
   o->gmres_atol = 1e-30;
   o->precision = 64;
   o->seed = 0;
-  o->block_size = 8;
+  o->block_size = 4;
 }
 
 int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const double *rhs,

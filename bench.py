@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--precision", type=int, default=48, choices=[64, 48, 32],
                    help="factor arithmetic: 64 FP64, 48 double-float on the FP32 pipe, 32 FP32 "
                         "(solves and refinement are FP64 in every case)")
-    p.add_argument("--block", type=int, default=8, choices=[1, 2, 4, 8, 16],
+    p.add_argument("--block", type=int, default=4, choices=[1, 2, 4, 8, 16],
                    help="Lanczos block size")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
