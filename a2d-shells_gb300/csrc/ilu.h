@@ -110,8 +110,8 @@ constexpr int FACTOR_CTA_COLS = 10240;
 constexpr int FACTOR_MAX_SPLIT = 8;
 // Panels of the factorization: runs of levels with at most PANEL_LEVEL_ROWS
 // rows each, PANEL_MAX_ROWS rows in total.
-constexpr int PANEL_LEVEL_ROWS = 16;
-constexpr int PANEL_MAX_ROWS = 32;
+constexpr int PANEL_LEVEL_ROWS = 32;
+constexpr int PANEL_MAX_ROWS = 64;
 // union U columns of a panel staged in shared memory by its phase-2 kernel
 constexpr int PANEL_UC_SMEM = 8192;
 
