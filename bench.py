@@ -131,7 +131,7 @@ PREC_NAME = {64: "FP64 factors", 48: "double-float (2 x FP32) factors with FP64 
 
 # DRAM traffic of one numeric factorization of the bench workload, summed
 # over all its launches from an ncu capture (profiles/factor_cylinder256x512_traffic.md)
-FACTOR_TRAFFIC = {(256, 512, 48): 625.05e9}
+FACTOR_TRAFFIC = {(256, 512, 48): 279.65e9}
 
 
 def measured_peaks():
@@ -409,8 +409,9 @@ def main():
                 "h2d_bytes_per_step": int(m.num_nodes * 6 * 8),
                 "d2h_bytes_per_step": int((args.neig * (2 + 6 * m.num_nodes) + 6 * m.num_nodes) * 8)},
         "roofline": {
-            "kernel": ("numeric complete-LU factorization of K + sigma G: k_update_long / "
-                       "k_update_group with k_factor_pivot and k_factor_lcol, per level"),
+            "kernel": ("numeric complete-LU factorization of K + sigma G: panel-blocked trailing "
+                       "updates (k_update_panel), per-level k_update_long / k_update_group, "
+                       "k_factor_pivot_df"),
             "bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
             "frac": (achieved_gbs / hbm) if hbm else None,
             "traffic": FACTOR_TRAFFIC.get((args.nx, args.ny, args.precision)),
@@ -421,9 +422,11 @@ def main():
                         "fp64_peak_tflops_measured_dgemm": fp64,
                         "frac_of_fp64_peak": (achieved_tf / fp64) if fp64 else None,
                         "flops_per_factorization": stats["factor_flops"]},
-            "note": ("neither HBM nor tensor bound: the level-scheduled update is bound by "
-                     "the FP64 pipe in FP64 (~1/58 of FP32 on GB300) and by memory latency in "
-                     "double-float; the HBM fraction is reported for the contract"),
+            "note": ("neither HBM nor tensor bound: in FP64 the block updates are bound by the "
+                     "FP64 pipe (~1/58 of FP32 on GB300); in double-float (~12 FP32 operations "
+                     "per multiply-subtract) the panel updates are bound by the FP32 issue rate "
+                     "and the per-level kernels by launch and memory latency; the HBM fraction "
+                     "is reported for the contract"),
         },
         "phases_s": {k: stats[k] for k in ["assemble_k_s", "assemble_g_s", "factor_s", "path_s",
                                             "lanczos_s"]},
