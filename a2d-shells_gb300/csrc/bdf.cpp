@@ -16,9 +16,9 @@
 //   * Element cards, first matching prefix of CBAR CQUADR CQUAD4 CQUAD8
 //     CQUAD9 CQUAD CHEXA27 CHEXA CTRIA3 CTETRA ('*' after the name: 16-wide
 //     fields): element number and component at fields 1-2, then node
-//     numbers; blank fields are skipped, a field reading <= 0 ends the list,
-//     and a following line that starts with ' ' or '*' continues it (from
-//     column 8).  Node order is converted to the tensor-product order of
+//     numbers; blank fields are skipped, a field reading <= 0 (or cut short
+//     by the end of the line) ends the list, and a following line that
+//     starts with ' ' or '*' continues it (from column 8).  Node order is converted to the tensor-product order of
 //     the shell elements for CQUAD4/CQUADR, CQUAD9/CQUAD and CHEXA
 //     (TACSMeshLoader.cpp:932-956).
 //   * Reals accept the Nastran short exponent forms (1.5-3, 2.+4) and D
@@ -128,8 +128,11 @@ bool parse_element(const Lines &L, size_t &k, size_t width, int max_nodes, int &
   if (comp <= 0) return false;
   while ((int)nodes.size() < max_nodes) {
     for (; (int)nodes.size() < max_nodes && at < line.size(); at += width) {
+      // blank only when the whole field is present and white (a field cut
+      // short by the end of the line, e.g. a trailing "\r", reads as 0 and
+      // ends the list, as in the reference)
       const std::string f = field(line, at, width);
-      if (blank(f)) continue;
+      if (f.size() == width && blank(f)) continue;
       const int v = to_int(f);
       if (v <= 0) return true;  // end of the node list
       nodes.push_back(v);

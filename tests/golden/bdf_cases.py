@@ -8,6 +8,11 @@ mixed_deck()     every card form the loader reads: GRID in small fixed, free
                  nodes), SPC and SPC*, comment and component-name lines,
                  cards the loader skips, unsorted and gapped node and
                  element numbers, and text after ENDDATA.
+plain_deck()     the whole file as bulk data (no BEGIN BULK, no ENDDATA),
+                 CRLF line ends.
+crlf_continuation_deck()
+                 CRLF line ends under a continued card: a deck the
+                 reference's loader rejects.
 cylinder_deck()  a Quad4 cylinder as GRID* / CQUAD4 cards (nodes and
                  elements written in shuffled order), clamped at x = 0 and
                  compressed by a prescribed axial displacement at x = L
@@ -87,6 +92,31 @@ def mixed_deck() -> str:
     L.append("ENDDATA")
     L.append("GRID           999       0     9.0     9.0     9.0")
     return "\n".join(L) + "\n"
+
+
+def plain_deck() -> str:
+    """No executive/case sections and no BEGIN BULK (the whole file is bulk
+    data), CRLF line ends, no ENDDATA, one-line element cards and a trailing
+    comment."""
+    L = []
+    for k in range(1, 10):
+        L.append(_small("GRID", 10 * k, 0, f"{(k - 1) % 3}.", f"{(k - 1) // 3}.", "0."))
+    L.append(_small("CQUAD4", 3, 2, 10, 20, 50, 40))
+    L.append(_small("CQUAD4", 1, 2, 20, 30, 60, 50))
+    L.append(_small("CTRIA3", 2, 1, 40, 50, 80))
+    L.append(_small("SPC", 3, 10, "123", "1.5-2"))
+    L.append("$ end of deck")
+    return "\r\n".join(L) + "\r\n"
+
+
+def crlf_continuation_deck() -> str:
+    """CRLF line ends under a card that continues: the "\r" ending the first
+    line is read as a node field of 0, so the card ends there and has too few
+    nodes (the reference's loader aborts on this deck)."""
+    L = [_small("GRID", k, 0, f"{k}.", "0.", "0.") for k in range(1, 10)]
+    L.append(_small("CQUAD9", 1, 1, 1, 2, 3, 4, 5, 6))
+    L.append(f"{'':<8}{7:>8}{8:>8}{9:>8}")
+    return "\r\n".join(L) + "\r\n"
 
 
 def cylinder_deck(m, disp=-1.0e-5, seed=5):

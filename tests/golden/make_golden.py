@@ -201,12 +201,12 @@ def make_bdf():
     arrays for each in bdf.npz, and a buckling case on the cylinder deck's
     parsed mesh (displacement control through nonzero SPC values)."""
     import bdf_cases
-    decks = {"bdf_mixed": bdf_cases.mixed_deck(),
+    decks = {"bdf_mixed": bdf_cases.mixed_deck(), "bdf_plain": bdf_cases.plain_deck(),
              "bdf_cyl_q4_8x16": bdf_cases.cylinder_deck(meshgen.cylinder(8, 16, order=2))}
     out = {}
     for name, text in decks.items():
         path = os.path.join(HERE, name + ".bdf")
-        with open(path, "w") as f:
+        with open(path, "w", newline="") as f:
             f.write(text)
         for k, v in parse_bdf_reference(path).items():
             out[f"{name}__{k}"] = v

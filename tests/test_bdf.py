@@ -17,7 +17,7 @@ import pytest
 from conftest import GOLDEN
 from a2ds import capi
 
-DECKS = ["bdf_mixed", "bdf_cyl_q4_8x16"]
+DECKS = ["bdf_mixed", "bdf_plain", "bdf_cyl_q4_8x16"]
 
 
 def golden(name):
@@ -62,9 +62,14 @@ def test_loader_errors(tmp_path):
         "short": ("BEGIN BULK\nGRID           1       0     0.0     0.0     0.0\n"
                   "CQUAD4         1       1       1       1       1\nENDDATA\n"),
     }
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import bdf_cases
+    # CRLF under a continued card: the reference's loader aborts on it too
+    bad["crlf_continuation"] = bdf_cases.crlf_continuation_deck()
     for key, text in bad.items():
         p = tmp_path / f"{key}.bdf"
-        p.write_text(text)
+        p.write_bytes(text.encode())
         with pytest.raises(capi.A2dsError):
             ml.scan_bdf_file(str(p))
 
