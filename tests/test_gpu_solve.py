@@ -355,3 +355,39 @@ def test_thermal_buckling_matches_reference():
     # G, so it agrees only to a few 1e-6 here
     ref = f["eigvals"][np.argmin(np.abs(f["eigvals"]))]
     assert abs(lam[0] - ref) <= 1e-5 * abs(ref), (lam[0], ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [64, 48, 32])
+def test_zero_pivot_block_is_reported(precision):
+    """A zero diagonal block (TACS's BMatComputeInverse fails on it): the
+    factorization reports A2DS_ERR_SINGULAR for FP64, double-float and FP32
+    factors (the kernels carry on with zero inverses; no value is used)."""
+    f = np.load(os.path.join(GOLDEN, "cyl_q4_4x8_lu.npz"))
+    a = setup(f)
+    K = a.create_mat()
+    a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
+    rowp, cols, vals = K.get_arrays()
+    r = 0  # the first row: no L blocks, so its diagonal block stays exactly zero
+    d = rowp[r] + int(np.searchsorted(cols[rowp[r]:rowp[r + 1]], r))
+    vals = vals.copy()
+    vals[d] = 0.0
+    K.set_values(vals)
+    pc = capi.SchurPc(K, 1000000, precision)
+    with pytest.raises(capi.A2dsError) as e:
+        pc.factor()
+    assert e.value.code == 5  # A2DS_ERR_SINGULAR
+
+
+@pytest.mark.gpu
+def test_lanczos_budget_exhausted_returns_ritz_pairs():
+    """max_lanczos too small for the requested loads: A2DS_ERR_NOCONV, with
+    the current Ritz pairs still returned (finite, shift-side ordered)."""
+    f = np.load(os.path.join(GOLDEN, "cyl_q4_4x8_lu.npz"))
+    a = setup(f)
+    b = capi.LinearBuckling(a, float(f["sigma"]), max_lanczos=6, num_eigvals=5,
+                            eig_tol=1e-14, lev_fill=1000000, precision=64, block_size=1)
+    with pytest.raises(capi.A2dsError) as e:
+        b.solve(f["rhs"])
+    assert e.value.code == 6  # A2DS_ERR_NOCONV
+    assert np.all(np.isfinite(b.eigvals))
