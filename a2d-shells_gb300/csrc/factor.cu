@@ -31,13 +31,10 @@
 #include <type_traits>
 
 #include "a2ds_internal.h"
+#include "df64.h"
 #include "ilu.h"
 
 namespace a2ds {
-
-struct __align__(8) df64 {
-  float hi, lo;
-};
 
 // ------------------------------------------------------------ value types
 template <typename T>
@@ -71,33 +68,11 @@ __device__ __forceinline__ float from_f64<float>(double v) {
 }
 template <>
 __device__ __forceinline__ df64 from_f64<df64>(double v) {
-  const float h = __double2float_rn(v);
-  return df64{h, __double2float_rn(v - (double)h)};
+  return df_split(v);
 }
 __device__ __forceinline__ double from_c(double v, double *) { return v; }
 __device__ __forceinline__ float from_c(float v, float *) { return v; }
 __device__ __forceinline__ df64 from_c(double v, df64 *) { return from_f64<df64>(v); }
-
-// --------------------------------------------------------- df64 arithmetic
-// (hi, lo) -= a b: the FP32 product a.hi b.hi with its exact error (FMA),
-// cross terms in FP32, Knuth's two-sum for the leading parts, and the
-// low-order terms gathered in lo.  The _rn intrinsics keep the compiler from
-// fusing the two-sum's operations into FMAs, which would break its exactness.
-__device__ __forceinline__ void df_sub_prod(float &hi, float &lo, df64 a, df64 b) {
-  const float ph = __fmul_rn(a.hi, b.hi);
-  float pe = fmaf(a.hi, b.hi, -ph);
-  pe = fmaf(a.hi, b.lo, pe);
-  pe = fmaf(a.lo, b.hi, pe);
-  const float s = __fsub_rn(hi, ph);
-  const float bb = __fsub_rn(s, hi);
-  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(-ph, bb));
-  hi = s;
-  lo = __fadd_rn(lo, __fsub_rn(err, pe));
-}
-__device__ __forceinline__ df64 df_norm(float hi, float lo) {
-  const float s = __fadd_rn(hi, lo);
-  return df64{s, __fsub_rn(lo, __fsub_rn(s, hi))};
-}
 
 // ------------------------------------------------------- 6x6 block kernels
 // Entry e = 6 a + b of A B (L_ij = A_ij D_j^{-1}).
