@@ -90,8 +90,8 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
   pn = PanelSchedule();
   pn.level_panel.assign(nl, -1);
   {
-    // the tables hold at most PANEL_MAX_ROWS entries per U block of P; keep
-    // their offsets within int range
+    // the tables hold at most PANEL_MAX_ROWS entries per U block of P; their
+    // total stays below PANEL_TABLE_MAX (int32 offsets, bounded memory)
     long long tab_bound = 0;
     int l = 0;
     while (l < nl) {
@@ -107,7 +107,7 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
         rows += r;
         l1++;
       }
-      if (l1 - l >= 2 && tab_bound + PANEL_MAX_ROWS * ublocks < (1LL << 30)) {
+      if (l1 - l >= 2 && tab_bound + PANEL_MAX_ROWS * ublocks < PANEL_TABLE_MAX) {
         tab_bound += PANEL_MAX_ROWS * ublocks;
         for (int k = l; k < l1; k++) pn.level_panel[k] = (int)pn.l0.size();
         pn.l0.push_back(l);

@@ -112,6 +112,9 @@ constexpr int FACTOR_MAX_SPLIT = 8;
 // rows each, PANEL_MAX_ROWS rows in total.
 constexpr int PANEL_LEVEL_ROWS = 32;
 constexpr int PANEL_MAX_ROWS = 64;
+// upper bound on the panel tables' entries (a bound on host and device
+// memory, 1 GB of int32; runs of levels past it are factored level by level)
+constexpr long long PANEL_TABLE_MAX = 1LL << 28;
 // union U columns of a panel staged in shared memory by its phase-2 kernel
 constexpr int PANEL_UC_SMEM = 8192;
 
