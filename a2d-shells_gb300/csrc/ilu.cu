@@ -95,7 +95,7 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
     long long tab_bound = 0;
     int l = 0;
     while (l < nl) {
-      int l1 = l, rows = 0;
+      int l1 = l, rows = 0, minrow = n;
       long long ublocks = 0;
       while (l1 < nl) {
         const int r = f.flv.ptr[l1 + 1] - f.flv.ptr[l1];
@@ -103,12 +103,16 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
         for (int k = f.flv.ptr[l1]; k < f.flv.ptr[l1 + 1]; k++) {
           const int j = f.flv.rows[k];
           ublocks += f.frowp[j + 1] - f.fdiag[j] - 1;
+          minrow = std::min(minrow, j);
         }
         rows += r;
         l1++;
       }
-      if (l1 - l >= 2 && tab_bound + PANEL_MAX_ROWS * ublocks < PANEL_TABLE_MAX) {
-        tab_bound += PANEL_MAX_ROWS * ublocks;
+      // table entries: np x (union of P's U columns), the union bounded by
+      // the U blocks of P and by the columns after P's first row
+      const long long est = (long long)rows * std::min<long long>(ublocks, n - minrow);
+      if (l1 - l >= 2 && tab_bound + est < PANEL_TABLE_MAX) {
+        tab_bound += est;
         for (int k = l; k < l1; k++) pn.level_panel[k] = (int)pn.l0.size();
         pn.l0.push_back(l);
         pn.l1.push_back(l1);
