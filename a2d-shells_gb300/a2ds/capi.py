@@ -451,12 +451,13 @@ class LinearBuckling:
         return out
 
 
-A2DS_F5_CONNECTIVITY, A2DS_F5_NODES, A2DS_F5_DISPLACEMENTS = 1, 2, 4
+A2DS_F5_CONNECTIVITY, A2DS_F5_NODES, A2DS_F5_DISPLACEMENTS, A2DS_F5_LOADS = 1, 2, 4, 64
 
 
 class ToFH5:
     """TACSToFH5 for shell meshes (src/io/TACSToFH5.h): the connectivity,
-    node and displacement output classes written as a .f5 file."""
+    node, displacement and load output classes written as a .f5 file (loads
+    need an initialized Assembler)."""
 
     def __init__(self, assembler: "Assembler",
                  write_flag=A2DS_F5_CONNECTIVITY | A2DS_F5_NODES | A2DS_F5_DISPLACEMENTS,

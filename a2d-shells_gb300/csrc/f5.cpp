@@ -1,7 +1,7 @@
 // .f5 output: the binary layout TACSToFH5::writeToFile writes through
 // TACSFH5File (src/io/TACSToFH5.cpp:126-358, src/io/TACSFH5.cpp:64-210) for
-// one process, restricted to the connectivity, node and displacement
-// classes (TACS_OUTPUT_CONNECTIVITY | NODES | DISPLACEMENTS).
+// one process, for the connectivity, node, displacement and load classes
+// (TACS_OUTPUT_CONNECTIVITY | NODES | DISPLACEMENTS | LOADS).
 //
 // File = header + zones, native byte order.
 //   header: int num_components; per component: int length (with the NUL),
@@ -12,8 +12,10 @@
 // Zones, in order: with CONNECTIVITY "components" (component of each
 // element), "ltypes" (element layout: 8 = Quad4, 9 = Quad9), "ptr"
 // (num_elements + 1 offsets), "connectivity"; with NODES and/or
-// DISPLACEMENTS one float zone "continuous data t=<time %.10e>" with
-// variables "X,Y,Z" then "u,v,w,rotx,roty,rotz", one row per node.
+// DISPLACEMENTS and/or LOADS one float zone "continuous data t=<time %.10e>"
+// with variables "X,Y,Z", then "u,v,w,rotx,roty,rotz", then
+// "fx,fy,fz,mx,my,mz" (the residual at vars without external loads,
+// assembleRes(F, 0.0), which needs an initialized mesh), one row per node.
 #include <stdio.h>
 #include <string.h>
 
@@ -63,9 +65,11 @@ extern "C" int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_fl
   try {
     using a2ds::fail;
     if (!mesh || !file_name) return fail(A2DS_ERR_ARG, "mesh and file_name are required");
-    const int allowed = A2DS_F5_CONNECTIVITY | A2DS_F5_NODES | A2DS_F5_DISPLACEMENTS;
+    const int allowed =
+        A2DS_F5_CONNECTIVITY | A2DS_F5_NODES | A2DS_F5_DISPLACEMENTS | A2DS_F5_LOADS;
     if (write_flag & ~allowed)
-      return fail(A2DS_ERR_ARG, "write_flag: only connectivity, nodes and displacements");
+      return fail(A2DS_ERR_ARG,
+                  "write_flag: only connectivity, nodes, displacements and loads");
     const a2ds::Mesh &m = mesh->m;
     const int ne = m.ne, nn = m.nn, npe = m.npe;
     int maxc = 0;
@@ -96,10 +100,21 @@ extern "C" int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_fl
       put_zone(b, kF5Int, "connectivity", "connectivity", ne * npe, 1, m.conn.data());
     }
     const bool nodes = write_flag & A2DS_F5_NODES, disp = write_flag & A2DS_F5_DISPLACEMENTS;
-    if (nodes || disp) {
+    const bool loads = write_flag & A2DS_F5_LOADS;
+    std::vector<double> res;
+    if (loads) {  // assembleRes(F, 0.0) at vars: internal forces, BC rows as the reference
+      res.resize((size_t)nn * 6);
+      std::vector<double> zero;
+      if (!vars) zero.assign((size_t)nn * 6, 0.0);
+      const int rc = a2ds_assemble_res(mesh, vars ? vars : zero.data(), res.data());
+      if (rc) return rc;
+    }
+    if (nodes || disp || loads) {
       std::string names = nodes ? "X,Y,Z" : "";
       if (disp) names += std::string(nodes ? "," : "") + "u,v,w,rotx,roty,rotz";
-      const int dim2 = (nodes ? 3 : 0) + (disp ? 6 : 0), off = nodes ? 3 : 0;
+      if (loads) names += std::string(nodes || disp ? "," : "") + "fx,fy,fz,mx,my,mz";
+      const int dim2 = (nodes ? 3 : 0) + (disp ? 6 : 0) + (loads ? 6 : 0);
+      const int off = nodes ? 3 : 0, loff = off + (disp ? 6 : 0);
       std::vector<float> v((size_t)nn * dim2, 0.0f);
       for (int i = 0; i < nn; i++) {
         if (nodes)
@@ -107,6 +122,8 @@ extern "C" int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_fl
         if (disp)
           for (int j = 0; j < 6; j++)
             v[(size_t)i * dim2 + off + j] = vars ? (float)vars[(size_t)i * 6 + j] : 0.0f;
+        if (loads)
+          for (int j = 0; j < 6; j++) v[(size_t)i * dim2 + loff + j] = (float)res[(size_t)i * 6 + j];
       }
       char zone[128];
       snprintf(zone, sizeof(zone), "continuous data t=%.10e", time);

@@ -328,10 +328,12 @@ int a2ds_bdf_get_component_descript(a2ds_bdf bdf, int comp, char *descript, int 
    Replaces: TACSToFH5(assembler, TACS_BEAM_OR_SHELL_ELEMENT, write_flag)
    with setComponentName and writeToFile (src/io/TACSToFH5.cpp:35-358;
    file layout of TACSFH5File, src/io/TACSFH5.cpp:64-210) on one process,
-   for the connectivity, node and displacement output classes: the same
-   bytes as the reference for the same mesh, names and variables.
-   write_flag: A2DS_F5_* bits (strain, stress, extra and load output
-   classes are not written: A2DS_ERR_ARG).  component_names: NULL or
+   for the connectivity, node, displacement and load output classes: the
+   same layout as the reference for the same mesh, names and variables.
+   write_flag: A2DS_F5_* bits (the element output classes, strains,
+   stresses and extras, are not written: A2DS_ERR_ARG).  Loads are the
+   residual at vars without external loads (assembleRes(F, 0.0)), so they
+   need an initialized mesh and a GPU.  component_names: NULL or
    num_components entries (NULL entries give "Component k");
    num_components is raised to 1 + the largest elem_component value;
    elem_component: NULL (all 0) or num_elements values; vars: NULL (zeros)
@@ -340,6 +342,7 @@ int a2ds_bdf_get_component_descript(a2ds_bdf bdf, int comp, char *descript, int 
 #define A2DS_F5_CONNECTIVITY 1
 #define A2DS_F5_NODES 2
 #define A2DS_F5_DISPLACEMENTS 4
+#define A2DS_F5_LOADS 64
 int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_flag, int num_components,
                   const char *const *component_names, const int *elem_component,
                   const double *vars, double time);
