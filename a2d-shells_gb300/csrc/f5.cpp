@@ -78,12 +78,14 @@ extern "C" int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_fl
         if (elem_component[e] < 0) return fail(A2DS_ERR_ARG, "negative component number");
         maxc = std::max(maxc, elem_component[e]);
       }
-    // TACSAssembler::getNumComponents: largest component number + 1
+    // TACSAssembler::getNumComponents: largest component number + 1 (the
+    // caller's names cover its own num_components entries only)
+    const int given = component_names ? std::max(num_components, 0) : 0;
     if (num_components < maxc + 1) num_components = maxc + 1;
     std::vector<char> b;
     put_int(b, num_components);
     for (int k = 0; k < num_components; k++) {
-      std::string name = (component_names && component_names[k])
+      std::string name = (k < given && component_names[k])
                              ? std::string(component_names[k])
                              : "Component " + std::to_string(k);
       put_int(b, (int)name.size() + 1);
