@@ -41,7 +41,8 @@ ERRORS = {1: "A2DS_ERR_ARG", 2: "A2DS_ERR_STATE", 3: "A2DS_ERR_CUDA", 4: "A2DS_E
 # Every entry point of include/a2ds.h
 EXPORTS = [
     "a2ds_last_error", "a2ds_device_count", "a2ds_mesh_create", "a2ds_mesh_destroy",
-    "a2ds_mesh_set_material", "a2ds_mesh_set_thickness", "a2ds_mesh_add_bcs",
+    "a2ds_mesh_set_material", "a2ds_mesh_set_yield_stress", "a2ds_mesh_set_thickness",
+    "a2ds_mesh_add_bcs",
     "a2ds_mesh_plan", "a2ds_mesh_get_pattern", "a2ds_mesh_ilu_pattern",
     "a2ds_mesh_initialize", "a2ds_mesh_get_ordering", "a2ds_mesh_node_csr",
     "a2ds_bcsr_create", "a2ds_bcsr_destroy", "a2ds_bcsr_get", "a2ds_bcsr_set_values",
@@ -99,6 +100,7 @@ def load(build: bool = False):
     lib.a2ds_mesh_set_material.argtypes = [VP, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double]
     lib.a2ds_mesh_set_thickness.argtypes = [VP, ctypes.c_int, P_D, P_I]
+    lib.a2ds_mesh_set_yield_stress.argtypes = [VP, ctypes.c_double]
     lib.a2ds_mesh_add_bcs.argtypes = [VP, ctypes.c_int, P_I, P_I, P_D]
     lib.a2ds_mesh_initialize.argtypes = [VP, ctypes.c_int]
     lib.a2ds_mesh_plan.argtypes = [VP, ctypes.c_int]
@@ -194,6 +196,10 @@ class Assembler:
 
     def set_material(self, E, nu, alpha=0.0, temperature=0.0):
         _check(self.lib.a2ds_mesh_set_material(self.h, E, nu, alpha, temperature))
+
+    def set_yield_stress(self, ys):
+        """ys of TACSMaterialProperties (failure values of the .f5 extras)."""
+        _check(self.lib.a2ds_mesh_set_yield_stress(self.h, float(ys)))
 
     def set_thickness(self, t, elem_group=None):
         t = _f64(np.atleast_1d(t))
@@ -451,13 +457,15 @@ class LinearBuckling:
         return out
 
 
-A2DS_F5_CONNECTIVITY, A2DS_F5_NODES, A2DS_F5_DISPLACEMENTS, A2DS_F5_LOADS = 1, 2, 4, 64
+A2DS_F5_CONNECTIVITY, A2DS_F5_NODES, A2DS_F5_DISPLACEMENTS = 1, 2, 4
+A2DS_F5_STRAINS, A2DS_F5_STRESSES, A2DS_F5_EXTRAS, A2DS_F5_LOADS = 8, 16, 32, 64
 
 
 class ToFH5:
-    """TACSToFH5 for shell meshes (src/io/TACSToFH5.h): the connectivity,
-    node, displacement and load output classes written as a .f5 file (loads
-    need an initialized Assembler)."""
+    """TACSToFH5 for shell meshes (src/io/TACSToFH5.h): every output class
+    (connectivity, nodes, displacements, strains, stresses, extras, loads)
+    written as a .f5 file; loads and the element classes need an
+    initialized Assembler, extras its yield stress."""
 
     def __init__(self, assembler: "Assembler",
                  write_flag=A2DS_F5_CONNECTIVITY | A2DS_F5_NODES | A2DS_F5_DISPLACEMENTS,

@@ -66,7 +66,9 @@ struct DBuf {
 };
 
 // --------------------------------------------------------- element kernel
-enum ElemMode { MODE_K = 0, MODE_G = 1, MODE_R = 2, MODE_KR = 3 };
+// MODE_OUT: strain and stress of the state at each element's node points
+// (TACSShellElement::getOutputData), written to out (element-major).
+enum ElemMode { MODE_K = 0, MODE_G = 1, MODE_R = 2, MODE_KR = 3, MODE_OUT = 4 };
 
 struct ElemLaunch {
   int order;             // 2 or 3
@@ -92,6 +94,8 @@ struct ElemLaunch {
   const double *cx, *cy;
   double *cout;
   double ccoef;
+  // MODE_OUT: Ne x NN x 18 (strain e[9], stress C e[9] per node point)
+  double *out;
 };
 
 int launch_element_kernel(const ElemLaunch &L, cudaStream_t s);

@@ -94,6 +94,14 @@ int a2ds_mesh_set_material(a2ds_mesh mesh, double E, double nu, double alpha, do
   return 0;
 }
 
+int a2ds_mesh_set_yield_stress(a2ds_mesh mesh, double ys) {
+  int rc = check_mesh(mesh, false);
+  if (rc) return rc;
+  if (!(ys > 0.0)) return fail(A2DS_ERR_ARG, "yield stress must be positive");
+  mesh->m.ys = ys;
+  return 0;
+}
+
 int a2ds_mesh_set_thickness(a2ds_mesh mesh, int num_groups, const double *t, const int *elem_group) {
   A2DS_GUARD_BEGIN
   int rc = check_mesh(mesh, false);

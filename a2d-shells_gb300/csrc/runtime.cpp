@@ -194,6 +194,15 @@ ElemLaunch Mesh::launch_params(int mode, const double *d_st, double *vals, doubl
   return L;
 }
 
+int Mesh::element_output(const double *d_st, double *d_out) {
+  ElemLaunch L = launch_params(MODE_OUT, d_st, nullptr, nullptr);
+  L.out = d_out;
+  int rc;
+  if ((rc = launch_element_kernel(L, stream))) return rc;
+  launches++;
+  return 0;
+}
+
 // Element assembly into vals (zeroed first) and/or res, device state
 int Mesh::assemble_device(int mode, const double *d_st, double *vals, double *res, int scatter) {
   int rc;

@@ -16,6 +16,7 @@ struct Mesh {
   std::vector<int> conn;    // ne x npe, caller's node numbering
   std::vector<double> X;    // nn x 3
   double E = 70e9, nu = 0.3, alpha = 0.0, temperature = 0.0;
+  double ys = 0.0;  // yield stress for the failure output (0: not set)
   std::vector<double> tvals{1e-2};
   std::vector<int> tgroup;  // ne
   std::vector<int> bc_nodes, bc_masks;
@@ -48,6 +49,9 @@ struct Mesh {
   int from_rows(const double *d, double *h);
   ElemLaunch launch_params(int mode, const double *d_st, double *vals, double *res) const;
   int assemble_device(int mode, const double *d_st, double *vals, double *res, int scatter);
+  // strain and stress at every element's node points (MODE_OUT), d_out
+  // ne x npe x 18 on the device
+  int element_output(const double *d_st, double *d_out);
   ~Mesh();
 };
 

@@ -54,6 +54,9 @@ struct ShellTables {
   double nNa[9][9], nNb[9][9];            // [node point][node]
 };
 __constant__ ShellTables c_tab[2];
+// The same tables with the node points in place of the Gauss points (element
+// output at the visualization nodes, basis::getNodePoint order).
+__constant__ ShellTables c_tab_vis[2];
 
 enum { F11 = 0, F22 = 1, F12 = 2, F23 = 3, F13 = 4 };
 
@@ -91,7 +94,7 @@ static void h_shape(int o, const double pt[2], double *N, double *Na, double *Nb
     }
 }
 
-static void build_tables(int o, ShellTables *T) {
+static void build_tables(int o, ShellTables *T, bool at_nodes) {
   static const double gp2[2] = {-0.577350269189626, 0.577350269189626};
   static const double gp3[3] = {-0.774596669241483, 0.0, 0.774596669241483};
   static const double gw3[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
@@ -100,7 +103,11 @@ static void build_tables(int o, ShellTables *T) {
   const int nn = o * o;
   for (int g = 0; g < nn; g++) {
     double pt[2];
-    if (o == 2) {
+    if (at_nodes) {
+      pt[0] = -1.0 + (2.0 / (o - 1)) * (g % o);
+      pt[1] = -1.0 + (2.0 / (o - 1)) * (g / o);
+      T->gw[g] = 1.0;
+    } else if (o == 2) {
       pt[0] = gp2[g % 2];
       pt[1] = gp2[g / 2];
       T->gw[g] = 1.0;
@@ -158,10 +165,13 @@ static void build_tables(int o, ShellTables *T) {
 }
 
 int upload_shell_tables() {
-  static ShellTables tabs[2];
-  build_tables(2, &tabs[0]);
-  build_tables(3, &tabs[1]);
+  static ShellTables tabs[2], vis[2];
+  build_tables(2, &tabs[0], false);
+  build_tables(3, &tabs[1], false);
+  build_tables(2, &vis[0], true);
+  build_tables(3, &vis[1], true);
   A2DS_CUDA_TRY(cudaMemcpyToSymbol(c_tab, tabs, sizeof(tabs)));
+  A2DS_CUDA_TRY(cudaMemcpyToSymbol(c_tab_vis, vis, sizeof(vis)));
   return 0;
 }
 
@@ -344,7 +354,7 @@ template <int O, int MODE, int NL>
 __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
   using D = Dims<O>;
   constexpr int NN = D::NN, NV = D::NV, NTY = D::NTY, NGP = D::NGP, TPE = D::TPE;
-  const ShellTables &tb = c_tab[O - 2];
+  const ShellTables &tb = (MODE == MODE_OUT) ? c_tab_vis[O - 2] : c_tab[O - 2];
   extern __shared__ double smem_raw[];
   const int eslot = threadIdx.x / TPE;
   const int tid = threadIdx.x % TPE;
@@ -358,10 +368,12 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
   const int *conn = L.conn + (size_t)e * NN;
 
   // Variants that need the state (nonlinear tangent, G direction, residual)
-  constexpr bool NEED_STATE = (MODE == MODE_G) || (MODE == MODE_R) || (MODE == MODE_KR) || NL;
+  constexpr bool OUT = (MODE == MODE_OUT);
+  constexpr bool NEED_STATE = (MODE == MODE_G) || (MODE == MODE_R) || (MODE == MODE_KR) || NL || OUT;
   constexpr bool NEED_P = (MODE == MODE_G) || NL;  // bilinear-form terms present
-  constexpr bool NEED_STRESS = (MODE == MODE_G) || (MODE == MODE_R) || (MODE == MODE_KR) || NL;
-  constexpr bool NEED_MAT = (MODE != MODE_R);
+  constexpr bool NEED_STRESS =
+      (MODE == MODE_G) || (MODE == MODE_R) || (MODE == MODE_KR) || NL || OUT;
+  constexpr bool NEED_MAT = (MODE != MODE_R) && !OUT;
   constexpr bool NEED_RES = (MODE == MODE_R) || (MODE == MODE_KR);
 
   // ---- gather
@@ -687,6 +699,22 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
         S.e[tid] = v;
       }
       esync<O>();
+      if (OUT) {
+        // output at node point g: the strain and C e (evalStress of the
+        // total strain, as getOutputData)
+        if (tid == 0 && active && L.out) {
+          double em[9], s[9];
+          for (int i = 0; i < 9; i++) em[i] = S.e[i];
+          d_stress(C, em, s);
+          double *o = L.out + ((size_t)e * NN + g) * 18;
+          for (int i = 0; i < 9; i++) {
+            o[i] = em[i];
+            o[9 + i] = s[i];
+          }
+        }
+        esync<O>();
+        continue;  // nothing else at this point (uniform over the element)
+      }
       if (tid == 0) {
         double em[9];
         for (int i = 0; i < 9; i++) em[i] = S.e[i];
@@ -911,6 +939,7 @@ static int launch_order(const ElemLaunch &L, cudaStream_t s) {
     case MODE_G: return launch_one<O, MODE_G, 0>(L, s);
     case MODE_R: return nl ? launch_one<O, MODE_R, 1>(L, s) : launch_one<O, MODE_R, 0>(L, s);
     case MODE_KR: return nl ? launch_one<O, MODE_KR, 1>(L, s) : launch_one<O, MODE_KR, 0>(L, s);
+    case MODE_OUT: return nl ? launch_one<O, MODE_OUT, 1>(L, s) : launch_one<O, MODE_OUT, 0>(L, s);
   }
   return fail(A2DS_ERR_ARG, "unknown element kernel mode");
 }

@@ -87,6 +87,11 @@ int a2ds_mesh_destroy(a2ds_mesh mesh);
 int a2ds_mesh_set_material(a2ds_mesh mesh, double E, double nu, double alpha,
                            double temperature);
 
+/* Yield stress of the material (the ys argument of TACSMaterialProperties,
+   src/constitutive/TACSMaterialProperties.h); used only by the failure
+   values of the .f5 element output. */
+int a2ds_mesh_set_yield_stress(a2ds_mesh mesh, double ys);
+
 /* Thickness design variables: one TACSIsoShellConstitutive per group
    (src/constitutive/TACSIsoShellConstitutive.cpp:28-43, design variable
    tNum); elem_group[e] in [0, num_groups).  Default: one group, t = 1e-2. */
@@ -329,11 +334,14 @@ int a2ds_bdf_get_component_descript(a2ds_bdf bdf, int comp, char *descript, int 
    with setComponentName and writeToFile (src/io/TACSToFH5.cpp:35-358;
    file layout of TACSFH5File, src/io/TACSFH5.cpp:64-210) on one process,
    for the connectivity, node, displacement and load output classes: the
-   same layout as the reference for the same mesh, names and variables.
-   write_flag: A2DS_F5_* bits (the element output classes, strains,
-   stresses and extras, are not written: A2DS_ERR_ARG).  Loads are the
-   residual at vars without external loads (assembleRes(F, 0.0)), so they
-   need an initialized mesh and a GPU.  component_names: NULL or
+   same layout as the reference for the same mesh, names and variables,
+   and the element output classes.
+   write_flag: A2DS_F5_* bits.  Loads are the residual at vars without
+   external loads (assembleRes(F, 0.0)); the element classes (strains,
+   stresses, extras: failure0-5 and dv1-7 as getOutputData) are evaluated
+   at every element's node points on the GPU (an "element data" zone).
+   Both need an initialized mesh and a GPU; extras need
+   a2ds_mesh_set_yield_stress.  component_names: NULL or
    num_components entries (NULL entries give "Component k");
    num_components is raised to 1 + the largest elem_component value;
    elem_component: NULL (all 0) or num_elements values; vars: NULL (zeros)
@@ -342,6 +350,9 @@ int a2ds_bdf_get_component_descript(a2ds_bdf bdf, int comp, char *descript, int 
 #define A2DS_F5_CONNECTIVITY 1
 #define A2DS_F5_NODES 2
 #define A2DS_F5_DISPLACEMENTS 4
+#define A2DS_F5_STRAINS 8
+#define A2DS_F5_STRESSES 16
+#define A2DS_F5_EXTRAS 32
 #define A2DS_F5_LOADS 64
 int a2ds_write_f5(a2ds_mesh mesh, const char *file_name, int write_flag, int num_components,
                   const char *const *component_names, const int *elem_component,

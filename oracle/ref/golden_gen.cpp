@@ -542,7 +542,7 @@ static void run_bdf(const std::string &file, const std::string &out) {
 
 // TACSToFH5::writeToFile (src/io/TACSToFH5.cpp:126) for a shell mesh with
 // per-element components, named components 0 and 1, the given variables
-// and each of six output-class flags: in/X, conn, comp, vars ->
+// and each of nine output-class flags: in/X, conn, comp, vars ->
 // out/f5_<flag>.f5.
 static void run_f5(const std::string &in, const std::string &out) {
   std::vector<long> xs, cs;
@@ -586,12 +586,16 @@ static void run_f5(const std::string &in, const std::string &out) {
   q->getArray(&qa);
   for (int i = 0; i < 6 * nn; i++) qa[i] = vars[i];
   assembler->setVariables(q);
-  const int flags[6] = {TACS_OUTPUT_CONNECTIVITY | TACS_OUTPUT_NODES | TACS_OUTPUT_DISPLACEMENTS,
+  const int all = TACS_OUTPUT_CONNECTIVITY | TACS_OUTPUT_NODES | TACS_OUTPUT_DISPLACEMENTS |
+                  TACS_OUTPUT_STRAINS | TACS_OUTPUT_STRESSES | TACS_OUTPUT_EXTRAS |
+                  TACS_OUTPUT_LOADS;
+  const int flags[9] = {TACS_OUTPUT_CONNECTIVITY | TACS_OUTPUT_NODES | TACS_OUTPUT_DISPLACEMENTS,
                         TACS_OUTPUT_NODES, TACS_OUTPUT_DISPLACEMENTS, TACS_OUTPUT_CONNECTIVITY,
                         TACS_OUTPUT_LOADS,
                         TACS_OUTPUT_CONNECTIVITY | TACS_OUTPUT_NODES | TACS_OUTPUT_DISPLACEMENTS |
-                            TACS_OUTPUT_LOADS};
-  for (int f = 0; f < 6; f++) {
+                            TACS_OUTPUT_LOADS,
+                        TACS_OUTPUT_STRAINS | TACS_OUTPUT_STRESSES, TACS_OUTPUT_EXTRAS, all};
+  for (int f = 0; f < 9; f++) {
     TACSToFH5 *f5 = new TACSToFH5(assembler, TACS_BEAM_OR_SHELL_ELEMENT, flags[f]);
     f5->incref();
     f5->setComponentName(0, "skin");

@@ -15,7 +15,7 @@ builds) and packs inputs and outputs into small .npz files:
   bdf_*.bdf, bdf.npz    synthetic Nastran decks (bdf_cases.py) and the
                         reference loader's arrays for each
   f5.npz                .f5 files of the reference's TACSToFH5 (raw bytes)
-                        for two seeded meshes and six output-class flags
+                        for two seeded meshes and nine output-class flags
 
 Only this container has the reference sources; the fixtures are committed so
 the tests never need them.  Run:  python tests/golden/make_golden.py
@@ -235,9 +235,9 @@ def make_bdf():
 
 def make_f5():
     """.f5 files written by the reference's TACSToFH5 for a Quad4 and a Quad9
-    cylinder with two components and a seeded variable vector, for six
-    output-class flags (with and without loads); stored as raw bytes in
-    f5.npz with the inputs."""
+    cylinder with two components and a seeded variable vector, for nine
+    output-class flags (node, element and load classes); stored as raw
+    bytes in f5.npz with the inputs."""
     rng = np.random.default_rng(11)
     out = {}
     for name, m in {"q4": meshgen.cylinder(4, 8, order=2),

@@ -2,8 +2,8 @@
 TACSFH5File) against files the reference itself wrote (tests/golden/f5.npz,
 oracle/ref/golden_gen.cpp f5 mode): byte-identical for a Quad4 and a Quad9
 mesh with two named components, for the connectivity, node and
-displacement output classes alone and together (CPU); with the load class
-(the residual assembled on the GPU) the layout is byte-identical and the
+displacement output classes alone and together (CPU); with the load and
+element classes (computed on the GPU) the layout is byte-identical and the
 values agree to FP32 rounding (GPU)."""
 import os
 
@@ -49,12 +49,17 @@ def f5_zones(b):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("mesh", ["q4", "q9"])
-@pytest.mark.parametrize("flag", [capi.A2DS_F5_LOADS, 71])
-def test_f5_loads_match_reference(mesh, flag, tmp_path):
+@pytest.mark.parametrize("flag", [capi.A2DS_F5_LOADS, 71, capi.A2DS_F5_STRAINS | capi.A2DS_F5_STRESSES,
+                                  capi.A2DS_F5_EXTRAS, 127])
+def test_f5_gpu_classes_match_reference(mesh, flag, tmp_path):
+    """Loads (the GPU residual) and the element classes (strains, stresses
+    and extras at every element node point, from the GPU element kernel):
+    layout byte-identical, values to FP32 rounding of the reference's."""
     g = np.load(os.path.join(GOLDEN, "f5.npz"))
     a = capi.Assembler(g[f"{mesh}__X"], g[f"{mesh}__conn"])
     a.set_material(70e9, 0.3)
     a.set_thickness([1e-2])
+    a.set_yield_stress(270e6)
     a.initialize()
     out = capi.ToFH5(a, flag, elem_component=g[f"{mesh}__comp"])
     out.set_component_name(0, "skin")
@@ -70,12 +75,22 @@ def test_f5_loads_match_reference(mesh, flag, tmp_path):
         else:
             vo = np.frombuffer(zo[1], np.float32).astype(np.float64)
             vr = np.frombuffer(zr[1], np.float32).astype(np.float64)
-            assert np.abs(vo - vr).max() <= 1e-6 * np.abs(vr).max()
+            # per column: FP32 rounding of values computed in a different
+            # order (the columns span strains, stresses and failure values)
+            d2 = zo[4]
+            vo, vr = vo.reshape(-1, d2), vr.reshape(-1, d2)
+            scale = np.maximum(np.abs(vr).max(axis=0), 1e-30)
+            assert np.all(np.abs(vo - vr).max(axis=0) <= 1e-5 * scale), (
+                np.abs(vo - vr).max(axis=0) / scale)
 
 
-def test_f5_rejects_element_output_classes(tmp_path):
+def test_f5_argument_errors(tmp_path):
     g = np.load(os.path.join(GOLDEN, "f5.npz"))
     a = capi.Assembler(g["q4__X"], g["q4__conn"])
-    strains = 8  # TACS_OUTPUT_STRAINS: element output classes are not written
-    with pytest.raises(capi.A2dsError):
-        capi.ToFH5(a, capi.A2DS_F5_NODES | strains).write_to_file(str(tmp_path / "x.f5"))
+    with pytest.raises(capi.A2dsError):  # an unknown output class bit
+        capi.ToFH5(a, capi.A2DS_F5_NODES | 128).write_to_file(str(tmp_path / "x.f5"))
+    with pytest.raises(capi.A2dsError):  # failure values without a yield stress
+        capi.ToFH5(a, capi.A2DS_F5_EXTRAS).write_to_file(str(tmp_path / "x.f5"))
+    with pytest.raises(capi.A2dsError):  # element classes before initialize()
+        a.set_yield_stress(270e6)
+        capi.ToFH5(a, capi.A2DS_F5_STRAINS).write_to_file(str(tmp_path / "x.f5"))
