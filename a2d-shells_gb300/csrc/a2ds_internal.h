@@ -65,6 +65,35 @@ struct DBuf {
   }
 };
 
+// Page-locked host staging buffer (grown on demand): host<->device copies at
+// the C ABI run from pinned memory at full link rate.
+template <typename T>
+struct PinnedBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf &) = delete;
+  PinnedBuf &operator=(const PinnedBuf &) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  int reserve(size_t count) {
+    if (p && count <= n) return 0;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost((void **)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(A2DS_ERR_NOMEM, std::string("cudaMallocHost of ") +
+                                      std::to_string(count * sizeof(T)) + " bytes: " +
+                                      cudaGetErrorString(e));
+    }
+    n = count;
+    return 0;
+  }
+};
+
 // --------------------------------------------------------- element kernel
 // MODE_OUT: strain and stress of the state at each element's node points
 // (TACSShellElement::getOutputData), written to out (element-major).

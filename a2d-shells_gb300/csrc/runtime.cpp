@@ -146,27 +146,30 @@ int Mesh::upload() {
 
 // Node-ordered host vector -> row-ordered device vector
 int Mesh::to_rows(const double *h, DBuf<double> &d) {
-  int rc = d.alloc((size_t)nn * 6);
+  const size_t n6 = (size_t)nn * 6;
+  int rc = d.alloc(n6);
   if (rc) return rc;
-  h_tmp.resize((size_t)nn * 6);
+  if ((rc = h_stage.reserve(n6))) return rc;
+  double *st = h_stage.p;
   if (h) {
-    for (int i = 0; i < nn; i++) memcpy(&h_tmp[(size_t)i * 6], &h[(size_t)perm[i] * 6], 6 * sizeof(double));
+    for (int i = 0; i < nn; i++) memcpy(&st[(size_t)i * 6], &h[(size_t)perm[i] * 6], 6 * sizeof(double));
   } else {
-    std::fill(h_tmp.begin(), h_tmp.end(), 0.0);
+    std::fill(st, st + n6, 0.0);
   }
-  A2DS_CUDA_TRY(cudaMemcpyAsync(d.p, h_tmp.data(), h_tmp.size() * sizeof(double),
-                                cudaMemcpyHostToDevice, stream));
+  A2DS_CUDA_TRY(cudaMemcpyAsync(d.p, st, n6 * sizeof(double), cudaMemcpyHostToDevice, stream));
   A2DS_CUDA_TRY(cudaStreamSynchronize(stream));
   return 0;
 }
 
 // Row-ordered device vector -> node-ordered host vector
 int Mesh::from_rows(const double *d, double *h) {
-  h_tmp.resize((size_t)nn * 6);
-  A2DS_CUDA_TRY(cudaMemcpyAsync(h_tmp.data(), d, h_tmp.size() * sizeof(double),
-                                cudaMemcpyDeviceToHost, stream));
+  const size_t n6 = (size_t)nn * 6;
+  int rc;
+  if ((rc = h_stage.reserve(n6))) return rc;
+  double *st = h_stage.p;
+  A2DS_CUDA_TRY(cudaMemcpyAsync(st, d, n6 * sizeof(double), cudaMemcpyDeviceToHost, stream));
   A2DS_CUDA_TRY(cudaStreamSynchronize(stream));
-  for (int i = 0; i < nn; i++) memcpy(&h[(size_t)perm[i] * 6], &h_tmp[(size_t)i * 6], 6 * sizeof(double));
+  for (int i = 0; i < nn; i++) memcpy(&h[(size_t)perm[i] * 6], &st[(size_t)i * 6], 6 * sizeof(double));
   return 0;
 }
 

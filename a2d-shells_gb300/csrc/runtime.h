@@ -36,7 +36,7 @@ struct Mesh {
   cudaStream_t stream = nullptr;
   DBuf<double> d_X, d_tvals, d_state, d_res;
   DBuf<int> d_conn, d_slots, d_rowp, d_cols, d_tgroup, d_bc_rows, d_bc_masks, d_color_elems;
-  std::vector<double> h_tmp;
+  PinnedBuf<double> h_stage;  // pinned staging of node <-> row permuted vectors
   long long launches = 0;
 
   // buckling-solve state kept for sensitivities / stats

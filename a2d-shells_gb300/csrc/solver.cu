@@ -1137,7 +1137,9 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   ta = now();
   if ((rc = m.assemble_device(MODE_R, nullptr, nullptr, S.r.p, A2DS_SCATTER_ATOMIC))) return rc;
   {
-    std::vector<double> h((size_t)m.nn * 6, 0.0);
+    if ((rc = m.h_stage.reserve(n6))) return rc;
+    double *h = m.h_stage.p;  // pinned staging
+    std::fill(h, h + n6, 0.0);
     if (rhs) {
       for (int i = 0; i < m.nn; i++)
         for (int k = 0; k < 6; k++) h[(size_t)i * 6 + k] = rhs[(size_t)m.perm[i] * 6 + k];
@@ -1146,13 +1148,13 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
       for (int k = 0; k < 6; k++)
         if (m.bc_masks[b] & (1 << k)) h[(size_t)m.bc_rows[b] * 6 + k] = m.bc_vals[b * 6 + k];
     // rhs' = f with BC rows replaced by the BC values; res = R(0) - rhs'
-    A2DS_CUDA_TRY(cudaMemcpyAsync(S.rhs.p, h.data(), n6 * sizeof(double), cudaMemcpyHostToDevice,
+    A2DS_CUDA_TRY(cudaMemcpyAsync(S.rhs.p, h, n6 * sizeof(double), cudaMemcpyHostToDevice,
                                   m.stream));
     k_zero_bc<<<((int)m.bc_rows.size() * 6 + 255) / 256 + 1, 256, 0, m.stream>>>(
         S.r.p, m.d_bc_rows.p, m.d_bc_masks.p, (int)m.bc_rows.size());
     m.launches++;
     B.axpby(S.rhs.p, -1.0, S.r.p, 1.0, n6);  // rhs = rhs - R(0): K path = rhs
-    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // h is pageable and goes out of scope
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // the staging buffer is reused next
   }
   int inner = 0;
   // complete factors: direct solves with FP64 refinement; incomplete (ILU(k))

@@ -14,7 +14,8 @@ assemble K, load path, assemble G, factor, Lanczos, eigenpairs) through the
 C ABI call a2ds_buckling_solve:
   value  -- mesh resident on the device, eigenvalues returned to the host;
   e2e    -- the same call with host load vector in and host eigenvectors and
-            load path out (the copies inside the timed region).
+            load path out (the copies inside the timed region, staged by the
+            library through page-locked host buffers).
 Device time comes from CUDA events recorded by the library on its own
 stream around each solve.  The shift sigma is 0.95 x the lowest load found
 by a cheap first solve at 0.35 x the classical load (untimed setup).
