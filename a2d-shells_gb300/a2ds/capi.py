@@ -47,6 +47,7 @@ EXPORTS = [
     "a2ds_mesh_initialize", "a2ds_mesh_get_ordering", "a2ds_mesh_node_csr",
     "a2ds_bcsr_create", "a2ds_bcsr_destroy", "a2ds_bcsr_get", "a2ds_bcsr_set_values",
     "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
+    "a2ds_add_mat_xpt_sens_inner_product", "a2ds_eig_sens_xpts",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
     "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
@@ -137,6 +138,9 @@ def load(build: bool = False):
     lib.a2ds_eigen_shift_invert.argtypes = [VP, ctypes.POINTER(BucklingOpts), VP, VP, P_D, P_D,
                                             P_D]
     lib.a2ds_eig_sens_thickness.argtypes = [VP, ctypes.c_int, P_D]
+    lib.a2ds_eig_sens_xpts.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
+    lib.a2ds_add_mat_xpt_sens_inner_product.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D,
+                                                        P_D, P_D, ctypes.c_double, P_D]
     lib.a2ds_bdf_scan.argtypes = [ctypes.c_char_p, ctypes.POINTER(VP)]
     lib.a2ds_bdf_destroy.argtypes = [VP]
     lib.a2ds_bdf_get_sizes.argtypes = [VP, P_I, P_I, P_I, P_I, P_I, P_I]
@@ -265,6 +269,24 @@ class Assembler:
         res = np.zeros((self.num_nodes, 6)) if want_res else None
         _check(self.lib.a2ds_assemble_jacobian(self.h, _d(v), _d(res), A.h))
         return res
+
+    def add_mat_xpt_sens_inner_product(self, scale, mat_type, psi, phi, dfdX=None, vars_=None,
+                                       dh=1e-7):
+        """dfdX += scale * d(psi^T M phi)/dX (num_nodes x 3), M = K at vars_
+        or G along vars_; element-by-element central differences with step
+        dh (TACSElement::addMatXptSensInnerProduct)."""
+        if dfdX is None:
+            dfdX = np.zeros((self.num_nodes, 3))
+        assert dfdX.dtype == np.float64 and dfdX.flags.c_contiguous
+        ps, ph, v = _f64(psi), _f64(phi), _f64(vars_)
+        for a in (ps, ph) + (() if v is None else (v,)):
+            if a.size != self.num_nodes * 6:
+                raise ValueError("vectors are num_nodes x 6")
+        if dfdX.size != self.num_nodes * 3:
+            raise ValueError("dfdX is num_nodes x 3")
+        _check(self.lib.a2ds_add_mat_xpt_sens_inner_product(
+            self.h, int(mat_type), float(scale), _d(ps), _d(ph), _d(v), float(dh), _d(dfdX)))
+        return dfdX
 
 
 class BCSRMat:
@@ -454,6 +476,12 @@ class LinearBuckling:
     def eig_sens_thickness(self, n, num_groups):
         out = np.zeros(num_groups)
         _check(self.lib.a2ds_eig_sens_thickness(self.a.h, int(n), _d(out)))
+        return out
+
+    def eval_eigen_xpt_sens(self, n, dh=1e-7):
+        """TACSLinearBuckling::evalEigenXptSens: dlambda_n/dX, num_nodes x 3."""
+        out = np.zeros((self.a.num_nodes, 3))
+        _check(self.lib.a2ds_eig_sens_xpts(self.a.h, int(n), float(dh), _d(out)))
         return out
 
 

@@ -114,6 +114,23 @@ def cylinder(nx: int, ny: int, order: int = 2, R: float = 1.0, L: float = 2.0,
                                imperfection=imperfection, seed=seed, phases=phi.tolist()))
 
 
+def radial_shape_modes(m: ShellMesh, mmax: int = 8, nmax: int = 8) -> np.ndarray:
+    """Node-coordinate derivatives dX/ds_p (P x nn x 3) of a cylinder's radial
+    shape parameters: delta r = sum_p s_p sin(m_p pi x/L) cos(n_p theta),
+    (m_p, n_p) = (1 + p // nmax, p % nmax) on an mmax x nmax grid (64
+    parameters by default), along each node's radial direction (axis x)."""
+    X = m.X
+    L = float(m.meta.get("L", X[:, 0].max()))
+    th = np.arctan2(X[:, 2], X[:, 1])
+    radial = np.stack([np.zeros_like(th), np.cos(th), np.sin(th)], axis=1)
+    out = np.zeros((mmax * nmax, X.shape[0], 3))
+    for p in range(mmax * nmax):
+        mp, n_p = 1 + p // nmax, p % nmax
+        amp = np.sin(mp * np.pi * X[:, 0] / L) * np.cos(n_p * th)
+        out[p] = amp[:, None] * radial
+    return out
+
+
 def classical_cylinder_load(E: float, nu: float, t: float, R: float) -> float:
     """Classical axial buckling load per unit circumference, E t^2/(R sqrt(3(1-nu^2)))."""
     return E * t * t / (R * np.sqrt(3.0 * (1.0 - nu * nu)))

@@ -329,6 +329,37 @@ int a2ds_assemble_mat(a2ds_mesh mesh, int mat_type, const double *vars, a2ds_bcs
   return a2ds_assemble_mat_ex(mesh, mat_type, vars, A, A2DS_SCATTER_ATOMIC);
 }
 
+int a2ds_add_mat_xpt_sens_inner_product(a2ds_mesh mesh, int mat_type, double scale,
+                                        const double *psi, const double *phi,
+                                        const double *vars, double dh, double *dfdX) {
+  A2DS_GUARD_BEGIN
+  int rc = check_mesh(mesh, true);
+  if (rc) return rc;
+  if (!psi || !phi || !dfdX) return fail(A2DS_ERR_ARG, "null argument");
+  int mode;
+  if (mat_type == A2DS_STIFFNESS_MATRIX)
+    mode = MODE_K;
+  else if (mat_type == A2DS_GEOMETRIC_STIFFNESS_MATRIX)
+    mode = MODE_G;
+  else
+    return fail(A2DS_ERR_ARG, "mat_type must be STIFFNESS (0) or GEOMETRIC_STIFFNESS (2)");
+  if (dh == 0.0) dh = 1e-7;  // the reference's real-mode element step
+  Mesh &m = mesh->m;
+  DBuf<double> dpsi, dphi;
+  if ((rc = m.to_rows(psi, dpsi)) || (rc = m.to_rows(phi, dphi))) return rc;
+  const double *dst = nullptr;
+  if (vars) {
+    if ((rc = m.to_rows(vars, m.d_state))) return rc;
+    dst = m.d_state.p;
+  }
+  ElemLaunch L = m.launch_params(mode, dst, nullptr, nullptr);
+  L.cx = dpsi.p;
+  L.cy = dphi.p;
+  L.ccoef = scale;
+  return m.xpt_sens(L, dh, dfdX);
+  A2DS_GUARD_END
+}
+
 int a2ds_assemble_res(a2ds_mesh mesh, const double *vars, double *res) {
   if (!res) return fail(A2DS_ERR_ARG, "res is null");
   return assemble(mesh, MODE_R, vars, nullptr, res, A2DS_SCATTER_ATOMIC);

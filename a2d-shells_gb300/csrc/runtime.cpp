@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -203,6 +204,46 @@ int Mesh::element_output(const double *d_st, double *d_out) {
   int rc;
   if ((rc = launch_element_kernel(L, stream))) return rc;
   launches++;
+  return 0;
+}
+
+// TACSElement::addMatXptSensInnerProduct (src/elements/TACSElement.cpp:
+// 434-507) over all elements: central differences (fdOrder 2) in each
+// element coordinate k, X_k +/- dh.  Every element holds its own copy of its
+// coordinates, so one launch steps coordinate k of all elements at once;
+// the two launches of a step add +/- coef / (2 dh) times the contraction
+// into ce[e][k].  The element rows are summed into the nodes on the host,
+// element by element in order.
+int Mesh::xpt_sens(ElemLaunch L, double dh, double *dfdX) {
+  if (!(dh > 0.0) || !std::isfinite(dh)) return fail(A2DS_ERR_ARG, "finite-difference step must be > 0");
+  const int nk = 3 * npe;
+  DBuf<double> ce;
+  int rc;
+  if ((rc = ce.alloc((size_t)ne * nk))) return rc;
+  A2DS_CUDA_TRY(cudaMemsetAsync(ce.p, 0, ce.n * sizeof(double), stream));
+  const double c1 = L.ccoef, c2 = L.ccoef2;
+  L.cout = ce.p;
+  L.cstride = nk;
+  for (int k = 0; k < nk; k++)
+    for (int sgn = 1; sgn >= -1; sgn -= 2) {
+      L.xk = k;
+      L.xh = sgn * dh;
+      L.ccoef = sgn * c1 / (2.0 * dh);
+      L.ccoef2 = sgn * c2 / (2.0 * dh);
+      if ((rc = launch_element_kernel(L, stream))) return rc;
+      launches++;
+    }
+  std::vector<double> h;
+  try {
+    h.resize(ce.n);
+  } catch (const std::bad_alloc &) {
+    return fail(A2DS_ERR_NOMEM, "host allocation failed");
+  }
+  A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), ce.p, ce.n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(stream));
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < nk; k++)
+      dfdX[(size_t)conn[(size_t)e * npe + k / 3] * 3 + k % 3] += h[(size_t)e * nk + k];
   return 0;
 }
 

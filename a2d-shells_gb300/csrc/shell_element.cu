@@ -378,7 +378,11 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
 
   // ---- gather
   if (active) {
-    for (int i = tid; i < NN * 3; i += TPE) S.X[i] = L.X[(size_t)conn[i / 3] * 3 + i % 3];
+    for (int i = tid; i < NN * 3; i += TPE) {
+      double x = L.X[(size_t)conn[i / 3] * 3 + i % 3];
+      if (L.cstride && i == L.xk) x += L.xh;  // coordinate step (X sensitivities)
+      S.X[i] = x;
+    }
     for (int i = tid; i < NV; i += TPE)
       S.st[i] = (NEED_STATE && L.state) ? L.state[(size_t)conn[i / 6] * 6 + i % 6] : 0.0;
   }
@@ -860,10 +864,12 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
 
   if (!active) return;
 
-  // ---- contraction cx^T M_e cy into the element's design group (a warp
-  //      belongs to one element: reduce in the warp, one atomic per warp)
+  // ---- contractions ccoef cx^T M_e cy (+ ccoef2 cx2^T M_e cy2) into the
+  //      element's design group, or into slot xk of the element's row of
+  //      cout when cstride != 0 (a warp belongs to one element: reduce in
+  //      the warp, one atomic per warp)
   if (NEED_MAT && L.cout) {
-    double v = 0.0;
+    double v = 0.0, v2 = 0.0;
 #pragma unroll
     for (int m = 0; m < D::EPT; m++) {
       int idx = tid + TPE * m;
@@ -873,11 +879,18 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
         const size_t ga = (size_t)conn[a / 6] * 6 + a % 6, gb = (size_t)conn[b / 6] * 6 + b % 6;
         const double xy = (a == b) ? L.cx[ga] * L.cy[ga] : L.cx[ga] * L.cy[gb] + L.cx[gb] * L.cy[ga];
         v += acc[m] * xy;
+        if (L.cx2) {
+          const double xy2 =
+              (a == b) ? L.cx2[ga] * L.cy2[ga] : L.cx2[ga] * L.cy2[gb] + L.cx2[gb] * L.cy2[ga];
+          v2 += acc[m] * xy2;
+        }
       }
     }
+    v = L.ccoef * v + L.ccoef2 * v2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(L.cout + L.tgroup[e], L.ccoef * v);
+    double *dst = L.cstride ? L.cout + (size_t)e * L.cstride + L.xk : L.cout + L.tgroup[e];
+    if ((threadIdx.x & 31) == 0) atomicAdd(dst, v);
     return;
   }
 

@@ -1267,6 +1267,41 @@ int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out) {
   return 0;
 }
 
+// phi^T G phi and the load-path adjoint of an eigenvector:
+// K psi = d(phi^T G(path) phi)/d(path) = G(phi) phi (the third derivative of
+// the strain energy is symmetric), Dirichlet rows zeroed.  Uses Aux, r, t.
+static int path_adjoint(Mesh &m, BucklingState &S, const double *phi, double *psi,
+                        double *phiGphi) {
+  const size_t n6 = (size_t)m.nn * 6;
+  const int nbc = (int)m.bc_rows.size();
+  Blas B{m.stream};
+  B.launches = &m.launches;
+  int rc;
+  // phi vanishes on the Dirichlet DOFs
+  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, phi, S.r.p, m.stream))) return rc;
+  m.launches++;
+  *phiGphi = B.dot(phi, S.r.p, n6);
+  if (!(*phiGphi != 0.0) || !std::isfinite(*phiGphi))
+    return fail(A2DS_ERR_NUMERIC, "phi^T G phi vanishes");
+  if ((rc = m.assemble_device(MODE_G, phi, S.Aux.p, nullptr, A2DS_SCATTER_ATOMIC))) return rc;
+  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.Aux.p, phi, S.t.p, m.stream))) return rc;
+  m.launches++;
+  if (nbc) {
+    k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.t.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
+    m.launches++;
+  }
+  int inner = 0;
+  if (S.lev_fill >= m.nn) {
+    if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.t.p, psi, 1, 1e-13, 4, &inner))) return rc;
+  } else {
+    GmresWork gw;
+    double rn = 0.0;
+    if ((rc = gmres_device(m, &S.fk, S.K.p, S.t.p, psi, 30, 15, 1e-12, 1e-30, gw, B, &inner, &rn)))
+      return rc;
+  }
+  return 0;
+}
+
 int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt) {
   if (!mesh || !dlam_dt) return fail(A2DS_ERR_ARG, "null argument");
   Mesh &m = mesh->m;
@@ -1281,36 +1316,11 @@ int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt) {
   const int ng = (int)m.tvals.size();
   const double lam = S.lam[n];
   const double *phi = S.phi.p + (size_t)n * n6;
-  const int nbc = (int)m.bc_rows.size();
-  Blas B{m.stream};
-  B.launches = &m.launches;
   int rc;
-  // phi^T G phi (phi vanishes on the Dirichlet DOFs)
-  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, phi, S.r.p, m.stream))) return rc;
-  m.launches++;
-  const double phiGphi = B.dot(phi, S.r.p, n6);
-  if (!(phiGphi != 0.0) || !std::isfinite(phiGphi))
-    return fail(A2DS_ERR_NUMERIC, "phi^T G phi vanishes");
-  // adjoint: K psi = d(phi^T G(path) phi)/d(path) = G(phi) phi (the third
-  // derivative of the strain energy is symmetric), Dirichlet rows zeroed
-  if ((rc = m.assemble_device(MODE_G, phi, S.Aux.p, nullptr, A2DS_SCATTER_ATOMIC))) return rc;
-  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.Aux.p, phi, S.t.p, m.stream))) return rc;
-  m.launches++;
-  if (nbc) {
-    k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(S.t.p, m.d_bc_rows.p, m.d_bc_masks.p, nbc);
-    m.launches++;
-  }
   DBuf<double> psi, dd;
+  double phiGphi;
   if ((rc = psi.alloc(n6)) || (rc = dd.alloc(ng))) return rc;
-  int inner = 0;
-  if (S.lev_fill >= m.nn) {
-    if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.t.p, psi.p, 1, 1e-13, 4, &inner))) return rc;
-  } else {
-    GmresWork gw;
-    double rn = 0.0;
-    if ((rc = gmres_device(m, &S.fk, S.K.p, S.t.p, psi.p, 30, 15, 1e-12, 1e-30, gw, B, &inner, &rn)))
-      return rc;
-  }
+  if ((rc = path_adjoint(m, S, phi, psi.p, &phiGphi))) return rc;
   // dlam/dt_g = -[phi^T K' phi + lam phi^T G'(path) phi - lam psi^T K' path] / phi^T G phi,
   // ' = d/dt_g (element matrices with the derivative constitutive matrix)
   A2DS_CUDA_TRY(cudaMemsetAsync(dd.p, 0, ng * sizeof(double), m.stream));
@@ -1320,6 +1330,9 @@ int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt) {
   L.cx = phi;
   L.cy = phi;
   L.ccoef = 1.0;
+  L.cx2 = psi.p;
+  L.cy2 = S.path.p;
+  L.ccoef2 = -lam;
   if ((rc = launch_element_kernel(L, m.stream))) return rc;
   L = m.launch_params(MODE_G, S.path.p, nullptr, nullptr);
   L.dconst = 1;
@@ -1328,18 +1341,49 @@ int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt) {
   L.cy = phi;
   L.ccoef = lam;
   if ((rc = launch_element_kernel(L, m.stream))) return rc;
-  L = m.launch_params(MODE_K, nullptr, nullptr, nullptr);
-  L.dconst = 1;
-  L.cout = dd.p;
-  L.cx = psi.p;
-  L.cy = S.path.p;
-  L.ccoef = -lam;
-  if ((rc = launch_element_kernel(L, m.stream))) return rc;
-  m.launches += 3;
+  m.launches += 2;
   std::vector<double> h(ng);
   A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), dd.p, ng * sizeof(double), cudaMemcpyDeviceToHost, m.stream));
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   for (int g = 0; g < ng; g++) dlam_dt[g] = -h[g] / phiGphi;
+  return 0;
+}
+
+int a2ds_eig_sens_xpts(a2ds_mesh mesh, int n, double dh, double *dlam_dX) {
+  if (!mesh || !dlam_dX) return fail(A2DS_ERR_ARG, "null argument");
+  Mesh &m = mesh->m;
+  BucklingState *Sp = (BucklingState *)m.solver;
+  if (!Sp || Sp->lam.empty())
+    return fail(A2DS_ERR_STATE, "eigenvalue sensitivities need a preceding a2ds_buckling_solve");
+  BucklingState &S = *Sp;
+  if (n < 0 || n >= (int)S.lam.size()) return fail(A2DS_ERR_ARG, "eigenvalue index out of range");
+  if (m.alpha * m.temperature != 0.0)
+    return fail(A2DS_ERR_ARG, "coordinate sensitivities of thermal buckling loads are not supported");
+  if (dh == 0.0) dh = 1e-7;
+  const size_t n6 = (size_t)m.nn * 6;
+  const double lam = S.lam[n];
+  const double *phi = S.phi.p + (size_t)n * n6;
+  int rc;
+  DBuf<double> psi;
+  double phiGphi;
+  if ((rc = psi.alloc(n6)) || (rc = path_adjoint(m, S, phi, psi.p, &phiGphi))) return rc;
+  std::fill(dlam_dX, dlam_dX + (size_t)m.nn * 3, 0.0);
+  // K': phi^T K' phi - lam psi^T K' path in one pass per step; G': lam phi^T G'(path) phi
+  ElemLaunch L = m.launch_params(MODE_K, nullptr, nullptr, nullptr);
+  L.cx = phi;
+  L.cy = phi;
+  L.ccoef = 1.0;
+  L.cx2 = psi.p;
+  L.cy2 = S.path.p;
+  L.ccoef2 = -lam;
+  if ((rc = m.xpt_sens(L, dh, dlam_dX))) return rc;
+  L = m.launch_params(MODE_G, S.path.p, nullptr, nullptr);
+  L.cx = phi;
+  L.cy = phi;
+  L.ccoef = lam;
+  if ((rc = m.xpt_sens(L, dh, dlam_dX))) return rc;
+  const double s = -1.0 / phiGphi;
+  for (size_t i = 0; i < (size_t)m.nn * 3; i++) dlam_dX[i] *= s;
   return 0;
 }
 

@@ -159,6 +159,20 @@ int a2ds_assemble_mat(a2ds_mesh mesh, int mat_type, const double *vars,
 int a2ds_assemble_mat_ex(a2ds_mesh mesh, int mat_type, const double *vars,
                          a2ds_bcsr A, int scatter);
 
+/* The assembler-level element inner product that the reference's (commented)
+   TACSLinearBuckling::evalEigenXptSens calls (src/TACSBuckling.cpp:471-476),
+   element by element TACSElement::addMatXptSensInnerProduct
+   (src/elements/TACSElement.cpp:434-507): dfdX += scale *
+   d(psi^T M(X, vars) phi)/dX for M = K (mat_type A2DS_STIFFNESS_MATRIX, at
+   vars) or G (A2DS_GEOMETRIC_STIFFNESS_MATRIX, along vars), by second-order
+   central differences with step dh in every element coordinate (dh = 0: the
+   reference's real-mode step 1e-7).  psi, phi, vars: num_nodes x 6 (vars
+   NULL = zero); dfdX: num_nodes x 3, added into.  Element matrices without
+   the Dirichlet rows. */
+int a2ds_add_mat_xpt_sens_inner_product(a2ds_mesh mesh, int mat_type, double scale,
+                                        const double *psi, const double *phi,
+                                        const double *vars, double dh, double *dfdX);
+
 /* TACSAssembler::assembleRes (src/TACSAssembler.cpp:4000) at vars (NULL =
    zero); res is num_nodes x 6, BC DOFs set to vars - bcval as in
    TACSBVec::applyBCs / the assembler's BC residual. */
@@ -299,6 +313,17 @@ int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out);
    src/TACSBuckling.cpp:359-382; the reference's evalEigenDVSens body is
    commented out).  Needs a preceding a2ds_buckling_solve on this mesh. */
 int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt);
+
+/* TACSLinearBuckling::evalEigenXptSens (src/TACSBuckling.cpp:457-497, body
+   commented out in the reference; the same formula):
+   dlambda/dX = -[phi^T K' phi + lambda phi^T G'(path) phi
+                  - lambda psi^T K' path] / (phi^T G phi),
+   ' = d/dX at fixed states, K psi = d(phi^T G(path) phi)/d(path), the
+   element derivatives by central differences with step dh (0 = 1e-7, the
+   reference's element default).  dlam_dX: num_nodes x 3.  Needs a
+   preceding a2ds_buckling_solve on this mesh; loads are fixed nodal forces
+   (no thermal load). */
+int a2ds_eig_sens_xpts(a2ds_mesh mesh, int n, double dh, double *dlam_dX);
 
 /* ------------------------------------------------------ BDF mesh input
    Replaces: TACSMeshLoader::scanBDFFile (src/io/TACSMeshLoader.cpp:569-1098),

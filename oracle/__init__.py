@@ -115,6 +115,27 @@ def element_jacobian(order, nonlinear, mat: Material, X, vars_, alpha=1.0):
     return res, J
 
 
+def element_xpt_inner_product(order, nonlinear, kind, mat: Material, X, vars_, psi, phi,
+                              dh=1e-7):
+    """d(sum_ij M[j][i] psi_i phi_j)/dX for one element (3 nn values):
+    TACSElement::addMatXptSensInnerProduct (src/elements/TACSElement.cpp:
+    434-507) in its real-mode form, second-order central differences with
+    step dh in each coordinate."""
+    X = np.array(X, dtype=np.float64).reshape(-1)
+    psi = np.asarray(psi, dtype=np.float64)
+    phi = np.asarray(phi, dtype=np.float64)
+    out = np.zeros(X.size)
+    for k in range(X.size):
+        xt = X[k]
+        X[k] = xt + dh
+        p2 = phi @ element_matrix(order, nonlinear, kind, mat, X, vars_) @ psi
+        X[k] = xt - dh
+        p1 = phi @ element_matrix(order, nonlinear, kind, mat, X, vars_) @ psi
+        X[k] = xt
+        out[k] = 0.5 * (p2 - p1) / dh
+    return out
+
+
 # ------------------------------------------------------------- solve path
 def _declare_solver(lib):
     lib.orc_assemble.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -198,6 +198,8 @@ static void run_elements(const std::string &out) {
     const int nv = 6 * nn;
     SplitMix rng(20261203ull + 7919ull * (uint64_t)e);
     std::vector<TacsScalar> Xall, Vall, Kall, Gall, Rall, Jall, JRall, params;
+    std::vector<TacsScalar> PSall, PHall, KXall, GXall;
+    SplitMix rng_x(977ull + 31ull * (uint64_t)e);  // psi, phi of the coordinate products
     for (int s = 0; s < nsamples; s++) {
       double h = rng.uniform(0.02, 0.6);
       double t = rng.uniform(1e-3, 2e-2);
@@ -237,6 +239,34 @@ static void run_elements(const std::string &out) {
                         zero.data(), JR.data(), J.data());
       elem->getMatType(TACS_GEOMETRIC_STIFFNESS_MATRIX, 0, 0.0, X.data(), vars.data(),
                        G.data());
+      // Coordinate inner products d(psi^T M phi)/dX of K and G
+      // (TACSElement::addMatXptSensInnerProduct, TACSElement.cpp:434-507:
+      // central differences with dh = 1e-7 in the real build, complex step
+      // in the complex build, where G is then the real-step central
+      // difference).  Zero-temperature samples only: every G evaluation of
+      // a nonlinear instantiation leaves its temperature stepped.
+      std::vector<TacsScalar> psi(nv), phi(nv), KX(3 * nn, 0.0), GX(3 * nn, 0.0);
+      for (int i = 0; i < nv; i++) {
+        psi[i] = rng_x.uniform(-1, 1);
+        phi[i] = rng_x.uniform(-1, 1);
+      }
+      if (temp == 0.0) {
+#ifdef TACS_USE_COMPLEX
+        if (e == 0) ((TACSQuad4Shell *)elem)->setComplexStepGmatrix(false);
+        if (e == 1) ((TACSQuad4NonlinearShell *)elem)->setComplexStepGmatrix(false);
+        if (e == 2) ((TACSQuad9Shell *)elem)->setComplexStepGmatrix(false);
+        if (e == 3) ((TACSQuad9NonlinearShell *)elem)->setComplexStepGmatrix(false);
+#endif
+        elem->addMatXptSensInnerProduct(TACS_STIFFNESS_MATRIX, 0, 0.0, 1.0, psi.data(),
+                                        phi.data(), X.data(), vars.data(), KX.data());
+        elem->addMatXptSensInnerProduct(TACS_GEOMETRIC_STIFFNESS_MATRIX, 0, 0.0, 1.0,
+                                        psi.data(), phi.data(), X.data(), vars.data(),
+                                        GX.data());
+      }
+      PSall.insert(PSall.end(), psi.begin(), psi.end());
+      PHall.insert(PHall.end(), phi.begin(), phi.end());
+      KXall.insert(KXall.end(), KX.begin(), KX.end());
+      GXall.insert(GXall.end(), GX.begin(), GX.end());
       Xall.insert(Xall.end(), X.begin(), X.end());
       Vall.insert(Vall.end(), vars.begin(), vars.end());
       Kall.insert(Kall.end(), K.begin(), K.end());
@@ -257,6 +287,10 @@ static void run_elements(const std::string &out) {
     save_d(out, pre + "res", Rall.data(), {nsamples, nv});
     save_d(out, pre + "J", Jall.data(), {nsamples, nv, nv});
     save_d(out, pre + "Jres", JRall.data(), {nsamples, nv});
+    save_d(out, pre + "xs_psi", PSall.data(), {nsamples, nv});
+    save_d(out, pre + "xs_phi", PHall.data(), {nsamples, nv});
+    save_d(out, pre + "KX", KXall.data(), {nsamples, nn, 3});
+    save_d(out, pre + "GX", GXall.data(), {nsamples, nn, 3});
   }
   tr->decref();
 }

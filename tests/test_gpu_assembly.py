@@ -51,6 +51,37 @@ def one_element(X, order, nl, E, nu, t, alpha, temp):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name,order,nl", TYPES)
+def test_element_xpt_products_vs_reference(name, order, nl):
+    """d(psi^T K phi)/dX and d(psi^T G phi)/dX (TACSElement::
+    addMatXptSensInnerProduct) on one-element meshes: GPU central
+    differences (dh = 1e-7, the reference's real-mode step) against the
+    reference's complex-step values (exact for K; for G the derivative of its
+    central-difference G, which is exact up to rounding here) and its
+    real-mode values (same formula for K)."""
+    f = np.load(os.path.join(GOLDEN, f"elements_{name}.npz"))
+    nn = order * order
+    for s in range(f["X"].shape[0]):
+        E, nu, t, alpha, temp, _ = f["params"][s]
+        if temp != 0.0:
+            continue
+        a = one_element(f["X"][s], order, nl, E, nu, t, alpha, temp)
+        v = f["vars"][s].reshape(nn, 6)
+        psi, phi = f["xs_psi"][s].reshape(nn, 6), f["xs_phi"][s].reshape(nn, 6)
+        KX = a.add_mat_xpt_sens_inner_product(1.0, capi.A2DS_STIFFNESS_MATRIX, psi, phi, vars_=v)
+        assert rel(KX, f["KX_cs"][s]) < 2e-8, (name, s, "K")
+        assert rel(KX, f["KX"][s]) < 2e-8, (name, s, "K vs real-mode")
+        GX = a.add_mat_xpt_sens_inner_product(1.0, capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, psi, phi,
+                                              vars_=v)
+        assert rel(GX, f["GX_cs"][s]) < 2e-8, (name, s, "G")
+        # scale and accumulation (atomic order of multi-warp elements: the
+        # stepped contractions cancel to ~1e-10 of the derivative)
+        acc = a.add_mat_xpt_sens_inner_product(-2.0, capi.A2DS_STIFFNESS_MATRIX, psi, phi,
+                                               dfdX=KX.copy(), vars_=v)
+        assert rel(acc, -KX) < 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,order,nl", TYPES)
 def test_element_matrices_vs_reference(name, order, nl):
     f = np.load(os.path.join(GOLDEN, f"elements_{name}.npz"))
     nn = order * order

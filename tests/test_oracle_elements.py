@@ -46,3 +46,30 @@ def test_element_matrices_match_reference(name, order, nl):
         assert rel(G, f["G"][s]) < 1e-12
         if temp == 0.0:
             assert rel(G, f["G_cs"][s]) < 1e-11
+
+
+@pytest.mark.parametrize("name,order,nl", TYPES)
+def test_element_xpt_products_match_reference(name, order, nl):
+    """Coordinate derivatives of psi^T K phi and psi^T G phi
+    (TACSElement::addMatXptSensInnerProduct): the oracle's central
+    differences (dh = 1e-7) against the reference's complex-step values.
+    K: the reference's real-build formula, ~5e-9 from its complex step.
+    G: a central difference (dh = 1e-4) inside the coordinate difference in
+    both the oracle and the reference's real build (the two agree to
+    ~1e-8), up to ~2e-5 from the complex step."""
+    f = np.load(os.path.join(GOLDEN, f"elements_{name}.npz"))
+    nn = order * order
+    for s in range(f["X"].shape[0]):
+        E, nu, t, alpha, temp, _ = f["params"][s]
+        if temp != 0.0:
+            continue
+        m = oracle.Material.iso(E, nu, t, alpha, temp)
+        args = (f["X"][s], f["vars"][s])
+        psi, phi = f["xs_psi"][s], f["xs_phi"][s]
+        KX = oracle.element_xpt_inner_product(order, nl, oracle.STIFFNESS, m, *args, psi, phi)
+        assert rel(KX, f["KX_cs"][s].reshape(-1)) < 2e-8, (name, s)
+        assert rel(KX, f["KX"][s].reshape(-1)) < 2e-8, (name, s)
+        GX = oracle.element_xpt_inner_product(order, nl, oracle.GEOMETRIC, m, *args, psi, phi)
+        assert rel(GX, f["GX"][s].reshape(-1)) < 2e-8, (name, s)
+        assert rel(GX, f["GX_cs"][s].reshape(-1)) < 5e-5, (name, s)
+    assert f["KX"].shape == (f["X"].shape[0], nn, 3)
