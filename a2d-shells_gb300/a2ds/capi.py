@@ -47,7 +47,8 @@ EXPORTS = [
     "a2ds_mesh_initialize", "a2ds_mesh_get_ordering", "a2ds_mesh_node_csr",
     "a2ds_bcsr_create", "a2ds_bcsr_destroy", "a2ds_bcsr_get", "a2ds_bcsr_set_values",
     "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
-    "a2ds_add_mat_xpt_sens_inner_product", "a2ds_eig_sens_xpts",
+    "a2ds_add_mat_xpt_sens_inner_product", "a2ds_add_adjoint_res_xpt_sens_product",
+    "a2ds_eval_mat_sv_sens_inner_product", "a2ds_eig_sens_xpts",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
     "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
@@ -141,6 +142,10 @@ def load(build: bool = False):
     lib.a2ds_eig_sens_xpts.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
     lib.a2ds_add_mat_xpt_sens_inner_product.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D,
                                                         P_D, P_D, ctypes.c_double, P_D]
+    lib.a2ds_add_adjoint_res_xpt_sens_product.argtypes = [VP, ctypes.c_double, P_D, P_D,
+                                                          ctypes.c_double, P_D]
+    lib.a2ds_eval_mat_sv_sens_inner_product.argtypes = [VP, ctypes.c_int, P_D, P_D, P_D,
+                                                        ctypes.c_double, P_D]
     lib.a2ds_bdf_scan.argtypes = [ctypes.c_char_p, ctypes.POINTER(VP)]
     lib.a2ds_bdf_destroy.argtypes = [VP]
     lib.a2ds_bdf_get_sizes.argtypes = [VP, P_I, P_I, P_I, P_I, P_I, P_I]
@@ -287,6 +292,35 @@ class Assembler:
         _check(self.lib.a2ds_add_mat_xpt_sens_inner_product(
             self.h, int(mat_type), float(scale), _d(ps), _d(ph), _d(v), float(dh), _d(dfdX)))
         return dfdX
+
+    def _vec6(self, a):
+        a = _f64(a)
+        if a is not None and a.size != self.num_nodes * 6:
+            raise ValueError("vectors are num_nodes x 6")
+        return a
+
+    def add_adjoint_res_xpt_sens_products(self, scale, psi, dfdX=None, vars_=None, dh=1e-7):
+        """dfdX += scale * psi^T dR(X, vars_)/dX (num_nodes x 3), element by
+        element central differences (TACSElement::addAdjResXptProduct)."""
+        if dfdX is None:
+            dfdX = np.zeros((self.num_nodes, 3))
+        if not (dfdX.dtype == np.float64 and dfdX.flags.c_contiguous
+                and dfdX.size == self.num_nodes * 3):
+            raise ValueError("dfdX is a contiguous float64 num_nodes x 3 array")
+        ps, v = self._vec6(psi), self._vec6(vars_)
+        _check(self.lib.a2ds_add_adjoint_res_xpt_sens_product(
+            self.h, float(scale), _d(ps), _d(v), float(dh), _d(dfdX)))
+        return dfdX
+
+    def eval_mat_sv_sens_inner_product(self, mat_type, psi, phi, vars_=None, dh=1e-7):
+        """d(psi^T M(vars_) phi)/d(vars_) (num_nodes x 6, Dirichlet entries
+        zero), element by element central differences
+        (TACSElement::getMatSVSensInnerProduct)."""
+        ps, ph, v = self._vec6(psi), self._vec6(phi), self._vec6(vars_)
+        out = np.zeros((self.num_nodes, 6))
+        _check(self.lib.a2ds_eval_mat_sv_sens_inner_product(
+            self.h, int(mat_type), _d(ps), _d(ph), _d(v), float(dh), _d(out)))
+        return out
 
 
 class BCSRMat:

@@ -12,7 +12,13 @@ This module is the driver on top of the GB300 library:
   factored on the GPU each step;
 * `preload_buckling`: the eigenproblem K_T(u) x + lam G(u) x = 0 about the
   converged preload u, with G(u) the geometric stiffness along u (stated
-  definition), solved by the library's shift-invert Lanczos.
+  definition), solved by the library's shift-invert Lanczos;
+* `preload_xpt_sens`: d(lam)/dX of one of those multipliers, the
+  coordinate-sensitivity formula of the reference's (commented-out)
+  TACSLinearBuckling::evalEigenXptSens (src/TACSBuckling.cpp:457-497) with
+  the preload's Newton system K_T(u) in place of K: element states are
+  recomputed from u and the coordinates on the GPU for every derivative
+  (nothing of the Newton iterations is stored).
 """
 from __future__ import annotations
 
@@ -76,3 +82,32 @@ def preload_buckling(assembler: capi.Assembler, u, sigma: float, num_eigvals: in
                             eig_tol=eig_tol, precision=precision, block_size=block_size)
     lam = b.solve_matrices(KT, G)
     return lam, b, KT, G
+
+
+def preload_xpt_sens(assembler: capi.Assembler, u, lam: float, phi, KT, G,
+                     precision: int = 64, dh: float = 1e-7):
+    """d(lam)/dX (num_nodes x 3) for K_T(u) phi + lam G(u) phi = 0 about the
+    preload R(u, X) = s f (f fixed nodal loads):
+
+      dlam/dX = -[phi^T K_T' phi + lam phi^T G' phi - psi^T R'] / (phi^T G phi),
+      K_T(u) psi = d/du [phi^T (K_T(u) + lam G(u)) phi],
+
+    ' = d/dX at fixed u.  KT and G are the matrices the buckling solve used
+    (K_T(u) with its Dirichlet rows, G(u)).  All element derivatives are the
+    library's element-by-element central differences (step dh)."""
+    phi = np.asarray(phi, float).reshape(-1, 6)
+    u = np.asarray(u, float).reshape(-1, 6)
+    K_, G_ = capi.A2DS_STIFFNESS_MATRIX, capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX
+    phiGphi = float(np.sum(phi * G.mult(phi)))
+    if not np.isfinite(phiGphi) or phiGphi == 0.0:
+        raise RuntimeError("phi^T G phi vanishes")
+    g = (assembler.eval_mat_sv_sens_inner_product(K_, phi, phi, u, dh=dh)
+         + lam * assembler.eval_mat_sv_sens_inner_product(G_, phi, phi, u, dh=dh))
+    pc = capi.SchurPc(KT, 1000000, precision)
+    pc.factor(KT)
+    psi = pc.apply_factor(g)
+    psi = psi + pc.apply_factor(g - KT.mult(psi))  # one refinement step
+    dX = assembler.add_mat_xpt_sens_inner_product(1.0, K_, phi, phi, vars_=u, dh=dh)
+    assembler.add_mat_xpt_sens_inner_product(lam, G_, phi, phi, dfdX=dX, vars_=u, dh=dh)
+    assembler.add_adjoint_res_xpt_sens_products(-1.0, psi, dfdX=dX, vars_=u, dh=dh)
+    return -dX / phiGphi

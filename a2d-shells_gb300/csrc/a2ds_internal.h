@@ -126,10 +126,12 @@ struct ElemLaunch {
   // optional second contraction in the same launch (NULL = none)
   const double *cx2, *cy2;
   double ccoef2;
-  // Coordinate sensitivities: cstride != 0 adds xh to the element's local
-  // coordinate xk (0..3*NN-1) and sends the contractions to
-  // cout[e * cstride + xk] instead of the design group.
-  int cstride, xk;
+  // Finite-difference sensitivities: cstride != 0 adds xh to the element's
+  // local coordinate xk (0..3*NN-1), or with xstate = 1 to its local state
+  // entry xk (0..6*NN-1), and sends the contractions to cout[e * cstride + xk]
+  // instead of the design group.  MODE_R with cout contracts the element
+  // residual with cx instead of scattering it.
+  int cstride, xk, xstate;
   double xh;
   // MODE_OUT: Ne x NN x 18 (strain e[9], stress C e[9] per node point)
   double *out;

@@ -356,7 +356,62 @@ int a2ds_add_mat_xpt_sens_inner_product(a2ds_mesh mesh, int mat_type, double sca
   L.cx = dpsi.p;
   L.cy = dphi.p;
   L.ccoef = scale;
-  return m.xpt_sens(L, dh, dfdX);
+  return m.fd_sens(L, dh, 0, dfdX);
+  A2DS_GUARD_END
+}
+
+int a2ds_add_adjoint_res_xpt_sens_product(a2ds_mesh mesh, double scale, const double *psi,
+                                          const double *vars, double dh, double *dfdX) {
+  A2DS_GUARD_BEGIN
+  int rc = check_mesh(mesh, true);
+  if (rc) return rc;
+  if (!psi || !dfdX) return fail(A2DS_ERR_ARG, "null argument");
+  if (dh == 0.0) dh = 1e-7;  // the reference's real-mode element step
+  Mesh &m = mesh->m;
+  DBuf<double> dpsi;
+  if ((rc = m.to_rows(psi, dpsi))) return rc;
+  const double *dst = nullptr;
+  if (vars) {
+    if ((rc = m.to_rows(vars, m.d_state))) return rc;
+    dst = m.d_state.p;
+  }
+  ElemLaunch L = m.launch_params(MODE_R, dst, nullptr, nullptr);
+  L.cx = dpsi.p;
+  L.ccoef = scale;
+  return m.fd_sens(L, dh, 0, dfdX);
+  A2DS_GUARD_END
+}
+
+int a2ds_eval_mat_sv_sens_inner_product(a2ds_mesh mesh, int mat_type, const double *psi,
+                                        const double *phi, const double *vars, double dh,
+                                        double *dfdu) {
+  A2DS_GUARD_BEGIN
+  int rc = check_mesh(mesh, true);
+  if (rc) return rc;
+  if (!psi || !phi || !dfdu) return fail(A2DS_ERR_ARG, "null argument");
+  int mode;
+  if (mat_type == A2DS_STIFFNESS_MATRIX)
+    mode = MODE_K;
+  else if (mat_type == A2DS_GEOMETRIC_STIFFNESS_MATRIX)
+    mode = MODE_G;
+  else
+    return fail(A2DS_ERR_ARG, "mat_type must be STIFFNESS (0) or GEOMETRIC_STIFFNESS (2)");
+  if (dh == 0.0) dh = 1e-7;
+  Mesh &m = mesh->m;
+  DBuf<double> dpsi, dphi;
+  if ((rc = m.to_rows(psi, dpsi)) || (rc = m.to_rows(phi, dphi))) return rc;
+  if ((rc = m.to_rows(vars, m.d_state))) return rc;  // NULL = zero state
+  ElemLaunch L = m.launch_params(mode, m.d_state.p, nullptr, nullptr);
+  L.cx = dpsi.p;
+  L.cy = dphi.p;
+  L.ccoef = 1.0;
+  const size_t n6 = (size_t)m.nn * 6;
+  std::fill(dfdu, dfdu + n6, 0.0);
+  if ((rc = m.fd_sens(L, dh, 1, dfdu))) return rc;
+  for (size_t b = 0; b < m.bc_nodes.size(); b++)
+    for (int k = 0; k < 6; k++)
+      if (m.bc_masks[b] & (1 << k)) dfdu[(size_t)m.bc_nodes[b] * 6 + k] = 0.0;
+  return 0;
   A2DS_GUARD_END
 }
 

@@ -207,16 +207,20 @@ int Mesh::element_output(const double *d_st, double *d_out) {
   return 0;
 }
 
-// TACSElement::addMatXptSensInnerProduct (src/elements/TACSElement.cpp:
-// 434-507) over all elements: central differences (fdOrder 2) in each
-// element coordinate k, X_k +/- dh.  Every element holds its own copy of its
-// coordinates, so one launch steps coordinate k of all elements at once;
-// the two launches of a step add +/- coef / (2 dh) times the contraction
-// into ce[e][k].  The element rows are summed into the nodes on the host,
-// element by element in order.
-int Mesh::xpt_sens(ElemLaunch L, double dh, double *dfdX) {
+// Element-by-element central differences (fdOrder 2) of the contractions
+// that L describes, in each element coordinate (wrt_state = 0: the
+// reference's TACSElement::addMatXptSensInnerProduct and addAdjResXptProduct,
+// src/elements/TACSElement.cpp:434-507, 270-330) or each element state entry
+// (wrt_state = 1: getMatSVSensInnerProduct, :509-581), step +/- dh.  Every
+// element holds its own copy of its coordinates and state, so one launch
+// steps entry k of all elements at once; the two launches of a step add
+// +/- coef / (2 dh) times the contraction into ce[e][k].  The element rows
+// are summed into the nodes on the host, element by element in order:
+// out is num_nodes x 3 (coordinates) or num_nodes x 6 (state), caller
+// numbering, added into.
+int Mesh::fd_sens(ElemLaunch L, double dh, int wrt_state, double *out) {
   if (!(dh > 0.0) || !std::isfinite(dh)) return fail(A2DS_ERR_ARG, "finite-difference step must be > 0");
-  const int nk = 3 * npe;
+  const int per = wrt_state ? 6 : 3, nk = per * npe;
   DBuf<double> ce;
   int rc;
   if ((rc = ce.alloc((size_t)ne * nk))) return rc;
@@ -224,6 +228,7 @@ int Mesh::xpt_sens(ElemLaunch L, double dh, double *dfdX) {
   const double c1 = L.ccoef, c2 = L.ccoef2;
   L.cout = ce.p;
   L.cstride = nk;
+  L.xstate = wrt_state ? 1 : 0;
   for (int k = 0; k < nk; k++)
     for (int sgn = 1; sgn >= -1; sgn -= 2) {
       L.xk = k;
@@ -243,7 +248,7 @@ int Mesh::xpt_sens(ElemLaunch L, double dh, double *dfdX) {
   A2DS_CUDA_TRY(cudaStreamSynchronize(stream));
   for (int e = 0; e < ne; e++)
     for (int k = 0; k < nk; k++)
-      dfdX[(size_t)conn[(size_t)e * npe + k / 3] * 3 + k % 3] += h[(size_t)e * nk + k];
+      out[(size_t)conn[(size_t)e * npe + k / per] * per + k % per] += h[(size_t)e * nk + k];
   return 0;
 }
 

@@ -52,11 +52,12 @@ struct Mesh {
   // strain and stress at every element's node points (MODE_OUT), d_out
   // ne x npe x 18 on the device
   int element_output(const double *d_st, double *d_out);
-  // Coordinate derivative of the element contractions that L describes
-  // (cx, cy, ccoef and optionally cx2, cy2, ccoef2), by second-order central
-  // differences with step dh over every element coordinate; adds the result
-  // into dfdX (nn x 3, caller numbering).
-  int xpt_sens(ElemLaunch L, double dh, double *dfdX);
+  // Derivative of the element contractions that L describes (cx, cy, ccoef
+  // and optionally cx2, cy2, ccoef2; or cx^T R_e for MODE_R) with respect to
+  // every element coordinate (wrt_state = 0; out nn x 3) or state entry
+  // (wrt_state = 1; out nn x 6), by second-order central differences with
+  // step dh; added into out (caller numbering).
+  int fd_sens(ElemLaunch L, double dh, int wrt_state, double *out);
   ~Mesh();
 };
 

@@ -380,11 +380,14 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
   if (active) {
     for (int i = tid; i < NN * 3; i += TPE) {
       double x = L.X[(size_t)conn[i / 3] * 3 + i % 3];
-      if (L.cstride && i == L.xk) x += L.xh;  // coordinate step (X sensitivities)
+      if (L.cstride && !L.xstate && i == L.xk) x += L.xh;  // coordinate step
       S.X[i] = x;
     }
-    for (int i = tid; i < NV; i += TPE)
-      S.st[i] = (NEED_STATE && L.state) ? L.state[(size_t)conn[i / 6] * 6 + i % 6] : 0.0;
+    for (int i = tid; i < NV; i += TPE) {
+      double q = (NEED_STATE && L.state) ? L.state[(size_t)conn[i / 6] * 6 + i % 6] : 0.0;
+      if (NEED_STATE && L.cstride && L.xstate && i == L.xk) q += L.xh;  // state step
+      S.st[i] = q;
+    }
   }
   const double t = active ? L.tvals[L.tgroup[e]] : 1.0;
   const Stiff C = L.dconst ? d_stiff_dt(L.E, L.nu, t) : d_stiff(L.E, L.nu, t);
@@ -887,6 +890,20 @@ __global__ void __launch_bounds__(128) shell_kernel(ElemLaunch L) {
       }
     }
     v = L.ccoef * v + L.ccoef2 * v2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    double *dst = L.cstride ? L.cout + (size_t)e * L.cstride + L.xk : L.cout + L.tgroup[e];
+    if ((threadIdx.x & 31) == 0) atomicAdd(dst, v);
+    return;
+  }
+
+  // ---- residual contraction ccoef cx^T R_e into slot xk of the element's
+  //      row of cout (coordinate derivatives of adjoint-residual products)
+  if (NEED_RES && L.cout) {
+    double v = 0.0;
+    for (int j = tid, m = 0; j < NV; j += TPE, m++)
+      v += racc[m] * L.cx[(size_t)conn[j / 6] * 6 + j % 6];
+    v *= L.ccoef;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     double *dst = L.cstride ? L.cout + (size_t)e * L.cstride + L.xk : L.cout + L.tgroup[e];

@@ -1376,12 +1376,12 @@ int a2ds_eig_sens_xpts(a2ds_mesh mesh, int n, double dh, double *dlam_dX) {
   L.cx2 = psi.p;
   L.cy2 = S.path.p;
   L.ccoef2 = -lam;
-  if ((rc = m.xpt_sens(L, dh, dlam_dX))) return rc;
+  if ((rc = m.fd_sens(L, dh, 0, dlam_dX))) return rc;
   L = m.launch_params(MODE_G, S.path.p, nullptr, nullptr);
   L.cx = phi;
   L.cy = phi;
   L.ccoef = lam;
-  if ((rc = m.xpt_sens(L, dh, dlam_dX))) return rc;
+  if ((rc = m.fd_sens(L, dh, 0, dlam_dX))) return rc;
   const double s = -1.0 / phiGphi;
   for (size_t i = 0; i < (size_t)m.nn * 3; i++) dlam_dX[i] *= s;
   return 0;

@@ -173,6 +173,27 @@ int a2ds_add_mat_xpt_sens_inner_product(a2ds_mesh mesh, int mat_type, double sca
                                         const double *psi, const double *phi,
                                         const double *vars, double dh, double *dfdX);
 
+/* The adjoint-residual coordinate product of the same body
+   (addAdjointResXptSensProducts, src/TACSBuckling.cpp:486), element by
+   element TACSElement::addAdjResXptProduct (src/elements/TACSElement.cpp:
+   270-330): dfdX += scale * psi^T dR(X, vars)/dX, central differences with
+   step dh (0 = 1e-7).  psi, vars: num_nodes x 6 (vars NULL = zero); dfdX
+   num_nodes x 3, added into.  The element residuals only (no Dirichlet
+   rows). */
+int a2ds_add_adjoint_res_xpt_sens_product(a2ds_mesh mesh, double scale, const double *psi,
+                                          const double *vars, double dh, double *dfdX);
+
+/* The state derivative of the same body (evalMatSVSensInnerProduct,
+   src/TACSBuckling.cpp:481), element by element
+   TACSElement::getMatSVSensInnerProduct (src/elements/TACSElement.cpp:
+   509-581): dfdu = d(psi^T M(vars) phi)/d(vars) for M = K (the tangent at
+   vars) or G (along vars), central differences with step dh (0 = 1e-7) in
+   every element state entry.  dfdu: num_nodes x 6, overwritten, Dirichlet
+   entries zero (the right-hand side of a load-path adjoint). */
+int a2ds_eval_mat_sv_sens_inner_product(a2ds_mesh mesh, int mat_type, const double *psi,
+                                        const double *phi, const double *vars, double dh,
+                                        double *dfdu);
+
 /* TACSAssembler::assembleRes (src/TACSAssembler.cpp:4000) at vars (NULL =
    zero); res is num_nodes x 6, BC DOFs set to vars - bcval as in
    TACSBVec::applyBCs / the assembler's BC residual. */

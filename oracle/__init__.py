@@ -136,6 +136,45 @@ def element_xpt_inner_product(order, nonlinear, kind, mat: Material, X, vars_, p
     return out
 
 
+def element_sv_inner_product(order, nonlinear, kind, mat: Material, X, vars_, psi, phi,
+                             dh=1e-7):
+    """d(sum_ij M[j][i] psi_i phi_j)/d(vars) for one element (6 nn values):
+    TACSElement::getMatSVSensInnerProduct (src/elements/TACSElement.cpp:
+    509-581), real-mode central differences with step dh."""
+    v = np.array(vars_, dtype=np.float64).reshape(-1)
+    psi = np.asarray(psi, dtype=np.float64)
+    phi = np.asarray(phi, dtype=np.float64)
+    out = np.zeros(v.size)
+    for k in range(v.size):
+        vt = v[k]
+        v[k] = vt + dh
+        p2 = phi @ element_matrix(order, nonlinear, kind, mat, X, v) @ psi
+        v[k] = vt - dh
+        p1 = phi @ element_matrix(order, nonlinear, kind, mat, X, v) @ psi
+        v[k] = vt
+        out[k] = 0.5 * (p2 - p1) / dh
+    return out
+
+
+def element_adjres_xpt_product(order, nonlinear, mat: Material, X, vars_, psi, dh=1e-7):
+    """psi^T dR/dX for one element (3 nn values): TACSElement::
+    addAdjResXptProduct (src/elements/TACSElement.cpp:270-330), real-mode
+    central differences with step dh (psi times the residual difference,
+    divided by 2 dh)."""
+    X = np.array(X, dtype=np.float64).reshape(-1)
+    psi = np.asarray(psi, dtype=np.float64)
+    out = np.zeros(X.size)
+    for k in range(X.size):
+        xt = X[k]
+        X[k] = xt + dh
+        r2 = element_residual(order, nonlinear, mat, X, vars_)
+        X[k] = xt - dh
+        r1 = element_residual(order, nonlinear, mat, X, vars_)
+        X[k] = xt
+        out[k] = np.sum(psi * (r2 - r1) / (2.0 * dh))
+    return out
+
+
 # ------------------------------------------------------------- solve path
 def _declare_solver(lib):
     lib.orc_assemble.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -198,7 +198,7 @@ static void run_elements(const std::string &out) {
     const int nv = 6 * nn;
     SplitMix rng(20261203ull + 7919ull * (uint64_t)e);
     std::vector<TacsScalar> Xall, Vall, Kall, Gall, Rall, Jall, JRall, params;
-    std::vector<TacsScalar> PSall, PHall, KXall, GXall;
+    std::vector<TacsScalar> PSall, PHall, KXall, GXall, KUall, GUall, RXall;
     SplitMix rng_x(977ull + 31ull * (uint64_t)e);  // psi, phi of the coordinate products
     for (int s = 0; s < nsamples; s++) {
       double h = rng.uniform(0.02, 0.6);
@@ -246,6 +246,7 @@ static void run_elements(const std::string &out) {
       // difference).  Zero-temperature samples only: every G evaluation of
       // a nonlinear instantiation leaves its temperature stepped.
       std::vector<TacsScalar> psi(nv), phi(nv), KX(3 * nn, 0.0), GX(3 * nn, 0.0);
+      std::vector<TacsScalar> KU(nv, 0.0), GU(nv, 0.0), RX(3 * nn, 0.0);
       for (int i = 0; i < nv; i++) {
         psi[i] = rng_x.uniform(-1, 1);
         phi[i] = rng_x.uniform(-1, 1);
@@ -262,7 +263,18 @@ static void run_elements(const std::string &out) {
         elem->addMatXptSensInnerProduct(TACS_GEOMETRIC_STIFFNESS_MATRIX, 0, 0.0, 1.0,
                                         psi.data(), phi.data(), X.data(), vars.data(),
                                         GX.data());
+        // state derivatives (getMatSVSensInnerProduct, :509-581) and the
+        // adjoint-residual coordinate product (addAdjResXptProduct, :270)
+        elem->getMatSVSensInnerProduct(TACS_STIFFNESS_MATRIX, 0, 0.0, psi.data(), phi.data(),
+                                       X.data(), vars.data(), KU.data());
+        elem->getMatSVSensInnerProduct(TACS_GEOMETRIC_STIFFNESS_MATRIX, 0, 0.0, psi.data(),
+                                       phi.data(), X.data(), vars.data(), GU.data());
+        elem->addAdjResXptProduct(0, 0.0, 1.0, psi.data(), X.data(), vars.data(), zero.data(),
+                                  zero.data(), RX.data());
       }
+      KUall.insert(KUall.end(), KU.begin(), KU.end());
+      GUall.insert(GUall.end(), GU.begin(), GU.end());
+      RXall.insert(RXall.end(), RX.begin(), RX.end());
       PSall.insert(PSall.end(), psi.begin(), psi.end());
       PHall.insert(PHall.end(), phi.begin(), phi.end());
       KXall.insert(KXall.end(), KX.begin(), KX.end());
@@ -291,6 +303,9 @@ static void run_elements(const std::string &out) {
     save_d(out, pre + "xs_phi", PHall.data(), {nsamples, nv});
     save_d(out, pre + "KX", KXall.data(), {nsamples, nn, 3});
     save_d(out, pre + "GX", GXall.data(), {nsamples, nn, 3});
+    save_d(out, pre + "KU", KUall.data(), {nsamples, nv});
+    save_d(out, pre + "GU", GUall.data(), {nsamples, nv});
+    save_d(out, pre + "RX", RXall.data(), {nsamples, nn, 3});
   }
   tr->decref();
 }

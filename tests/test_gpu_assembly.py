@@ -73,6 +73,19 @@ def test_element_xpt_products_vs_reference(name, order, nl):
         GX = a.add_mat_xpt_sens_inner_product(1.0, capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, psi, phi,
                                               vars_=v)
         assert rel(GX, f["GX_cs"][s]) < 2e-8, (name, s, "G")
+        # state derivatives (getMatSVSensInnerProduct) and the
+        # adjoint-residual coordinate product (addAdjResXptProduct)
+        KU = a.eval_mat_sv_sens_inner_product(capi.A2DS_STIFFNESS_MATRIX, psi, phi, v)
+        if nl:
+            assert rel(KU, f["KU_cs"][s].reshape(nn, 6)) < 2e-8, (name, s, "K state")
+        else:  # the linear tangent does not depend on the state
+            scale = np.abs(f["K"][s]).max() * np.abs(psi).max() * np.abs(phi).max()
+            assert np.abs(KU).max() <= 1e-6 * scale, (name, s, "linear K state")
+        GU = a.eval_mat_sv_sens_inner_product(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, psi, phi, v)
+        assert rel(GU, f["GU_cs"][s].reshape(nn, 6)) < 2e-8, (name, s, "G state")
+        RX = a.add_adjoint_res_xpt_sens_products(1.0, psi, vars_=v)
+        assert rel(RX, f["RX_cs"][s]) < 5e-8, (name, s, "residual")
+        assert rel(RX, f["RX"][s]) < 2e-8, (name, s, "residual vs real-mode")
         # scale and accumulation (atomic order of multi-warp elements: the
         # stepped contractions cancel to ~1e-10 of the derivative)
         acc = a.add_mat_xpt_sens_inner_product(-2.0, capi.A2DS_STIFFNESS_MATRIX, psi, phi,

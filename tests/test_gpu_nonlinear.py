@@ -56,3 +56,51 @@ def test_newton_preload_and_buckling(precision):
     lam, b, _, _ = nonlinear.preload_buckling(a, u, 0.95 * dense[0], num_eigvals=nev,
                                               eig_tol=1e-12, precision=precision, block_size=4)
     assert np.max(np.abs(lam - dense[:nev]) / np.abs(dense[:nev])) < 1e-8, (lam, dense[:nev])
+
+
+@pytest.mark.gpu
+def test_preload_buckling_xpt_sensitivity_vs_finite_difference():
+    """d(lam)/dX about a nonlinear preloaded state (nonlinear.preload_xpt_sens:
+    the evalEigenXptSens formula with the Newton tangent K_T(u) in the load-path
+    adjoint and element states recomputed on the GPU) contracted with
+    axisymmetric radial shape modes, against central differences of whole
+    Newton + buckling solves on the moved meshes; rigid translations and
+    rotations about the axis leave the multiplier unchanged."""
+    m = meshgen.cylinder(8, 16)
+    t = m.meta["t"]
+    load = 0.3 * meshgen.classical_cylinder_load(m.E, m.nu, t, 1.0)
+    modes = meshgen.radial_shape_modes(m)
+    sigma = None
+
+    def solve(X):
+        nonlocal sigma
+        a = capi.Assembler(X, m.conn, nonlinear=True)
+        a.set_material(m.E, m.nu)
+        a.set_thickness([t])
+        a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+        a.initialize(capi.A2DS_TACS_AMD_ORDER)
+        u, _, _ = nonlinear.newton_preload(a, m.rhs, m.bc_nodes, m.bc_mask, load, nsteps=4,
+                                           rtol=1e-11)
+        if sigma is None:
+            from test_gpu_solve import dense_buckling
+            KT, G = a.create_mat(), a.create_mat()
+            a.assemble_jacobian(KT, u, want_res=False)
+            a.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, u)
+            sigma = 0.95 * dense_buckling(KT.to_dense_nodes(), G.to_dense_nodes(), m.bc_nodes,
+                                          m.bc_mask)[0]
+        lam, b, KT, G = nonlinear.preload_buckling(a, u, sigma, num_eigvals=2, eig_tol=1e-12,
+                                                   block_size=2)
+        return a, u, lam, b, KT, G
+
+    a, u, lam, b, KT, G = solve(m.X)
+    dX = nonlinear.preload_xpt_sens(a, u, lam[0], b.eigvecs[0], KT, G)
+    assert dX.shape == m.X.shape and np.all(np.isfinite(dX))
+    scale = np.abs(dX).sum()
+    assert np.all(np.abs(dX.sum(axis=0)) <= 1e-5 * scale), dX.sum(axis=0)
+    spin = np.stack([np.zeros(m.num_nodes), -m.X[:, 2], m.X[:, 1]], axis=1)
+    assert abs(np.sum(dX * spin)) <= 1e-5 * scale
+    eps = 1e-4
+    for p in (0, 8):  # (m, n) = (1, 0), (2, 0)
+        ds = float(np.sum(dX * modes[p]))
+        fd = (solve(m.X + eps * modes[p])[2][0] - solve(m.X - eps * modes[p])[2][0]) / (2 * eps)
+        assert abs(ds - fd) <= 1e-4 * abs(fd), (p, ds, fd)

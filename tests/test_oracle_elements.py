@@ -73,3 +73,31 @@ def test_element_xpt_products_match_reference(name, order, nl):
         assert rel(GX, f["GX"][s].reshape(-1)) < 2e-8, (name, s)
         assert rel(GX, f["GX_cs"][s].reshape(-1)) < 5e-5, (name, s)
     assert f["KX"].shape == (f["X"].shape[0], nn, 3)
+
+
+@pytest.mark.parametrize("name,order,nl", TYPES)
+def test_element_state_and_residual_products_match_reference(name, order, nl):
+    """d(psi^T M phi)/d(vars) for K and G (TACSElement::
+    getMatSVSensInnerProduct) and psi^T dR/dX (addAdjResXptProduct): the
+    oracle's central differences (dh = 1e-7) against the reference's
+    real-mode values (same formula) and its complex-step values."""
+    f = np.load(os.path.join(GOLDEN, f"elements_{name}.npz"))
+    for s in range(f["X"].shape[0]):
+        E, nu, t, alpha, temp, _ = f["params"][s]
+        if temp != 0.0:
+            continue
+        m = oracle.Material.iso(E, nu, t, alpha, temp)
+        X, v = f["X"][s], f["vars"][s]
+        psi, phi = f["xs_psi"][s], f["xs_phi"][s]
+        KU = oracle.element_sv_inner_product(order, nl, oracle.STIFFNESS, m, X, v, psi, phi)
+        if nl:
+            assert rel(KU, f["KU"][s]) < 2e-8, (name, s)
+            assert rel(KU, f["KU_cs"][s]) < 2e-8, (name, s)
+        else:  # the linear tangent does not depend on the state
+            assert not KU.any() and not f["KU"][s].any() and not f["KU_cs"][s].any()
+        GU = oracle.element_sv_inner_product(order, nl, oracle.GEOMETRIC, m, X, v, psi, phi)
+        assert rel(GU, f["GU"][s]) < 2e-8, (name, s)
+        assert rel(GU, f["GU_cs"][s]) < 1e-6, (name, s)
+        RX = oracle.element_adjres_xpt_product(order, nl, m, X, v, psi)
+        assert rel(RX, f["RX"][s].reshape(-1)) < 2e-8, (name, s)
+        assert rel(RX, f["RX_cs"][s].reshape(-1)) < 5e-8, (name, s)
