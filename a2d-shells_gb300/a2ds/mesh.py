@@ -131,6 +131,95 @@ def radial_shape_modes(m: ShellMesh, mmax: int = 8, nmax: int = 8) -> np.ndarray
     return out
 
 
+def stiffened_panel(nx: int, ny: int, nz: int, order: int = 3, Lx: float = 2.0,
+                    Ly: float = 0.6, H: float = 0.06, nstiff: int = 8, E: float = 70e9,
+                    nu: float = 0.3, load: float = 1e3, tmin: float = 2e-3, tmax: float = 20e-3,
+                    nseg: int = 20, nlanes_skin: int = 12,
+                    seed: int = DEFAULT_SEED) -> ShellMesh:
+    """Flat skin Lx x Ly (x-y plane) with `nstiff` blade webs of height H in
+    x-z planes at y_k = Ly (2k+1) / (2 nstiff), sharing the skin's nodes
+    along their roots.  nx x ny skin elements, nx x nz elements per web.
+
+    Thickness design groups g = L * a + lane with L = nlanes_skin + nstiff
+    lanes, a = the element's axial segment (nseg equal
+    segments of x), lane = its skin strip (nlanes_skin equal strips of y) or
+    nlanes_skin + k for web k; t_g ~ U[tmin, tmax] from `seed`.
+    Supports: x = 0 edge u = v = w = 0, x = Lx edge v = w = 0, skin y-edges
+    w = 0; the x = Lx edge (skin and webs) carries a uniform compressive line
+    load `load` [N/m] along -x as consistent nodal forces."""
+    p = order - 1
+    nxn, nyn, nzn = nx * p + 1, ny * p + 1, nz * p
+    if (ny * p) % (2 * nstiff):
+        raise ValueError("the skin needs node lines at the web roots: "
+                         "(order - 1) * ny must be a multiple of 2 * nstiff")
+    rng = np.random.default_rng(seed)
+    nlanes = nlanes_skin + nstiff
+    tvals = rng.uniform(tmin, tmax, size=nseg * nlanes)
+    xs = np.linspace(0.0, Lx, nxn)
+    ys = np.linspace(0.0, Ly, nyn)
+    zs = np.linspace(0.0, H, nzn + 1)
+
+    def skin(ix, iy):
+        return ix * nyn + iy
+    nskin = nxn * nyn
+    root = [(2 * k + 1) * (ny * p) // (2 * nstiff) for k in range(nstiff)]
+
+    def web(k, ix, iz):
+        if iz == 0:
+            return skin(ix, root[k])
+        return nskin + (k * nxn + ix) * nzn + (iz - 1)
+    nn = nskin + nstiff * nxn * nzn
+    X = np.zeros((nn, 3))
+    for ix in range(nxn):
+        for iy in range(nyn):
+            X[skin(ix, iy)] = (xs[ix], ys[iy], 0.0)
+        for k in range(nstiff):
+            for iz in range(1, nzn + 1):
+                X[web(k, ix, iz)] = (xs[ix], ys[root[k]], zs[iz])
+    conn, group = [], []
+
+    def seg(xc):
+        return min(int(xc / (Lx / nseg)), nseg - 1)
+    for ex in range(nx):
+        for ey in range(ny):
+            conn.append([skin(ex * p + a, ey * p + b) for b in range(order) for a in range(order)])
+            xc, yc = (ex + 0.5) * Lx / nx, (ey + 0.5) * Ly / ny
+            group.append(nlanes * seg(xc) + min(int(yc / (Ly / nlanes_skin)), nlanes_skin - 1))
+    for k in range(nstiff):
+        for ex in range(nx):
+            for ez in range(nz):
+                conn.append([web(k, ex * p + a, ez * p + b) for b in range(order)
+                             for a in range(order)])
+                group.append(nlanes * seg((ex + 0.5) * Lx / nx) + nlanes_skin + k)
+    conn = np.array(conn, dtype=np.int32)
+    group = np.array(group, dtype=np.int32)
+
+    mask = np.zeros(nn, dtype=np.int32)
+    mask[np.abs(X[:, 0]) < 1e-12] |= 0b111
+    mask[np.abs(X[:, 0] - Lx) < 1e-12] |= 0b110
+    for ix in range(nxn):
+        mask[skin(ix, 0)] |= 0b100
+        mask[skin(ix, nyn - 1)] |= 0b100
+    bc_nodes = np.nonzero(mask)[0].astype(np.int32)
+    bc_mask = mask[bc_nodes]
+    bc_vals = np.zeros((bc_nodes.size, 6))
+
+    rhs = np.zeros((nn, 6))
+    gp, gw = _G3
+    N = _lagrange_lobatto(order, gp)
+    for ey in range(ny):
+        for a in range(order):
+            rhs[skin(nx * p, ey * p + a), 0] -= load * 0.5 * (Ly / ny) * np.sum(gw * N[:, a])
+    for k in range(nstiff):
+        for ez in range(nz):
+            for a in range(order):
+                rhs[web(k, nx * p, ez * p + a), 0] -= load * 0.5 * (H / nz) * np.sum(gw * N[:, a])
+    return ShellMesh(X=X, conn=conn, bc_nodes=bc_nodes, bc_mask=bc_mask, bc_vals=bc_vals,
+                     rhs=rhs, thickness=tvals[group], dv_group=group, E=E, nu=nu, order=order,
+                     meta=dict(kind="stiffened_panel", nx=nx, ny=ny, nz=nz, Lx=Lx, Ly=Ly, H=H,
+                               nstiff=nstiff, load=load, seed=seed, tvals=tvals))
+
+
 def classical_cylinder_load(E: float, nu: float, t: float, R: float) -> float:
     """Classical axial buckling load per unit circumference, E t^2/(R sqrt(3(1-nu^2)))."""
     return E * t * t / (R * np.sqrt(3.0 * (1.0 - nu * nu)))

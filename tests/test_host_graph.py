@@ -2,7 +2,7 @@
 
 No GPU is needed: a2ds_mesh_plan builds the node-to-node pattern, the AMD
 ordering, the BCSR pattern and the ILU(k) pattern on the host.  The expected
-arrays come from the reference (tests/golden/cyl_*.npz):
+arrays come from the reference (tests/golden/cyl_*.npz, panel_*.npz):
 computeLocalNodeToNodeCSR, amd_order_interface, the TACSSchurMat B pattern
 and BCSRMat(comm, B, levFill, fill).
 """
@@ -15,7 +15,7 @@ import pytest
 from conftest import GOLDEN
 from a2ds import capi
 
-CASES = ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu"]
+CASES = ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu", "panel_q9_4x8x1_lu"]
 
 
 def test_library_exports_every_declared_symbol():
