@@ -1,0 +1,123 @@
+"""Dense CPU restatement of the buckling eigenvalue coordinate sensitivities
+-- TEST INFRASTRUCTURE (imported by tests/ only).
+
+The formula is the body of the reference's commented-out
+TACSLinearBuckling::evalEigenXptSens (src/TACSBuckling.cpp:457-497):
+
+  dlam/dX = -[phi^T K' phi + lam phi^T G'(u) phi - lam psi^T (K u)'] / phi^T G phi,
+  K psi = d(phi^T G(u) phi)/du,
+
+with the element derivatives of TACSElement::addMatXptSensInnerProduct,
+getMatSVSensInnerProduct and addAdjResXptProduct (src/elements/
+TACSElement.cpp:270-581; central differences, dh = 1e-7) from the oracle's
+element routines, and dense FP64 linear algebra for the solves.  About a
+nonlinear preloaded state R(u, X) = s f the same formula holds with the
+tangent K_T(u) in place of K and psi^T R' in place of psi^T (K u)'.
+Sizes: a few hundred nodes (dense matrices).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import (GEOMETRIC, STIFFNESS, Material, element_adjres_xpt_product, element_jacobian,
+               element_matrix, element_sv_inner_product, element_xpt_inner_product)
+
+
+def _dofs(c):
+    return (6 * np.asarray(c)[:, None] + np.arange(6)).ravel()
+
+
+class DenseShell:
+    """One-thickness shell mesh (a2ds.mesh.ShellMesh) on dense matrices."""
+
+    def __init__(self, m, nonlinear=False):
+        self.m, self.order, self.nl = m, m.order, int(nonlinear)
+        self.mat = Material.iso(m.E, m.nu, float(m.thickness[0]))
+        self.N = 6 * m.X.shape[0]
+        self.free = np.ones(self.N, bool)
+        for node, mask in zip(m.bc_nodes, m.bc_mask):
+            for k in range(6):
+                if int(mask) >> k & 1:
+                    self.free[6 * node + k] = False
+
+    def matrix(self, X, kind, u):
+        A = np.zeros((self.N, self.N))
+        for c in self.m.conn:
+            d = _dofs(c)
+            A[np.ix_(d, d)] += element_matrix(self.order, self.nl, kind, self.mat, X[c], u[d])
+        return A
+
+    def tangent(self, X, u):
+        A, R = np.zeros((self.N, self.N)), np.zeros(self.N)
+        for c in self.m.conn:
+            d = _dofs(c)
+            r, J = element_jacobian(self.order, self.nl, self.mat, X[c], u[d])
+            A[np.ix_(d, d)] += J
+            R[d] += r
+        return A, R
+
+    def state(self, X, load=None, nsteps=4, rtol=1e-11):
+        """Linear path K u = f (load None) or Newton load stepping to
+        load * f with the full tangent (nonlinear elements)."""
+        f = self.m.rhs.ravel()
+        fr = self.free
+        u = np.zeros(self.N)
+        if load is None:
+            K = self.matrix(X, STIFFNESS, u)
+            u[fr] = np.linalg.solve(K[np.ix_(fr, fr)], f[fr])
+            return u
+        for k in range(1, nsteps + 1):
+            fk = load * k / nsteps * f
+            for _ in range(40):
+                KT, R = self.tangent(X, u)
+                r = (R - fk)[fr]
+                if np.linalg.norm(r) <= rtol * np.linalg.norm(fk[fr]):
+                    break
+                u[fr] -= np.linalg.solve(KT[np.ix_(fr, fr)], r)
+            else:
+                raise RuntimeError("Newton did not converge")
+        return u
+
+    def buckling(self, X, u):
+        """K(u) phi + lam G(u) phi = 0 on the free DOFs, loads by magnitude;
+        K(u) is the tangent at u (K itself for linear elements)."""
+        import scipy.linalg as sla
+        fr = self.free
+        K = self.tangent(X, u)[0] if self.nl else self.matrix(X, STIFFNESS, u)
+        G = self.matrix(X, GEOMETRIC, u)
+        Kf, Gf = K[np.ix_(fr, fr)], G[np.ix_(fr, fr)]
+        mu, V = sla.eigh(-0.5 * (Gf + Gf.T), 0.5 * (Kf + Kf.T))
+        order = np.argsort(-np.abs(mu))
+        lam = 1.0 / mu[order]
+        phi = np.zeros((self.N, lam.size))
+        phi[fr] = V[:, order]
+        return lam, phi, K, G
+
+    def xpt_sens(self, X, u, lam, phi, K, G, dh=1e-7):
+        """dlam/dX (nodes x 3) of one load with eigenvector phi."""
+        o, nl, mat = self.order, self.nl, self.mat
+        fr = self.free
+        g = np.zeros(self.N)
+        for c in self.m.conn:
+            d = _dofs(c)
+            g[d] += lam * element_sv_inner_product(o, nl, GEOMETRIC, mat, X[c], u[d], phi[d],
+                                                   phi[d], dh)
+            if nl:
+                g[d] += element_sv_inner_product(o, nl, STIFFNESS, mat, X[c], u[d], phi[d],
+                                                 phi[d], dh)
+        psi = np.zeros(self.N)
+        psi[fr] = np.linalg.solve(K[np.ix_(fr, fr)], g[fr])
+        out = np.zeros((self.N // 6, 3))
+        nn = len(self.m.conn[0])
+        for c in self.m.conn:
+            d = _dofs(c)
+            v = (element_xpt_inner_product(o, nl, STIFFNESS, mat, X[c], u[d], phi[d], phi[d], dh)
+                 + lam * element_xpt_inner_product(o, nl, GEOMETRIC, mat, X[c], u[d], phi[d],
+                                                   phi[d], dh))
+            if nl:
+                v -= element_adjres_xpt_product(o, nl, mat, X[c], u[d], psi[d], dh)
+            else:  # R = K u for the linear element: psi^T (K u)'
+                v -= element_xpt_inner_product(o, nl, STIFFNESS, mat, X[c], u[d], psi[d], u[d],
+                                               dh)
+            out[c] += v.reshape(nn, 3)
+        return -out / float(phi @ G @ phi)

