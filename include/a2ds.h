@@ -293,7 +293,7 @@ typedef struct {
 } a2ds_buckling_opts;
 
 /* Fills opts with the defaults (sigma = 0, 100 vectors, 10 eigenvalues,
-   tol 1e-10, complete LU, GMRES(30, 15) at 1e-12, FP64, block size 8). */
+   tol 1e-10, complete LU, GMRES(30, 15) at 1e-12, FP64, block size 4). */
 void a2ds_buckling_default_opts(a2ds_buckling_opts *opts);
 
 /* TACSLinearBuckling::solve(rhs, NULL) (src/TACSBuckling.cpp:197-278) and
