@@ -237,14 +237,19 @@ def make_bdf():
 
 def make_f5():
     """.f5 files written by the reference's TACSToFH5 for a Quad4 and a Quad9
-    cylinder with two components and a seeded variable vector, for nine
+    cylinder and a Quad9 stiffened panel (skin and webs), each with two
+    components and a seeded variable vector, for nine
     output-class flags (node, element and load classes); stored as raw
     bytes in f5.npz with the inputs."""
     rng = np.random.default_rng(11)
     out = {}
     for name, m in {"q4": meshgen.cylinder(4, 8, order=2),
-                    "q9": meshgen.cylinder(2, 4, order=3)}.items():
-        comp = (np.arange(m.num_elements) % 3 == 1).astype(np.int32)
+                    "q9": meshgen.cylinder(2, 4, order=3),
+                    "panel": meshgen.stiffened_panel(2, 8, 1)}.items():
+        if name == "panel":  # skin and webs as the two components
+            comp = (np.arange(m.num_elements) >= 2 * 8).astype(np.int32)
+        else:
+            comp = (np.arange(m.num_elements) % 3 == 1).astype(np.int32)
         vars_ = rng.standard_normal((m.num_nodes, 6)) * 1e-3
         with tempfile.TemporaryDirectory() as d:
             ind, outd = os.path.join(d, "in"), os.path.join(d, "out")

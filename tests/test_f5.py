@@ -1,7 +1,8 @@
 """.f5 output (TACSToFH5::writeToFile, src/io/TACSToFH5.cpp:126, through
 TACSFH5File) against files the reference itself wrote (tests/golden/f5.npz,
 oracle/ref/golden_gen.cpp f5 mode): byte-identical for a Quad4 and a Quad9
-mesh with two named components, for the connectivity, node and
+cylinder and a Quad9 stiffened panel (skin and blade webs) with two named
+components, for the connectivity, node and
 displacement output classes alone and together (CPU); with the load and
 element classes (computed on the GPU) the layout is byte-identical and the
 values agree to FP32 rounding (GPU)."""
@@ -17,7 +18,7 @@ FLAGS = [capi.A2DS_F5_CONNECTIVITY | capi.A2DS_F5_NODES | capi.A2DS_F5_DISPLACEM
          capi.A2DS_F5_NODES, capi.A2DS_F5_DISPLACEMENTS, capi.A2DS_F5_CONNECTIVITY]
 
 
-@pytest.mark.parametrize("mesh", ["q4", "q9"])
+@pytest.mark.parametrize("mesh", ["q4", "q9", "panel"])
 @pytest.mark.parametrize("flag", FLAGS)
 def test_f5_bytes_match_reference(mesh, flag, tmp_path):
     g = np.load(os.path.join(GOLDEN, "f5.npz"))
