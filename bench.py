@@ -275,6 +275,17 @@ def run_reference(args):
     return 0
 
 
+def max_over_ranks(times, dist=None):
+    """Each timing's maximum over the ranks of the process group (the
+    replicas' slowest); the values themselves without a group."""
+    if dist is None:
+        return [float(x) for x in times]
+    import torch
+    t = torch.tensor([float(x) for x in times], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def workload_config(m, args):
     return {
         "workload": (f"cylinder {args.nx}x{args.ny} Quad4 MITC shell, {6 * m.num_nodes} DOF, "
@@ -356,13 +367,7 @@ def main():
     clk = clocks.stop()
 
     ms = sum(ev_ms) / len(ev_ms)
-    t_rank = sum(ev_ms) / 1000.0
-    t_e2e = sum(e2e_wall)
-    if dist:
-        import torch
-        t = torch.tensor([t_rank, t_e2e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_rank, t_e2e = float(t[0]), float(t[1])
+    t_rank, t_e2e = max_over_ranks([sum(ev_ms) / 1000.0, sum(e2e_wall)], dist)
     value = world * args.steps / t_rank
     e2e_value = world * args.steps / t_e2e
     if rank != 0:
