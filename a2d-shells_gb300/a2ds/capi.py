@@ -50,6 +50,7 @@ EXPORTS = [
     "a2ds_add_mat_xpt_sens_inner_product", "a2ds_add_adjoint_res_xpt_sens_product",
     "a2ds_eval_mat_sv_sens_inner_product", "a2ds_eig_sens_xpts",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
+    "a2ds_bcsr_time_mult",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
     "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
     "a2ds_buckling_stats", "a2ds_eig_sens_thickness", "a2ds_eigen_shift_invert",
@@ -139,6 +140,7 @@ def load(build: bool = False):
     lib.a2ds_eigen_shift_invert.argtypes = [VP, ctypes.POINTER(BucklingOpts), VP, VP, P_D, P_D,
                                             P_D]
     lib.a2ds_eig_sens_thickness.argtypes = [VP, ctypes.c_int, P_D]
+    lib.a2ds_bcsr_time_mult.argtypes = [VP, ctypes.c_int, ctypes.c_int, P_D]
     lib.a2ds_eig_sens_xpts.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
     lib.a2ds_add_mat_xpt_sens_inner_product.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D,
                                                         P_D, P_D, ctypes.c_double, P_D]
@@ -338,6 +340,13 @@ class BCSRMat:
             self.lib.a2ds_bcsr_destroy(self.h)
             self.h = None
 
+    def sizes(self):
+        """(block rows, 6x6 blocks)"""
+        nr, nz = ctypes.c_int(), ctypes.c_int()
+        _check(self.lib.a2ds_bcsr_get(self.h, ctypes.byref(nr), ctypes.byref(nz), None, None,
+                                      None))
+        return nr.value, nz.value
+
     def get_arrays(self):
         nr, nz = ctypes.c_int(), ctypes.c_int()
         _check(self.lib.a2ds_bcsr_get(self.h, ctypes.byref(nr), ctypes.byref(nz), None, None,
@@ -357,6 +366,12 @@ class BCSRMat:
         y = np.zeros_like(x)
         _check(self.lib.a2ds_bcsr_mult(self.h, _d(x), _d(y)))
         return y
+
+    def time_mult(self, nvec=1, iters=20):
+        """Device milliseconds per product with nvec device-resident vectors."""
+        ms = ctypes.c_double(0.0)
+        _check(self.lib.a2ds_bcsr_time_mult(self.h, int(nvec), int(iters), ctypes.byref(ms)))
+        return ms.value
 
     def mult_rows(self, x, noalloc=False):
         """y = A x with x, y in the matrix (row) ordering; noalloc=True uses

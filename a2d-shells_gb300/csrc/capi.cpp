@@ -8,6 +8,7 @@
 
 #include "a2ds.h"
 #include "a2ds_internal.h"
+#include "block.h"
 #include "host_graph.h"
 #include "kernels.h"
 #include "runtime.h"
@@ -437,6 +438,48 @@ int a2ds_bcsr_mult_rows(a2ds_bcsr A, const double *x, double *y) {
     return rc;
   A2DS_CUDA_TRY(cudaMemcpyAsync(y, dy.p, dy.n * sizeof(double), cudaMemcpyDeviceToHost, m.stream));
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  return 0;
+  A2DS_GUARD_END
+}
+
+int a2ds_bcsr_time_mult(a2ds_bcsr A, int nvec, int iters, double *ms_per_mult) {
+  A2DS_GUARD_BEGIN
+  if (!A || !ms_per_mult) return fail(A2DS_ERR_ARG, "null argument");
+  if (iters < 1 || iters > 100000) return fail(A2DS_ERR_ARG, "iters must be in [1, 100000]");
+  if (nvec != 1 && nvec != 2 && nvec != 4 && nvec != 8 && nvec != 16)
+    return fail(A2DS_ERR_ARG, "nvec must be 1, 2, 4, 8 or 16");
+  Mesh &m = A->mesh->m;
+  const size_t n = (size_t)m.nn * 6 * nvec;
+  DBuf<double> dx, dy;
+  int rc;
+  if ((rc = dx.alloc(n)) || (rc = dy.alloc(n))) return rc;
+  A2DS_CUDA_TRY(cudaMemsetAsync(dx.p, 0, n * sizeof(double), m.stream));
+  auto mult = [&]() {
+    return nvec == 1 ? launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, A->vals.p, dx.p, dy.p,
+                                       m.stream)
+                     : blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, A->vals.p, dx.p, nullptr, dy.p,
+                                nvec, m.stream);
+  };
+  for (int w = 0; w < 3; w++)
+    if ((rc = mult())) return rc;
+  cudaEvent_t e0, e1;
+  A2DS_CUDA_TRY(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(A2DS_ERR_CUDA, "cudaEventCreate failed");
+  }
+  float ms = 0.0f;
+  cudaEventRecord(e0, m.stream);
+  for (int it = 0; it < iters && !rc; it++) rc = mult();
+  cudaEventRecord(e1, m.stream);
+  cudaError_t e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(A2DS_ERR_CUDA, cudaGetErrorString(e));
+  m.launches += iters + 3;
+  *ms_per_mult = (double)ms / iters;
   return 0;
   A2DS_GUARD_END
 }

@@ -275,6 +275,29 @@ def run_reference(args):
     return 0
 
 
+def spmv_roofline(capi, a, m, hbm, iters=50):
+    """K times 1 and 4 device-resident vectors (the path's and the block
+    Lanczos' product), timed with CUDA events after the timed region;
+    algorithmic bytes nnzb (36 x 8 + 4) + (nn + 1) 4 + 2 (6 nn 8) p."""
+    try:
+        K = a.create_mat()
+        a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
+        nnzb = K.sizes()[1]
+        out = {"matrix": f"K, {nnzb} 6x6 FP64 blocks, {m.num_nodes} block rows",
+               "l2": "no flush: the matrix exceeds the 129 MB L2"}
+        for p in (1, 4):
+            ms = K.time_mult(p, iters)
+            nbytes = nnzb * (36 * 8 + 4) + (m.num_nodes + 1) * 4 + 2 * 6 * m.num_nodes * 8 * p
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            out[f"p{p}"] = {"kernel": "k_bcsr_spmv" if p == 1 else f"k_blk_spmm<{p}>",
+                            "ms": ms, "bytes": nbytes, "achieved_gbs": gbs,
+                            "frac_of_measured_hbm": (gbs / hbm) if hbm else None,
+                            "fp64_tflops": 72.0 * nnzb * p / (ms * 1e-3) / 1e12}
+        return out
+    except Exception as ex:  # reported beside the headline, never in place of it
+        return {"error": str(ex)[:200]}
+
+
 def max_over_ranks(times, dist=None):
     """Each timing's maximum over the ranks of the process group (the
     replicas' slowest); the values themselves without a group."""
@@ -446,6 +469,7 @@ def main():
         "eig_rel_err_vs_fp64": vs_fp64, "fp64_variant": fp64_variant,
         "clocks": clk,
     }
+    line["spmv"] = spmv_roofline(capi, a, m, hbm)
     if not args.no_cpu_baseline and world == 1:
         try:
             v, det = cpu_sample(m, args.nx, args.ny, args.neig)

@@ -223,6 +223,13 @@ int a2ds_bcsr_mult_rows_noalloc(a2ds_bcsr A, const double *x, double *y);
 
 /* BCSRMat::copyValues (src/bpmat/BCSRMat.cpp:2375): Y <- X;
    BCSRMat::axpy (:2430): Y <- Y + alpha X; same pattern required. */
+/* Device time of the matrix product on device-resident vectors: y = A x
+   (nvec = 1, BCSRMatVecMult6, src/bpmat/BCSRMatMult6.cpp:82-122) or A times
+   nvec stacked vectors (2, 4, 8, 16; the block Lanczos product), averaged
+   over iters launches after 3 warm-up launches, CUDA events on the mesh's
+   stream.  No counterpart in the reference (a measurement entry). */
+int a2ds_bcsr_time_mult(a2ds_bcsr A, int nvec, int iters, double *ms_per_mult);
+
 int a2ds_bcsr_copy(a2ds_bcsr Y, a2ds_bcsr X);
 int a2ds_bcsr_axpy(a2ds_bcsr Y, double alpha, a2ds_bcsr X);
 

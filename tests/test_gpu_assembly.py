@@ -197,3 +197,25 @@ def test_mesh_assembly_matches_oracle_elementwise():
         idx = (6 * nodes[:, None] + np.arange(6)[None, :]).ravel()
         ref[np.ix_(idx, idx)] += Ke
     assert rel(K.to_dense_nodes(), ref) < 1e-12
+
+
+@pytest.mark.gpu
+def test_bcsr_time_mult():
+    """The measurement entry behind bench.py's SpMV figures: positive device
+    times for 1 and 4 vectors, argument checks."""
+    f = np.load(os.path.join(GOLDEN, "cyl_q4_8x16_ilu1.npz"))
+    a = capi.Assembler(f["X"], f["conn"])
+    a.set_material(float(f["E"]), float(f["nu"]))
+    a.set_thickness(f["thickness"][:1])
+    a.add_bcs(f["bc_nodes"], f["bc_mask"], f["bc_vals"])
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    K = a.create_mat()
+    a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
+    assert K.sizes() == (f["bcsr_rowp"].size - 1, f["bcsr_cols"].size)
+    for p in (1, 4):
+        ms = K.time_mult(p, 5)
+        assert np.isfinite(ms) and ms > 0.0
+    with pytest.raises(capi.A2dsError):
+        K.time_mult(3, 5)
+    with pytest.raises(capi.A2dsError):
+        K.time_mult(1, 0)
