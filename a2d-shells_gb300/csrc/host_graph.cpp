@@ -76,13 +76,75 @@ void greedy_element_colors(int nn, int ne, int npe, const int *conn, std::vector
 }
 
 // ------------------------------------------------------------------ ILU(k)
+// Complete fill (levFill >= n - 1: no fill entry has a higher level) of a
+// structurally symmetric pattern.  computeILUk then produces the filled
+// graph of symmetric elimination in this order, which is computed here
+// column by column along the elimination tree: the upper structure of
+// column j is its own upper entries and those of its children (the columns
+// whose first upper entry is j), O(fill) instead of O(block updates).  The
+// lower part of row i is the transpose.  Returns false (nothing written)
+// when the pattern is not symmetric.
+static bool complete_fill_symbolic(int n, const std::vector<int> &rowp,
+                                   const std::vector<int> &cols, std::vector<int> &frowp,
+                                   std::vector<int> &fcols, std::vector<int> &fdiag) {
+  for (int i = 0; i < n; i++)
+    for (int q = rowp[i]; q < rowp[i + 1]; q++) {
+      const int c = cols[q];
+      if (c < 0 || c >= n ||
+          !std::binary_search(cols.begin() + rowp[c], cols.begin() + rowp[c + 1], i))
+        return false;
+    }
+  std::vector<std::vector<int>> U(n);
+  std::vector<int> mark(n, -1), child_head(n, -1), child_next(n, -1);
+  for (int j = 0; j < n; j++) {
+    std::vector<int> &u = U[j];
+    mark[j] = j;
+    for (int q = rowp[j]; q < rowp[j + 1]; q++) {
+      const int c = cols[q];
+      if (c > j && mark[c] != j) {
+        mark[c] = j;
+        u.push_back(c);
+      }
+    }
+    for (int ch = child_head[j]; ch >= 0; ch = child_next[ch])
+      for (int c : U[ch])
+        if (mark[c] != j) {  // every entry of a child's column is >= j
+          mark[c] = j;
+          u.push_back(c);
+        }
+    std::sort(u.begin(), u.end());
+    if (!u.empty()) {
+      child_next[j] = child_head[u[0]];
+      child_head[u[0]] = j;
+    }
+  }
+  std::vector<int> lcount(n, 0);
+  for (int k = 0; k < n; k++)
+    for (int c : U[k]) lcount[c]++;
+  frowp.assign(n + 1, 0);
+  for (int i = 0; i < n; i++) frowp[i + 1] = frowp[i] + lcount[i] + 1 + (int)U[i].size();
+  fcols.assign(frowp[n], 0);
+  fdiag.assign(n, 0);
+  std::vector<int> pos(frowp.begin(), frowp.end() - 1);
+  for (int k = 0; k < n; k++)
+    for (int c : U[k]) fcols[pos[c]++] = k;  // ascending k: sorted lower parts
+  for (int i = 0; i < n; i++) {
+    fdiag[i] = frowp[i] + lcount[i];
+    fcols[fdiag[i]] = i;
+    std::copy(U[i].begin(), U[i].end(), fcols.begin() + fdiag[i] + 1);
+  }
+  return true;
+}
+
 // Row-by-row level-of-fill symbolic factorization: lev(i, j) is the minimum
 // over eliminated k < i of lev(i, k) + lev(k, j) + 1 (original entries have
 // level 0); entries with lev <= lev_fill are kept.  The working row is a
 // sorted singly linked list over column indices so fill can be merged in
-// while the row is being eliminated left to right.
+// while the row is being eliminated left to right.  Complete fill of a
+// symmetric pattern takes the elimination-tree path above (same pattern).
 int ilu_symbolic(int n, const std::vector<int> &rowp, const std::vector<int> &cols, int lev_fill,
                  std::vector<int> &frowp, std::vector<int> &fcols, std::vector<int> &fdiag) {
+  if (lev_fill >= n - 1 && complete_fill_symbolic(n, rowp, cols, frowp, fcols, fdiag)) return 0;
   frowp.assign(n + 1, 0);
   fcols.clear();
   fdiag.assign(n, 0);

@@ -99,3 +99,21 @@ def test_amd_order_type_equals_tacs_amd_and_nd_is_refused():
     b = capi.Assembler(f["X"], f["conn"])
     with pytest.raises(capi.A2dsError, match="METIS"):
         b.plan(capi.A2DS_ND_ORDER)
+
+
+@pytest.mark.parametrize("order", [capi.A2DS_TACS_AMD_ORDER, capi.A2DS_RCM_ORDER,
+                                   capi.A2DS_NATURAL_ORDER, capi.A2DS_MULTICOLOR_ORDER])
+def test_complete_fill_paths_agree(order):
+    """Complete fill of a symmetric pattern takes the elimination-tree path;
+    levFill = n - 2 (still complete: no fill level exceeds the number of
+    intermediate rows) takes the row-by-row level-of-fill path of
+    computeILUk.  The two patterns are identical."""
+    from a2ds import mesh as meshgen
+    for m in (meshgen.cylinder(16, 32), meshgen.cylinder(4, 8, order=3),
+              meshgen.stiffened_panel(2, 8, 1)):
+        a = capi.Assembler(m.X, m.conn)
+        a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+        a.plan(order)
+        r1, c1 = a.ilu_pattern(1000000)
+        r2, c2 = a.ilu_pattern(m.num_nodes - 2)
+        assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
