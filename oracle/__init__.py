@@ -218,7 +218,7 @@ def assemble(mesh, kind, perm, rowp, cols, vars_=None, nonlinear=False, bc_rows=
     conn_rows = np.ascontiguousarray(iperm[conn], np.int32)
     X = np.ascontiguousarray(mesh.X, np.float64)
     v = None if vars_ is None else np.ascontiguousarray(vars_, np.float64)
-    tv = np.ascontiguousarray(np.unique(mesh.thickness) if False else mesh.thickness, np.float64)
+    tv = np.ascontiguousarray(mesh.thickness, np.float64)  # one group per element
     tg = np.arange(mesh.num_elements, dtype=np.int32)
     rowp = np.ascontiguousarray(rowp, np.int32)
     cols = np.ascontiguousarray(cols, np.int32)

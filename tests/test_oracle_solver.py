@@ -1,5 +1,6 @@
 """The CPU oracle's assembly, factorization, solves and buckling solve
-against the reference's own outputs (tests/golden/cyl_*.npz)."""
+against the reference's own outputs (tests/golden/cyl_*.npz and the
+stiffened panel, tests/golden/panel_q9_4x8x1_lu.npz)."""
 import os
 
 import numpy as np
@@ -34,7 +35,8 @@ def bc_rows(f, perm):
     return iperm[f["bc_nodes"]].astype(np.int32), f["bc_mask"].astype(np.int32)
 
 
-@pytest.mark.parametrize("case", ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu"])
+@pytest.mark.parametrize("case", ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu",
+                                  "panel_q9_4x8x1_lu"])
 def test_oracle_assembly_and_factor(case):
     f = np.load(os.path.join(GOLDEN, case + ".npz"))
     m = fixture_mesh(f)
