@@ -110,8 +110,8 @@ int element_data(a2ds_mesh mesh, int eflags, const double *vars, std::vector<flo
         // bottom surfaces (TACSIsoShellConstitutive::evalFailure, tOffset 0)
         double fail2[2];
         for (int side = 0; side < 2; side++) {
-          const double h = (side == 0 ? 0.5 : -0.5) * t;
-          const double es[3] = {o[0] + h * o[3], o[1] + h * o[4], o[2] + h * o[5]};
+          const double z = (side == 0 ? 0.5 : -0.5) * t;  // surface offset
+          const double es[3] = {o[0] + z * o[3], o[1] + z * o[4], o[2] + z * o[5]};
           const double sv[3] = {C[0] * es[0] + C[1] * es[1] + C[2] * es[2],
                                 C[1] * es[0] + C[3] * es[1] + C[4] * es[2],
                                 C[2] * es[0] + C[4] * es[1] + C[5] * es[2]};
