@@ -1116,7 +1116,6 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   BucklingState &S = *Sp;
   const int nev = opts->num_eigvals, p = opts->block_size;
   const size_t n6 = (size_t)m.nn * 6;
-  const size_t nv = (size_t)m.nnzb * 36;
   Blas B{m.stream};
   B.launches = &m.launches;
 
