@@ -131,6 +131,21 @@ def radial_shape_modes(m: ShellMesh, mmax: int = 8, nmax: int = 8) -> np.ndarray
     return out
 
 
+def seeded_shape_parameters(num: int = 64, scale: float = 1e-4, seed: int = DEFAULT_SEED):
+    """Seeded values s_p ~ scale * U[-1, 1] of the radial shape parameters."""
+    return scale * np.random.default_rng(seed + 5).uniform(-1.0, 1.0, size=num)
+
+
+def shaped_coordinates(m: ShellMesh, s, modes=None) -> np.ndarray:
+    """X + sum_p s_p dX/ds_p: the cylinder moved by the radial shape
+    parameters s (modes: radial_shape_modes(m) unless given).  The modes are
+    linear in s, so dlambda/ds_p = sum over nodes of dlambda/dX . modes[p]."""
+    if modes is None:
+        modes = radial_shape_modes(m)
+    s = np.asarray(s, dtype=np.float64)
+    return m.X + np.tensordot(s, modes[:s.size], axes=1)
+
+
 def stiffened_panel(nx: int, ny: int, nz: int, order: int = 3, Lx: float = 2.0,
                     Ly: float = 0.6, H: float = 0.06, nstiff: int = 8, E: float = 70e9,
                     nu: float = 0.3, load: float = 1e3, tmin: float = 2e-3, tmax: float = 20e-3,

@@ -158,3 +158,4 @@ def test_panel_thickness_sensitivities_vs_finite_difference():
         tm[g] -= h
         fd = (solve(tp)[1][0] - solve(tm)[1][0]) / (2 * h)
         assert abs(dl[g] - fd) <= 1e-4 * abs(fd) + 2e-6 * abs(lam[0]) / tv[g], (g, dl[g], fd)
+
