@@ -13,6 +13,10 @@ TACSElement.cpp:270-581; central differences, dh = 1e-7) from the oracle's
 element routines, and dense FP64 linear algebra for the solves.  About a
 nonlinear preloaded state R(u, X) = s f the same formula holds with the
 tangent K_T(u) in place of K and psi^T R' in place of psi^T (K u)'.
+The thickness derivative (the documented evalEigenDVSens formula,
+src/TACSBuckling.cpp:359-382) uses the same adjoint with the element
+matrices differentiated in the shell thickness (central differences of the
+oracle's element routines), for a one-thickness mesh.
 Sizes: a few hundred nodes (dense matrices).
 """
 from __future__ import annotations
@@ -121,3 +125,24 @@ class DenseShell:
                                                dh)
             out[c] += v.reshape(nn, 3)
         return -out / float(phi @ G @ phi)
+
+    def thickness_sens(self, X, u, lam, phi, K, G, rel_step=1e-6):
+        """dlam/dt for the mesh's single thickness t (linear elements):
+        -[phi^T K' phi + lam phi^T G'(u) phi - lam psi^T K' u] / phi^T G phi,
+        K psi = G(phi) phi, ' = d/dt by central differences of the element
+        matrices (they are polynomial in t)."""
+        fr = self.free
+        t0 = float(self.mat.t)
+        h = rel_step * t0
+        g = self.matrix(X, GEOMETRIC, phi) @ phi
+        psi = np.zeros(self.N)
+        psi[fr] = np.linalg.solve(K[np.ix_(fr, fr)], g[fr])
+        mats = []
+        for tt in (t0 + h, t0 - h):
+            self.mat = Material.iso(self.m.E, self.m.nu, tt)
+            mats.append((self.matrix(X, STIFFNESS, np.zeros(self.N)), self.matrix(X, GEOMETRIC, u)))
+        self.mat = Material.iso(self.m.E, self.m.nu, t0)
+        dK = (mats[0][0] - mats[1][0]) / (2 * h)
+        dG = (mats[0][1] - mats[1][1]) / (2 * h)
+        num = phi @ dK @ phi + lam * (phi @ dG @ phi) - lam * (psi @ dK @ u)
+        return -num / float(phi @ G @ phi)

@@ -4,7 +4,8 @@ oracle/sens.py from the oracle's element routines) against central
 differences of whole dense solves on moved meshes, for linear buckling and
 for buckling about a nonlinear preloaded state (4x8 Quad4 cylinders with a
 large imperfection, so the lowest load is simple), along axisymmetric
-radial shape modes; rigid motions leave the load unchanged."""
+radial shape modes; rigid motions leave the load unchanged.  The thickness
+derivative (the documented evalEigenDVSens formula) the same way."""
 import numpy as np
 import pytest
 
@@ -37,3 +38,25 @@ def test_dense_xpt_sensitivity_vs_finite_difference(nonlinear):
         d = float(np.sum(dX * modes[p]))
         fd = (solve(m.X + eps * modes[p])[1][0] - solve(m.X - eps * modes[p])[1][0]) / (2 * eps)
         assert abs(d - fd) <= 1e-4 * abs(fd), (p, d, fd)
+
+
+def test_dense_thickness_sensitivity_vs_finite_difference():
+    """The documented evalEigenDVSens formula (with the load-path adjoint)
+    restated densely, against central differences of whole solves in the
+    shell thickness."""
+    m = meshgen.cylinder(4, 8, imperfection=50.0)
+    t = float(m.thickness[0])
+    ds = DenseShell(m)
+    u = ds.state(m.X)
+    lam, phi, K, G = ds.buckling(m.X, u)
+    d = ds.thickness_sens(m.X, u, lam[0], phi[:, 0], K, G)
+
+    def load(tt):  # same coordinates and loads, thickness tt
+        import dataclasses
+        mm = dataclasses.replace(m, thickness=np.full_like(m.thickness, tt))
+        dd = DenseShell(mm)
+        uu = dd.state(mm.X)
+        return dd.buckling(mm.X, uu)[0][0]
+    h = 1e-6 * t
+    fd = (load(t + h) - load(t - h)) / (2 * h)
+    assert abs(d - fd) <= 1e-5 * abs(fd), (d, fd)
