@@ -69,3 +69,21 @@ def test_oracle_buckling_matches_reference(case):
     assert rel(cb.path, f["path"]) < 1e-9
     ref = f["eigvals"][:5]
     assert np.max(np.abs(lam - ref) / np.abs(ref)) < 1e-8, (lam, ref)
+
+
+def test_oracle_buckling_panel_lowest_load():
+    """The stiffened panel (Quad9 skin and webs): the reference ran 10
+    Lanczos steps (num_eigvals = 10, F3), which converge only the lowest
+    load; the oracle's path and lowest load agree with the reference's."""
+    f = np.load(os.path.join(GOLDEN, "panel_q9_4x8x1_lu.npz"))
+    m = fixture_mesh(f)
+    perm = f["amd_perm"].astype(np.int32)
+    br, bm = bc_rows(f, perm)
+    fr, fc = f["ilu_rowp"], f["ilu_cols"]
+    cb = oracle.CpuBuckling(m, perm, f["bcsr_rowp"], f["bcsr_cols"], fr, fc, diag_of(fr, fc),
+                            br, bm)
+    lam = cb.solve(float(f["sigma"]), f["rhs"], lanczos_iters=int(f["neig"]), num_eig=5,
+                   gm_m=int(f["gm_m"]), gm_restarts=int(f["gm_restarts"]))
+    assert rel(cb.path, f["path"]) < 1e-9
+    assert abs(lam[0] - f["eigvals"][0]) < 1e-8 * abs(f["eigvals"][0])
+    assert abs(lam[0] - f["eigvals_dense"][0]) < 1e-8 * abs(f["eigvals_dense"][0])
