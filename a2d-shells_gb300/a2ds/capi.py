@@ -52,7 +52,8 @@ EXPORTS = [
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_time_mult",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
-    "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
+    "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve",
+    "a2ds_fgmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
     "a2ds_buckling_stats", "a2ds_eig_sens_thickness", "a2ds_eigen_shift_invert",
     "a2ds_bdf_scan", "a2ds_bdf_destroy", "a2ds_bdf_get_sizes", "a2ds_bdf_get_connectivity",
     "a2ds_bdf_get_bcs", "a2ds_bdf_get_element_descript", "a2ds_bdf_get_component_descript",
@@ -132,6 +133,8 @@ def load(build: bool = False):
     lib.a2ds_pc_apply_multi.argtypes = [VP, ctypes.c_int, P_D, P_D]
     lib.a2ds_gmres_solve.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, P_D, P_D, P_I, P_D]
+    lib.a2ds_fgmres_solve.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_int, P_D, P_D, P_I]
     lib.a2ds_pc_get.argtypes = [VP, P_I, P_I, P_I, P_I, P_D]
     lib.a2ds_buckling_default_opts.argtypes = [ctypes.POINTER(BucklingOpts)]
     lib.a2ds_buckling_default_opts.restype = None
@@ -462,10 +465,28 @@ def gmres_solve(A: "BCSRMat", pc: "SchurPc", b, msub=30, nrestart=15, rtol=1e-12
     return x, it.value, rn.value
 
 
+def fgmres_solve(A: "BCSRMat", pc: "SchurPc", b, msub=24, nrestart=8, rtol=1e-10,
+                 raise_on_noconv=True):
+    """GMRES(mat, pc, msub, nrestart, isFlexible=1) as GMRES-IR: b is one
+    (num_nodes, 6) vector or a stack (nrhs, num_nodes, 6) of 1, 2, 4, 8 or 16;
+    returns (x, Arnoldi steps).  Convergence is judged on the FP64 residual."""
+    b = _f64(b)
+    single = b.ndim == 2
+    bb = np.ascontiguousarray(b.reshape(-1, A.a.num_nodes, 6) if not single else b[None])
+    x = np.zeros_like(bb)
+    it = ctypes.c_int()
+    rc = A.lib.a2ds_fgmres_solve(A.h, pc.h, int(msub), int(nrestart), float(rtol),
+                                 int(bb.shape[0]), _d(bb), _d(x), ctypes.byref(it))
+    if rc != 6 or raise_on_noconv:
+        _check(rc)
+    return (x[0] if single else x), it.value
+
+
 STAT_NAMES = ["total_s", "assemble_k_s", "assemble_g_s", "factor_s", "path_s", "lanczos_s",
               "lanczos_vectors", "inner_iters", "kernel_launches", "solve_event_ms",
               "factor_a_event_ms", "factor_k_event_ms", "factor_nnzb", "factor_levels",
-              "factor_flops", "block_size", "block_iters", "trisolve_ms", "trisolve_calls"]
+              "factor_flops", "block_size", "block_iters", "trisolve_ms", "trisolve_calls",
+              "gmres_ir_iters", "gmres_ir_cycles"]
 
 
 class LinearBuckling:

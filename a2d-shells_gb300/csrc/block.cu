@@ -253,6 +253,104 @@ int blk_combine(const double *Q, int nb, size_t bstride, int p, const double *C,
   return 0;
 }
 
+// ---------------------------------------------------- column-wise kernels
+// Each column of an n6 x p block carries its own Krylov space (p GMRES
+// solves in lockstep), so these kernels pair column c only with column c.
+// Grid strides are multiples of p (256-thread CTAs, p <= 16), so a thread
+// keeps one column for its whole walk.
+
+// out[b p + c] += sum_i Q_b[i][c] W[i][c] for b in [8 blockIdx.y, +8) and b < nb.
+__global__ void __launch_bounds__(256) k_col_dots(const double *__restrict__ Q, int nb,
+                                                  size_t bstride, const double *__restrict__ W,
+                                                  size_t n6, int p, double *__restrict__ out) {
+  __shared__ double red[8][8][16];
+  const int b0 = blockIdx.y * 8;
+  const int nbl = min(8, nb - b0);
+  double acc[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) acc[k] = 0.0;
+  const size_t total = n6 * p;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double w = W[e];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (k < nbl) acc[k] += Q[(size_t)(b0 + k) * bstride + e] * w;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    double v = acc[k];
+    for (int o = 16; o >= p; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane < p) red[wid][k][lane] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 8 * p) {
+    const int k = threadIdx.x / p, c = threadIdx.x % p;
+    if (k < nbl) {
+      double v = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w][k][c];
+      atomicAdd(&out[(size_t)(b0 + k) * p + c], v);
+    }
+  }
+}
+
+int col_dots(const double *Q, int nb, size_t bstride, const double *W, size_t n6, int p,
+             double *out, cudaStream_t s) {
+  if (p < 1 || p > 16 || (p & (p - 1))) return fail(A2DS_ERR_ARG, "block size must be 1..16, a power of 2");
+  if (nb < 1) return 0;
+  A2DS_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)nb * p * sizeof(double), s));
+  dim3 grid((unsigned)std::min<size_t>((n6 * p + 255) / 256, 152 * 4), (unsigned)((nb + 7) / 8));
+  k_col_dots<<<grid, 256, 0, s>>>(Q, nb, bstride, W, n6, p, out);
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// W[i][c] -= sum_b Q_b[i][c] h[b p + c]   (sign = -1), or
+// W[i][c] += sum_b Q_b[i][c] h[b p + c]   (sign = +1); h on the device.
+__global__ void __launch_bounds__(256) k_col_axpy(double *__restrict__ W,
+                                                  const double *__restrict__ Q, int nb,
+                                                  size_t bstride, const double *__restrict__ h,
+                                                  size_t n6, int p, double sign) {
+  __shared__ double sh[64 * 16];
+  for (int k = threadIdx.x; k < nb * p; k += blockDim.x) sh[k] = sign * h[k];
+  __syncthreads();
+  const size_t total = n6 * p;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e & (size_t)(p - 1));
+    double acc = 0.0;
+    for (int b = 0; b < nb; b++) acc += Q[(size_t)b * bstride + e] * sh[b * p + c];
+    W[e] += acc;
+  }
+}
+
+int col_axpy(double *W, const double *Q, int nb, size_t bstride, const double *h, size_t n6,
+             int p, double sign, cudaStream_t s) {
+  if (nb < 1) return 0;
+  if (nb > 64 || p > 16 || (p & (p - 1))) return fail(A2DS_ERR_ARG, "col_axpy: too many blocks");
+  k_col_axpy<<<grid_for(n6 * p), 256, 0, s>>>(W, Q, nb, bstride, h, n6, p, sign);
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// W[i][c] /= sqrt(nrm2[c]) (columns with nrm2[c] == 0 are left as they are).
+__global__ void k_col_unit(double *__restrict__ W, const double *__restrict__ nrm2, size_t n6,
+                           int p) {
+  const size_t total = n6 * p;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double q = nrm2[e & (size_t)(p - 1)];
+    if (q > 0.0) W[e] /= sqrt(q);
+  }
+}
+
+int col_unit(double *W, const double *nrm2, size_t n6, int p, cudaStream_t s) {
+  k_col_unit<<<grid_for(n6 * p), 256, 0, s>>>(W, nrm2, n6, p);
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 __global__ void k_blk_add(double *__restrict__ Y, const double *__restrict__ X, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)

@@ -26,4 +26,15 @@ int blk_combine(const double *Q, int nb, size_t bstride, int p, const double *C,
                 size_t n6, double *out, cudaStream_t s);
 // Y += X (n values).
 int blk_add(double *Y, const double *X, size_t n, cudaStream_t s);
+
+// Column-wise forms (column c of one block only meets column c of another;
+// p independent Krylov spaces in lockstep; p a power of 2 up to 16):
+// out[b p + c] = sum_i Q_b[i][c] W[i][c] for b < nb (out zeroed first).
+int col_dots(const double *Q, int nb, size_t bstride, const double *W, size_t n6, int p,
+             double *out, cudaStream_t s);
+// W[i][c] += sign * sum_b Q_b[i][c] h[b p + c], nb <= 64, h on the device.
+int col_axpy(double *W, const double *Q, int nb, size_t bstride, const double *h, size_t n6,
+             int p, double sign, cudaStream_t s);
+// W[i][c] /= sqrt(nrm2[c]) where nrm2[c] > 0 (nrm2 on the device).
+int col_unit(double *W, const double *nrm2, size_t n6, int p, cudaStream_t s);
 }  // namespace a2ds

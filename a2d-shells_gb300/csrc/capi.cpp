@@ -180,6 +180,7 @@ int a2ds_mesh_initialize(a2ds_mesh mesh, int order_type) {
   if (!m.planned && (rc = a2ds_mesh_plan(mesh, order_type))) return rc;
   if (!m.stream && cudaStreamCreateWithFlags(&m.stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(A2DS_ERR_CUDA, "cudaStreamCreate failed");
+  A2DS_CUDA_TRY(cudaGetDevice(&m.device));
   if ((rc = m.upload())) return rc;
   m.initialized = true;
   return 0;
@@ -430,6 +431,8 @@ int a2ds_bcsr_mult_rows(a2ds_bcsr A, const double *x, double *y) {
   A2DS_GUARD_BEGIN
   if (!A || !x || !y) return fail(A2DS_ERR_ARG, "null argument");
   Mesh &m = A->mesh->m;
+  if (!m.initialized || !m.d_rowp.p || !m.d_cols.p || !A->vals.p)
+    return fail(A2DS_ERR_STATE, "matrix of an uninitialized mesh");
   DBuf<double> dx, dy;
   int rc;
   if ((rc = dx.upload(x, (size_t)m.nn * 6, m.stream))) return rc;

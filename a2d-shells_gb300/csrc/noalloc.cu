@@ -13,10 +13,16 @@
 // every GPU that loads this library keeps it until the process exits.  Its
 // device address is looked up once per device, on the first call made with
 // that device current (cudaGetSymbolAddress); make that first call before
-// any stream capture.  All calls share the one array and it keeps the last
-// call's contents: both halves are fully overwritten by every call (x by
-// the host copy, y by the product), so nothing needs clearing, but calls
-// that overlap on the GPU race on it.
+// any stream capture.  The cached address belongs to the device's current
+// context: do not use this entry point across a device reset
+// (cudaDeviceReset) in the same process.  The device current at the call
+// must be the one the matrix's mesh was initialized on (the array of
+// another device would be staged through otherwise); a mismatch is
+// rejected.  All calls share the one array and it keeps the last call's
+// contents: the leading 6 n entries of both halves are overwritten by every
+// call (x by the host copy, y by the product) and nothing past them is
+// read, so nothing needs clearing, but calls that overlap on the GPU race
+// on it.
 #include <mutex>
 
 #include "a2ds_internal.h"
@@ -57,6 +63,13 @@ using namespace a2ds;
 extern "C" int a2ds_bcsr_mult_rows_noalloc(a2ds_bcsr A, const double *x, double *y) try {
   if (!A || !x || !y) return fail(A2DS_ERR_ARG, "null argument");
   Mesh &m = A->mesh->m;
+  if (!m.initialized || !m.d_rowp.p || !m.d_cols.p || !A->vals.p)
+    return fail(A2DS_ERR_STATE, "matrix of an uninitialized mesh");
+  int dev = -1;
+  A2DS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != m.device)
+    return fail(A2DS_ERR_ARG, "current device " + std::to_string(dev) +
+                                  " is not the mesh's device " + std::to_string(m.device));
   if (m.nn > A2DS_NOALLOC_MAX_ROWS)
     return fail(A2DS_ERR_ARG, "a2ds_bcsr_mult_rows_noalloc supports at most " +
                                   std::to_string(A2DS_NOALLOC_MAX_ROWS) + " block rows (matrix has " +

@@ -34,6 +34,7 @@ struct Mesh {
   std::vector<int> bc_rows;
 
   cudaStream_t stream = nullptr;
+  int device = -1;  // CUDA device current at initialize (the stream's device)
   DBuf<double> d_X, d_tvals, d_state, d_res;
   DBuf<int> d_conn, d_slots, d_rowp, d_cols, d_tgroup, d_bc_rows, d_bc_masks, d_color_elems;
   PinnedBuf<double> h_stage;  // pinned staging of node <-> row permuted vectors

@@ -58,6 +58,11 @@ __global__ void k_f64_to_f32(float *y, const double *x, size_t n) {
        i += (size_t)gridDim.x * blockDim.x)
     y[i] = (float)x[i];
 }
+__global__ void k_f32_to_f64(double *y, const float *x, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
 __global__ void k_add_f32(double *y, const float *x, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
@@ -394,6 +399,18 @@ static void inv_upper(int p, const std::vector<double> &R, std::vector<double> &
   }
 }
 
+// Krylov dimension and restart cycles of the GMRES-IR solves with an FP32
+// factor (restarts re-evaluate the FP64 residual).
+constexpr int GMRES_IR_MSUB = 24;
+constexpr int GMRES_IR_CYCLES = 8;
+
+// Work space of fgmres_block_solve: Arnoldi blocks V (msub + 1), the
+// preconditioned blocks Z (msub), small device coefficients H.
+struct IrWork {
+  DBuf<double> V, Z, H;
+  int iters = 0, cycles = 0;  // Arnoldi steps and cycles, accumulated
+};
+
 // --------------------------------------------------------- buckling state
 struct BucklingState {
   Factor fk, fa;
@@ -403,6 +420,11 @@ struct BucklingState {
   DBuf<double> dH1, dH2, dN, dM;  // small device scratch (coefficients)
   DBuf<double> phi, r, t, path, rhs;
   DBuf<float> w32;
+  // block FGMRES (GMRES-IR) work: Arnoldi blocks V, preconditioned blocks Z,
+  // small device coefficients; gw32 is the FP32 solve buffer (n6 x p floats,
+  // the path solve uses its leading n6 x 1)
+  IrWork ir;
+  DBuf<float> gw32;
   std::vector<double> lam, err, ritz;  // converged data
   int nconv = 0;
   double sigma = 0.0;
@@ -421,6 +443,9 @@ struct BucklingState {
     for (auto &e : tev)
       if (e) cudaEventDestroy(e);
   }
+  // the preconditioner of the GMRES-IR solves: the factor f through the
+  // fixed solve buffers, timed by an event pair like every other solve
+  int precond(Mesh &m, Factor &f, const double *V, double *Z, int p);
   cudaEvent_t next_event() {
     if (ntev == (int)tev.size()) {
       cudaEvent_t e = nullptr;
@@ -521,6 +546,165 @@ static int refined_block_solve(Mesh &m, BucklingState &S, Factor &f, const doubl
     m.launches++;
   }
   return 0;
+}
+
+// Z = M^{-1} V for a block of p vectors (row ordering) through the factor's
+// solve graph: an FP32 factor solves in FP32 (V rounded to FP32 into w32,
+// the result widened into Z), a double factor through the fixed xb / yb
+// buffers (the graph is keyed by its vectors, so they stay the same).
+static int precondition_block(Mesh &m, Factor &f, const double *V, double *Z, int p,
+                              float *w32, double *xb, double *yb) {
+  const size_t n = (size_t)m.nn * 6 * p;
+  int rc;
+  if (f.precision == 32) {
+    k_f64_to_f32<<<grid_for(n), 256, 0, m.stream>>>(w32, V, n);
+    if ((rc = solve_graph<float, float>(f, f.F32.p, w32, w32, p, m.stream, &m.launches)))
+      return rc;
+    k_f32_to_f64<<<grid_for(n), 256, 0, m.stream>>>(Z, w32, n);
+    m.launches += 2;
+  } else {
+    A2DS_CUDA_TRY(cudaMemcpyAsync(xb, V, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  m.stream));
+    if ((rc = solve_graph<double, double>(f, f.F64.p, xb, yb, p, m.stream, &m.launches)))
+      return rc;
+    A2DS_CUDA_TRY(cudaMemcpyAsync(Z, yb, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  m.stream));
+  }
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int BucklingState::precond(Mesh &m, Factor &f, const double *V, double *Z, int p) {
+  A2DS_CUDA_TRY(cudaEventRecord(next_event(), m.stream));
+  int rc = precondition_block(m, f, V, Z, p, gw32.p, Xb.p, Yb.p);
+  A2DS_CUDA_TRY(cudaEventRecord(next_event(), m.stream));
+  return rc;
+}
+
+// GMRES-IR: solve A Y = X for a block of p right-hand sides (row ordering,
+// X and Y must not alias) by p right-preconditioned flexible GMRES(msub)
+// solves in lockstep, one Krylov space per column.  Arnoldi vectors, the
+// products with A (the FP64 values Avals), the Gram-Schmidt coefficients
+// and the update of Y are FP64; the preconditioner is the factor f (FP32
+// for the mixed-precision solve), applied to every Arnoldi vector.  The
+// flexible form keeps Z_j = M^{-1} V_j and updates Y += Z y, so no solve is
+// spent on the update and the Arnoldi relation A Z = V H holds in FP64
+// although the FP32 solve is not an exact linear operator.  Every cycle
+// ends with the true FP64 residual X - A Y, which restarts the next cycle
+// and decides convergence: ||X_c - A Y_c|| <= rtol ||X_c|| for every column.
+// Orthogonalisation: two classical Gram-Schmidt passes.  One host
+// synchronisation per Arnoldi step (the p columns' Hessenberg entries).
+// precond(V, Z) applies the preconditioner to one n6 x p block.
+template <class Precond>
+static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const double *Avals,
+                              const double *X, double *Y, int p, double rtol, int msub,
+                              int max_cycles, int *iters) {
+  const size_t n6 = (size_t)m.nn * 6, bs = n6 * p;
+  const int ld = msub + 1;
+  int rc;
+  if (msub < 1 || msub > 63) return fail(A2DS_ERR_ARG, "GMRES-IR subspace must be 1..63");
+  if ((S.V.n < (size_t)(msub + 1) * bs && (rc = S.V.alloc((size_t)(msub + 1) * bs))) ||
+      (S.Z.n < (size_t)msub * bs && (rc = S.Z.alloc((size_t)msub * bs))) ||
+      (S.H.n < (size_t)(2 * ld + 1) * p && (rc = S.H.alloc((size_t)(2 * ld + 1) * p))))
+    return rc;
+  double *dH1 = S.H.p, *dH2 = S.H.p + (size_t)ld * p, *dN = S.H.p + (size_t)2 * ld * p;
+  std::vector<double> xn(p, 0.0), nrm2(p), h1((size_t)ld * p), h2((size_t)ld * p);
+  // per column: Hessenberg (column-major, ld x msub), rotated rhs g, Givens
+  std::vector<double> H((size_t)p * ld * msub), g((size_t)p * ld), qc((size_t)p * msub),
+      qs((size_t)p * msub), yv((size_t)msub * p);
+  auto Hc = [&](int c, int row, int col) -> double & {
+    return H[((size_t)c * msub + col) * ld + row];
+  };
+  A2DS_CUDA_TRY(cudaMemsetAsync(Y, 0, bs * sizeof(double), m.stream));
+  A2DS_CUDA_TRY(cudaMemcpyAsync(S.V.p, X, bs * sizeof(double), cudaMemcpyDeviceToDevice,
+                                m.stream));
+  for (int cyc = 0;; cyc++) {
+    // residual norms (V_0 holds X - A Y)
+    if ((rc = col_dots(S.V.p, 1, bs, S.V.p, n6, p, dN, m.stream))) return rc;
+    A2DS_CUDA_TRY(cudaMemcpyAsync(nrm2.data(), dN, p * sizeof(double), cudaMemcpyDeviceToHost,
+                                  m.stream));
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+    m.launches++;
+    if (cyc == 0)
+      for (int c = 0; c < p; c++) xn[c] = sqrt(nrm2[c]);
+    bool done = true;
+    for (int c = 0; c < p; c++)
+      if (!(sqrt(nrm2[c]) <= rtol * xn[c])) done = false;
+    if (done) return 0;
+    if (cyc == max_cycles)
+      return fail(A2DS_ERR_NOCONV, "GMRES-IR did not reach the tolerance in " +
+                                       std::to_string(max_cycles) + " cycles");
+    S.cycles++;
+    if ((rc = col_unit(S.V.p, dN, n6, p, m.stream))) return rc;
+    m.launches++;
+    std::fill(H.begin(), H.end(), 0.0);
+    std::fill(g.begin(), g.end(), 0.0);
+    for (int c = 0; c < p; c++) g[(size_t)c * ld] = sqrt(nrm2[c]);
+    int nit = 0;
+    for (int j = 0; j < msub; j++) {
+      double *Vj = S.V.p + (size_t)j * bs, *Zj = S.Z.p + (size_t)j * bs;
+      double *W = S.V.p + (size_t)(j + 1) * bs;
+      if ((rc = precond(Vj, Zj))) return rc;
+      if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Avals, Zj, nullptr, W, p, m.stream)))
+        return rc;
+      if ((rc = col_dots(S.V.p, j + 1, bs, W, n6, p, dH1, m.stream))) return rc;
+      if ((rc = col_axpy(W, S.V.p, j + 1, bs, dH1, n6, p, -1.0, m.stream))) return rc;
+      if ((rc = col_dots(S.V.p, j + 1, bs, W, n6, p, dH2, m.stream))) return rc;
+      if ((rc = col_axpy(W, S.V.p, j + 1, bs, dH2, n6, p, -1.0, m.stream))) return rc;
+      if ((rc = col_dots(W, 1, bs, W, n6, p, dN, m.stream))) return rc;
+      A2DS_CUDA_TRY(cudaMemcpyAsync(h1.data(), dH1, (size_t)(j + 1) * p * sizeof(double),
+                                    cudaMemcpyDeviceToHost, m.stream));
+      A2DS_CUDA_TRY(cudaMemcpyAsync(h2.data(), dH2, (size_t)(j + 1) * p * sizeof(double),
+                                    cudaMemcpyDeviceToHost, m.stream));
+      A2DS_CUDA_TRY(cudaMemcpyAsync(nrm2.data(), dN, p * sizeof(double), cudaMemcpyDeviceToHost,
+                                    m.stream));
+      if ((rc = col_unit(W, dN, n6, p, m.stream))) return rc;
+      m.launches += 7;
+      A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+      nit = j + 1;
+      S.iters++;
+      if (iters) (*iters)++;
+      bool conv = true;
+      for (int c = 0; c < p; c++) {
+        for (int k = 0; k <= j; k++) Hc(c, k, j) = h1[(size_t)k * p + c] + h2[(size_t)k * p + c];
+        Hc(c, j + 1, j) = sqrt(nrm2[c]);
+        double *qcc = qc.data() + (size_t)c * msub, *qsc = qs.data() + (size_t)c * msub;
+        for (int k = 0; k < j; k++) {
+          const double a = Hc(c, k, j), b = Hc(c, k + 1, j);
+          Hc(c, k, j) = a * qcc[k] + b * qsc[k];
+          Hc(c, k + 1, j) = -a * qsc[k] + b * qcc[k];
+        }
+        const double a = Hc(c, j, j), b = Hc(c, j + 1, j);
+        const double sq = sqrt(a * a + b * b);
+        qcc[j] = sq > 0.0 ? a / sq : 1.0;
+        qsc[j] = sq > 0.0 ? b / sq : 0.0;
+        Hc(c, j, j) = a * qcc[j] + b * qsc[j];
+        Hc(c, j + 1, j) = 0.0;
+        double *gc = g.data() + (size_t)c * ld;
+        const double r = gc[j];
+        gc[j] = r * qcc[j];
+        gc[j + 1] = -r * qsc[j];
+        if (!(fabs(gc[j + 1]) <= rtol * xn[c])) conv = false;
+      }
+      if (conv) break;
+    }
+    // y per column (back substitution), Y += Z y, next residual X - A Y
+    for (int c = 0; c < p; c++) {
+      const double *gc = g.data() + (size_t)c * ld;
+      for (int i = nit - 1; i >= 0; i--) {
+        double s = gc[i];
+        for (int k = i + 1; k < nit; k++) s -= Hc(c, i, k) * yv[(size_t)k * p + c];
+        const double d = Hc(c, i, i);
+        yv[(size_t)i * p + c] = d != 0.0 ? s / d : 0.0;
+      }
+    }
+    A2DS_CUDA_TRY(cudaMemcpyAsync(dH1, yv.data(), (size_t)nit * p * sizeof(double),
+                                  cudaMemcpyHostToDevice, m.stream));
+    if ((rc = col_axpy(Y, S.Z.p, nit, bs, dH1, n6, p, 1.0, m.stream))) return rc;
+    if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Avals, Y, X, S.V.p, p, m.stream)))
+      return rc;
+    m.launches += 2;
+  }
 }
 
 // K-orthonormalise the block W (with KW = K W): one Cholesky-QR pass,
@@ -741,10 +925,11 @@ static int prepare_solve(Mesh &m, const a2ds_buckling_opts *opts, BucklingState 
     m.solver = Sp;
     Sp->lev_fill = opts->lev_fill;
     Sp->precision = opts->precision;
-    // K's factor serves the load-path solve (FP64 refinement to 1e-13): FP64,
-    // or double-float when the shifted factor is double-float too; an FP32
-    // factor of K is too coarse for this (cond(K) ~ 1e11)
-    if ((rc = factor_setup(m, opts->lev_fill, opts->precision == 48 ? 48 : 64, Sp->fk))) return rc;
+    // K's factor serves the load-path solve in the same precision as the
+    // shifted factor: FP64 and double-float factors by FP64 iterative
+    // refinement, an FP32 factor as the preconditioner of FP64 GMRES-IR
+    // (cond(K) ~ 1e10 puts plain refinement with it out of reach)
+    if ((rc = factor_setup(m, opts->lev_fill, opts->precision, Sp->fk))) return rc;
     if (opts->lev_fill >= m.nn && (rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa)))
       return rc;
   }
@@ -760,7 +945,8 @@ static int prepare_solve(Mesh &m, const a2ds_buckling_opts *opts, BucklingState 
       (rc = S.r.alloc(n6)) || (rc = S.t.alloc(n6)) || (rc = S.path.alloc(n6)) ||
       (rc = S.rhs.alloc(n6)))
     return rc;
-  (void)S;
+  if (opts->precision == 32 && S.gw32.n < bs && (rc = S.gw32.alloc(bs))) return rc;
+  S.ir.iters = S.ir.cycles = 0;
   *out = Sp;
   return 0;
 }
@@ -836,7 +1022,14 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
       // [1e-12, 1e-9]): the Ritz values of the exact operator are then
       // unaffected at that tolerance
       const double rtol = std::max(1e-12, std::min(1e-9, 0.1 * opts->eig_tol));
-      if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, rtol, 2, &inner))) return rc;
+      if (S.fa.precision == 32) {
+        auto pc = [&](const double *V, double *Z) { return S.precond(m, S.fa, V, Z, p); };
+        if ((rc = fgmres_block_solve(m, S.ir, pc, S.Aux.p, KQj, W, p, rtol, GMRES_IR_MSUB,
+                                     GMRES_IR_CYCLES, &inner)))
+          return rc;
+      } else if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, rtol, 2, &inner))) {
+        return rc;
+      }
     } else {
       for (int c = 0; c < p; c++) {  // one GMRES solve per block column
         k_col_get<<<grid_for(n6), 256, 0, m.stream>>>(KQj, p, c, S.r.p, n6);
@@ -1063,6 +1256,54 @@ int a2ds_gmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rto
   return rc ? rc : rc2;
 }
 
+int a2ds_fgmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rtol, int nrhs,
+                      const double *b, double *x, int *iters) {
+  if (!A || !pc || !b || !x) return fail(A2DS_ERR_ARG, "null argument");
+  if (pc->mat->mesh != A->mesh) return fail(A2DS_ERR_ARG, "preconditioner of another mesh");
+  if (nrhs != 1 && nrhs != 2 && nrhs != 4 && nrhs != 8 && nrhs != 16)
+    return fail(A2DS_ERR_ARG, "nrhs must be 1, 2, 4, 8 or 16");
+  if (msub < 1 || msub > 63 || nrestart < 0)
+    return fail(A2DS_ERR_ARG, "need 1 <= msub <= 63 and nrestart >= 0");
+  if (!(rtol > 0.0)) return fail(A2DS_ERR_ARG, "rtol must be positive");
+  Mesh &m = A->mesh->m;
+  if (!m.initialized || !A->vals.p) return fail(A2DS_ERR_STATE, "mesh or matrix not initialized");
+  Factor &f = pc->f;
+  const size_t n6 = (size_t)m.nn * 6, tot = n6 * nrhs;
+  // node-ordered vectors -> row order, right-hand sides interleaved
+  std::vector<double> h(tot);
+  for (int k = 0; k < nrhs; k++)
+    for (int r = 0; r < m.nn; r++)
+      for (int d = 0; d < 6; d++)
+        h[((size_t)r * 6 + d) * nrhs + k] = b[(size_t)k * n6 + (size_t)m.perm[r] * 6 + d];
+  DBuf<double> db, dx, xb, yb;
+  DBuf<float> w32;
+  int rc;
+  if ((rc = db.upload(h.data(), tot, m.stream)) || (rc = dx.alloc(tot))) return rc;
+  if (f.precision == 32) {
+    if ((rc = w32.alloc(tot))) return rc;
+  } else if ((rc = xb.alloc(tot)) || (rc = yb.alloc(tot))) {
+    return rc;
+  }
+  IrWork w;
+  auto precond = [&](const double *V, double *Z) {
+    return precondition_block(m, f, V, Z, nrhs, w32.p, xb.p, yb.p);
+  };
+  int it = 0;
+  rc = fgmres_block_solve(m, w, precond, A->vals.p, db.p, dx.p, nrhs, rtol, msub, nrestart + 1,
+                          &it);
+  if (iters) *iters = it;
+  if (rc && rc != A2DS_ERR_NOCONV) return rc;
+  const int rc_conv = rc;
+  A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), dx.p, tot * sizeof(double), cudaMemcpyDeviceToHost,
+                                m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  for (int k = 0; k < nrhs; k++)
+    for (int r = 0; r < m.nn; r++)
+      for (int d = 0; d < 6; d++)
+        x[(size_t)k * n6 + (size_t)m.perm[r] * 6 + d] = h[((size_t)r * 6 + d) * nrhs + k];
+  return rc_conv;
+}
+
 int a2ds_pc_get(a2ds_pc pc, int *nrows, int *nnzb, int *rowp, int *cols, double *vals) {
   if (!pc) return fail(A2DS_ERR_ARG, "null preconditioner");
   Factor &f = pc->f;
@@ -1161,7 +1402,12 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   // for the path and on K + sigma G inside the shift-invert operator
   const bool direct = opts->lev_fill >= m.nn;
   GmresWork gw;
-  if (direct) {
+  if (direct && S.fk.precision == 32) {
+    auto pc = [&](const double *V, double *Z) { return S.precond(m, S.fk, V, Z, 1); };
+    if ((rc = fgmres_block_solve(m, S.ir, pc, S.K.p, S.rhs.p, S.path.p, 1, 1e-13, GMRES_IR_MSUB,
+                                 GMRES_IR_CYCLES, &inner)))
+      return rc;
+  } else if (direct) {
     if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.rhs.p, S.path.p, 1, 1e-13, 4, &inner)))
       return rc;
   } else {
@@ -1197,7 +1443,8 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   m.stats = {total, t_k, t_g, t_fk + t_fa, t_path, t_lan, (double)mdim, (double)inner,
              (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
              (double)S.fk.nnzb(), (double)S.fk.flv.nlevels, (double)S.fk.flops(), (double)p,
-             (double)nsteps, S.solve_ms(), (double)(S.ntev / 2)};
+             (double)nsteps, S.solve_ms(), (double)(S.ntev / 2), (double)S.ir.iters,
+             (double)S.ir.cycles};
   if (!converged) return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
   return 0;
 }
@@ -1253,7 +1500,8 @@ int a2ds_eigen_shift_invert(a2ds_mesh mesh, const a2ds_buckling_opts *opts, a2ds
   m.stats = {total, 0.0, 0.0, t_fk + po.t_fa, 0.0, po.t_lan, (double)po.mdim, (double)inner,
              (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
              (double)S.fk.nnzb(), (double)S.fk.flv.nlevels, (double)S.fk.flops(),
-             (double)opts->block_size, (double)po.nsteps, S.solve_ms(), (double)(S.ntev / 2)};
+             (double)opts->block_size, (double)po.nsteps, S.solve_ms(), (double)(S.ntev / 2),
+             (double)S.ir.iters, (double)S.ir.cycles};
   if (!po.converged)
     return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
   return 0;

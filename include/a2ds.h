@@ -279,6 +279,20 @@ int a2ds_gmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rto
                      double atol, const double *b, double *x, int *iters,
                      double *res_norm);
 
+/* GMRES(mat, pc, msub, nrestart, isFlexible = 1) (src/bpmat/KSM.h:391-419,
+   flexible variant of GMRES::solve, src/bpmat/KSM.cpp:785-970) run as GMRES-IR
+   for nrhs in {1, 2, 4, 8, 16} right-hand sides at once: one Krylov space per
+   right-hand side, FP64 Arnoldi vectors and products with A, the factor of
+   pc (FP32, double-float or FP64) applied to every Arnoldi vector, and the
+   true FP64 residual b - A x evaluated after every cycle of msub (<= 63)
+   steps.  Stops when ||b_k - A x_k|| <= rtol ||b_k|| for every k (zero
+   initial guess); A2DS_ERR_NOCONV after nrestart + 1 cycles (x then holds
+   the last iterate).  b and x hold nrhs node-ordered num_nodes x 6 vectors
+   one after another; *iters receives the Arnoldi steps (= preconditioner
+   applications). */
+int a2ds_fgmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rtol, int nrhs,
+                      const double *b, double *x, int *iters);
+
 /* --------------------------------------------------------- buckling solve */
 typedef struct {
   double sigma;          /* spectral shift (TACSLinearBuckling ctor) */
@@ -291,8 +305,10 @@ typedef struct {
   double gmres_rtol;     /* GMRES relative tolerance */
   double gmres_atol;     /* GMRES absolute tolerance */
   int precision;         /* 64: all-FP64; 48: double-float factors + FP64
-                            solves and refinement; 32: FP32 factors + FP64
-                            refinement */
+                            solves and refinement; 32: FP32 factors and
+                            FP32 triangular solves as the preconditioner of
+                            FP64 flexible GMRES (GMRES-IR) for the load
+                            path and every shift-invert solve */
   int seed;              /* Lanczos start vector seed */
   int block_size;        /* Lanczos block size p in {1, 2, 4, 8, 16}: p vectors
                             per shift-invert solve (1 = the reference's
@@ -331,7 +347,8 @@ int a2ds_eigen_shift_invert(a2ds_mesh mesh, const a2ds_buckling_opts *opts, a2ds
    path_s, lanczos_s, lanczos_vectors, inner_iters, kernel_launches,
    solve_event_ms, factor_a_event_ms, factor_k_event_ms, factor_nnzb,
    factor_levels, factor_flops, block_size, block_iters, trisolve_ms,
-   trisolve_calls}. */
+   trisolve_calls, gmres_ir_iters, gmres_ir_cycles} (the last two: Arnoldi
+   steps and restart cycles of the GMRES-IR solves with FP32 factors). */
 int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out);
 
 /* ---------------------------------------------- eigenvalue sensitivities

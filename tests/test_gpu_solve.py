@@ -44,9 +44,12 @@ def test_factor_matches_reference(case, precision):
     rowp, cols, vals = pc.get_arrays()
     assert np.array_equal(rowp, f["ilu_rowp"]) and np.array_equal(cols, f["ilu_cols"])
     # FP64: reference rounding differences only; double-float (48): ~2^-48
-    # rounding in the update chain; FP32 factors are only checked for pattern
-    tol = {64: 1e-10, 48: 1e-10, 32: 1e-3}[precision]
-    assert rel(vals, f["ilu_K"]) < tol or precision == 32
+    # rounding in the update chain; FP32: single-precision rounding of every
+    # update, amplified by the thin-shell cancellation in the Schur
+    # complements (a CPU FP32 restatement of the same factorization differs
+    # from the reference's values by 3e-7 .. 1.2e-5 on these three meshes)
+    tol = {64: 1e-10, 48: 1e-10, 32: 1e-4}[precision]
+    assert rel(vals, f["ilu_K"]) < tol
     # applyFactor in the row ordering: the fixture vector is in row order
     perm = a.get_ordering()
     x_rows = f["ilu_apply_x"].reshape(-1, 6)
@@ -60,11 +63,13 @@ def test_factor_matches_reference(case, precision):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["cyl_q4_4x8_lu", "cyl_q4_8x16_ilu1", "cyl_q9_2x4_lu"])
-@pytest.mark.parametrize("precision,block", [(64, 1), (64, 8), (48, 8)])
+@pytest.mark.parametrize("precision,block", [(64, 1), (64, 8), (48, 8), (32, 1), (32, 4)])
 def test_buckling_loads_match_dense_reference(case, precision, block):
     """Eigenvalues within 1e-8 (relative) of a dense FP64 solution, for the
-    single-vector and block Lanczos and for double-float factors (FP64
-    refinement of every shift-invert solve)."""
+    single-vector and block Lanczos, for double-float factors (FP64
+    refinement of every shift-invert solve) and for FP32 factors (FP32
+    triangular solves preconditioning FP64 GMRES-IR, for the load path and
+    every shift-invert solve)."""
     f = np.load(os.path.join(GOLDEN, case + ".npz"))
     a = setup(f)
     nev = 5
@@ -437,3 +442,55 @@ def test_lanczos_budget_exhausted_returns_ritz_pairs():
         b.solve(f["rhs"])
     assert e.value.code == 6  # A2DS_ERR_NOCONV
     assert np.all(np.isfinite(b.eigvals))
+
+
+def shifted_cylinder(nx, ny):
+    """K, G (along the load path) and A = K + sigma G (Dirichlet rows as the
+    reference's applyBCs) of a seeded cylinder, sigma = 0.95 x its lowest
+    load."""
+    from a2ds import mesh as meshgen
+    m = meshgen.cylinder(nx, ny)
+    a = capi.Assembler(m.X, m.conn)
+    a.set_material(m.E, m.nu)
+    a.set_thickness([m.meta["t"]])
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    lam_cl = meshgen.classical_cylinder_load(m.E, m.nu, m.meta["t"], 1.0)
+    b = capi.LinearBuckling(a, 0.35 * lam_cl, max_lanczos=120, num_eigvals=1, eig_tol=1e-10,
+                            precision=64, block_size=4)
+    b.solve(m.rhs, want_vectors=False)
+    sigma = 0.95 * float(b.eigvals[0])
+    K, G, A = a.create_mat(), a.create_mat(), a.create_mat()
+    a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
+    a.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, b.path)
+    A.copy_values(K)
+    A.axpy(sigma, G)
+    A.apply_bcs()
+    return m, a, K, A
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nrhs", [1, 4])
+def test_gmres_ir_fp32_factor_reaches_fp64_residual(nrhs):
+    """Flexible GMRES-IR on A = K + sigma G of a 24x48 thin cylinder
+    (cond ~1e10, far beyond 1/eps_32) with the FP32 complete-LU factor of A
+    as the preconditioner: the FP64 residual, recomputed here from the
+    returned solution, meets 1e-10 for every right-hand side; the FP32
+    factor alone (one solve) does not come near it."""
+    m, a, K, A = shifted_cylinder(24, 48)
+    pc = capi.SchurPc(A, 1000000, 32)
+    pc.factor()
+    rng = np.random.default_rng(11)
+    B = rng.standard_normal((nrhs, m.num_nodes, 6))
+    for bn, mk in zip(m.bc_nodes, m.bc_mask):
+        for k in range(6):
+            if mk >> k & 1:
+                B[:, bn, k] = 0.0
+    X, its = capi.fgmres_solve(A, pc, B, msub=24, nrestart=8, rtol=1e-10)
+    for k in range(nrhs):
+        r = B[k] - A.mult(X[k])
+        assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(B[k]), (k, np.linalg.norm(r))
+    # a single FP32 solve is far less accurate: the refinement is doing the work
+    y = pc.apply_factor(B[0])
+    assert np.linalg.norm(B[0] - A.mult(y)) > 1e-8 * np.linalg.norm(B[0])
+    assert its <= 8 * 24

@@ -56,6 +56,32 @@ def test_noalloc_mult_matches_allocating_entry_point():
 
 
 @pytest.mark.gpu
+def test_noalloc_smaller_matrix_after_larger():
+    """A 4x8 cylinder right after a 24x48 one: the shared array's tail still
+    holds the larger call's values, and the smaller product must not see
+    them."""
+    big = cylinder_assembler(24, 48)
+    Kb = big.create_mat()
+    big.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, Kb)
+    rng = np.random.default_rng(5)
+    xb = rng.standard_normal((big.num_nodes, 6))
+    assert rel(Kb.mult_rows(xb, noalloc=True), Kb.mult_rows(xb)) < 1e-13
+    small = cylinder_assembler(4, 8)
+    Ks = small.create_mat()
+    small.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, Ks)
+    rowp, cols, vals = Ks.get_arrays()
+    nn = rowp.size - 1
+    xs = rng.standard_normal((nn, 6))
+    y = Ks.mult_rows(xs, noalloc=True)
+    assert rel(y, Ks.mult_rows(xs)) < 1e-13
+    y_np = np.zeros_like(xs)
+    for r in range(nn):
+        for k in range(rowp[r], rowp[r + 1]):
+            y_np[r] += vals[k] @ xs[cols[k]]
+    assert rel(y, y_np) < 1e-13
+
+
+@pytest.mark.gpu
 def test_noalloc_rejects_oversize_matrix():
     a = cylinder_assembler(256, 256)
     assert a.num_nodes > MAX_ROWS
