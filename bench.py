@@ -1,13 +1,18 @@
 #!/usr/bin/env python
 """Buckling-solve benchmark on GB300 (and the CPU reference arm).
 
-Workload (N=1): the 256 x 512 Quad4 MITC cylinder (R = 1 m, L = 2 m,
-t = 2 mm, E = 70 GPa, nu = 0.3, 131 072 elements, 789 504 DOF), one end
+Workload (N=1): the 512 x 1024 Quad4 MITC cylinder (R = 1 m, L = 2 m,
+t = 2 mm, E = 70 GPa, nu = 0.3, 524 288 elements, 3 151 872 DOF), one end
 clamped, 1 N/m axial compression at the other, seeded 0.01 t radial
 imperfection; the 10 buckling loads of smallest magnitude by shift-invert
-Lanczos, all-FP64 on the GPU (assembly, complete-LU factor of K and of
-K + sigma G, solves, Lanczos).  Synthetic seeded inputs stand in for a
-dataset (the reference publishes none).
+block Lanczos.  Headline precision: FP32 complete-LU factors of K and of
+K + sigma G with FP32 triangular solves, preconditioning FP64 flexible
+GMRES (GMRES-IR) for the load path and every shift-invert solve; FP64
+assembly, products with K and K + sigma G, Lanczos orthogonalisation and
+Rayleigh quotients.  The all-FP64 variant of the same solve is measured in
+the same run: its eigenvalues are the reference for the FP32-IR error and
+its rate for the FP32-over-FP64 speed-up.  Synthetic seeded inputs stand in
+for a dataset (the reference publishes none).
 
 A step is one complete buckling solve (TACSLinearBuckling::solve semantics:
 assemble K, load path, assemble G, factor, Lanczos, eigenpairs) through the
@@ -21,11 +26,7 @@ stream around each solve.  The shift sigma is 0.95 x the lowest load found
 by a cheap first solve at 0.35 x the classical load (untimed setup).
 
 --impl reference times the reference's algorithm on the host cores through
-the CPU oracle (oracle/): LU of K, GMRES on K + sigma G, Lanczos with
-K-inner products by SpMV.  A full config solve takes many CPU-minutes, so
-the sample is a complete solve of the 64 x 128 cylinder plus the full-size
-K and G assemblies, scaled to the full size by exact factorization flop and
-factor-size ratios (stated in the JSON line).
+the CPU oracle (oracle/), as described in its JSON line.
 
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank runs an independent replica on its own GPU
@@ -55,12 +56,15 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--nx", type=int, default=256)
-    p.add_argument("--ny", type=int, default=512)
+    p.add_argument("--nx", type=int, default=512)
+    p.add_argument("--ny", type=int, default=1024)
     p.add_argument("--neig", type=int, default=10)
-    p.add_argument("--precision", type=int, default=48, choices=[64, 48, 32],
-                   help="factor arithmetic: 64 FP64, 48 double-float on the FP32 pipe, 32 FP32 "
-                        "(solves and refinement are FP64 in every case)")
+    p.add_argument("--precision", type=int, default=32, choices=[64, 48, 32],
+                   help="factor arithmetic: 32 FP32 factors and triangular solves inside FP64 "
+                        "GMRES-IR, 48 double-float factors on the FP32 pipe with FP64 "
+                        "refinement, 64 FP64")
+    p.add_argument("--no-variants", action="store_true",
+                   help="skip the FP64 and double-float variants of the same solve")
     p.add_argument("--block", type=int, default=4, choices=[1, 2, 4, 8, 16],
                    help="Lanczos block size")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -128,7 +132,8 @@ class ClockSampler:
 
 
 PREC_NAME = {64: "FP64 factors", 48: "double-float (2 x FP32) factors with FP64 refinement",
-             32: "FP32 factors with FP64 refinement"}
+             32: "FP32 factors and triangular solves inside FP64 GMRES-IR"}
+DTYPE = {64: "f64", 48: "df64 factor (2 x f32) + f64", 32: "f32 factor + f64"}
 
 # DRAM traffic of one numeric factorization of the bench workload, summed
 # over all its launches from an ncu capture (profiles/factor_cylinder256x512_traffic.md)
@@ -317,8 +322,28 @@ def workload_config(m, args):
         "elements": m.num_elements, "nodes": m.num_nodes, "dof": 6 * m.num_nodes,
         "num_eigvals": args.neig, "lev_fill": "complete LU (1e6)", "precision": args.precision,
         "lanczos_block_size": args.block,
-        "l2": "no flush: every step streams the ~3.5 GB factor and 0.34 GB matrices (> 129 MB L2)",
+        "l2": ("no flush: every step streams the complete-LU factors (57 M blocks at 512x1024, "
+               "8.2 GB in FP32) and the 1.4 GB matrices, far above the 129 MB L2"),
     }
+
+
+def variant_rate(capi, a, m, sigma, args, precision, ref_lam=None):
+    """One untimed and up to two timed solves of the same workload in another
+    factor precision: (rate line, eigenvalues)."""
+    import numpy as np
+    b = capi.LinearBuckling(a, sigma, max_lanczos=200, num_eigvals=args.neig, eig_tol=1e-8,
+                            precision=precision, block_size=args.block)
+    lam = b.solve(m.rhs, want_vectors=False).copy()  # also the warm-up
+    ms = []
+    for _ in range(max(1, min(args.steps, 2))):
+        b.solve(m.rhs, want_vectors=False)
+        ms.append(b.stats()["solve_event_ms"])
+    out = {"value": 1000.0 / (sum(ms) / len(ms)), "unit": "solves/s",
+           "ms_per_step": sum(ms) / len(ms), "steps": len(ms), "dtype": DTYPE[precision],
+           "eig_residual_max": float(np.max(b.errors))}
+    if ref_lam is not None:
+        out["eig_rel_err_vs_fp64"] = float(np.max(np.abs(lam - ref_lam) / np.abs(ref_lam)))
+    return out, lam
 
 
 def main():
@@ -382,7 +407,7 @@ def main():
     barrier()
     # e2e: host load vector in, host eigenvectors and path out
     e2e_wall = []
-    for _ in range(args.steps):
+    for _ in range(min(args.steps, 5)):
         t0 = time.perf_counter()
         b.solve(m.rhs, want_vectors=True)
         e2e_wall.append(time.perf_counter() - t0)
@@ -392,81 +417,94 @@ def main():
     ms = sum(ev_ms) / len(ev_ms)
     t_rank, t_e2e = max_over_ranks([sum(ev_ms) / 1000.0, sum(e2e_wall)], dist)
     value = world * args.steps / t_rank
-    e2e_value = world * args.steps / t_e2e
+    e2e_value = world * len(e2e_wall) / t_e2e
     if rank != 0:
         return 0
 
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     fp64 = fp64_peak_tflops()
-    # dominant kernel: the numeric factorization of K + sigma G (the update
-    # kernels of every dependency level with their pivot and L-column
-    # kernels, one launch sequence); algorithmic bytes = the factor values
-    # read and written once; flops from the exact symbolic count
+    # dominant kernel sequence of the step: the numeric factorization of
+    # K + sigma G (all its launches) or one triangular-solve pass (L then U
+    # for the Lanczos block), whichever takes more of the step; algorithmic
+    # bytes: the factor values read (and, factorization, written) once
     nnzf = stats["factor_nnzb"]
+    vbytes = 4 if args.precision == 32 else 8
     fa_ms = stats["factor_a_event_ms"]
-    bytes_factor = nnzf * 36 * 8 * 2
-    achieved_gbs = bytes_factor / (fa_ms * 1e-3) / 1e9
+    tri_calls = max(1.0, stats["trisolve_calls"])
+    tri_ms = stats["trisolve_ms"] / tri_calls
+    fact_total = fa_ms + stats["factor_k_event_ms"]
+    if stats["trisolve_ms"] > fact_total:
+        rl_kernel = ("one triangular-solve pass (unit-lower then upper with the stored inverse "
+                     f"diagonal blocks) on a block of {args.block} vectors, FP"
+                     f"{32 if args.precision == 32 else 64} factor values")
+        rl_bytes = nnzf * (36 * vbytes + 4) + 2 * 2 * 6 * m.num_nodes * args.block * vbytes
+        rl_ms = tri_ms
+        rl_unit = "bytes per solve pass (factor values and column indices read once)"
+    else:
+        rl_kernel = ("numeric complete-LU factorization of K + sigma G (panel-blocked trailing "
+                     "updates k_update_panel, per-level k_update_long / k_update_group, "
+                     "pivot inverses)")
+        rl_bytes = nnzf * 36 * vbytes * 2
+        rl_ms = fa_ms
+        rl_unit = "bytes per factorization (factor values read and written once)"
+    achieved_gbs = rl_bytes / (rl_ms * 1e-3) / 1e9
     achieved_tf = stats["factor_flops"] / (fa_ms * 1e-3) / 1e12
     lam_err = float(np.max(np.abs(b.eigvals - ref_lam) / np.abs(ref_lam)))
-    vs_fp64, fp64_variant = None, None
-    if args.precision != 64:
-        # the all-FP64 variant of the same solve: its eigenvalues are the
-        # reference for this precision's error, and its rate is reported beside
-        b64 = capi.LinearBuckling(a, sigma, max_lanczos=200, num_eigvals=args.neig, eig_tol=1e-8,
-                                  precision=64, block_size=args.block)
-        lam64 = b64.solve(m.rhs, want_vectors=False).copy()  # also the warm-up
-        vs_fp64 = float(np.max(np.abs(b.eigvals - lam64) / np.abs(lam64)))
-        ms64 = []
-        for _ in range(max(1, min(args.steps, 2))):
-            b64.solve(m.rhs, want_vectors=False)
-            ms64.append(b64.stats()["solve_event_ms"])
-        fp64_variant = {"value": 1000.0 / (sum(ms64) / len(ms64)), "unit": "solves/s",
-                        "ms_per_step": sum(ms64) / len(ms64), "steps": len(ms64),
-                        "dtype": "f64"}
-        if dist:
-            fp64_variant["note"] = "rank 0 only"
+    variants = {}
+    fp64_variant, lam64 = None, None
+    if not args.no_variants:
+        if args.precision != 64:
+            fp64_variant, lam64 = variant_rate(capi, a, m, sigma, args, 64)
+            fp64_variant["eig_rel_err_vs_fp64"] = 0.0
+            if dist:
+                fp64_variant["note"] = "rank 0 only"
+        if args.precision != 48:
+            variants["df64"], _ = variant_rate(capi, a, m, sigma, args, 48, lam64)
+    vs_fp64 = (float(np.max(np.abs(b.eigvals - lam64) / np.abs(lam64)))
+               if fp64_variant is not None else None)
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {64: "f64", 48: "df64 factor (2 x f32) + f64", 32: "f32 factor + f64"}[args.precision],
+        "dtype": DTYPE[args.precision],
         "data": "synthetic (seeded cylinder mesh, loads and imperfection; no dataset)",
         "config": workload_config(m, args),
         "gpu_launches": launches,
-        "e2e": {"value": e2e_value, "unit": "solves/s",
+        "e2e": {"value": e2e_value, "unit": "solves/s", "steps": len(e2e_wall),
                 "h2d_bytes_per_step": int(m.num_nodes * 6 * 8),
                 "d2h_bytes_per_step": int((args.neig * (2 + 6 * m.num_nodes) + 6 * m.num_nodes) * 8)},
         "roofline": {
-            "kernel": ("numeric complete-LU factorization of K + sigma G: panel-blocked trailing "
-                       "updates (k_update_panel), per-level k_update_long / k_update_group, "
-                       "k_factor_pivot_df"),
-            "bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
-            "frac": (achieved_gbs / hbm) if hbm else None,
+            "kernel": rl_kernel, "bound": "hbm", "achieved": achieved_gbs, "peak": hbm,
+            "unit": "GB/s", "frac": (achieved_gbs / hbm) if hbm else None,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": FACTOR_TRAFFIC.get((args.nx, args.ny, args.precision)),
-            "traffic_unit": "bytes per factorization (ncu dram__bytes read+write, all its launches)",
-            "compute": {"pipe": "fp32 (double-float)" if args.precision == 48 else
-                        ("fp64" if args.precision == 64 else "fp32"),
-                        "achieved_tflops_fp64_equivalent": achieved_tf,
-                        "fp64_peak_tflops_measured_dgemm": fp64,
-                        "frac_of_fp64_peak": (achieved_tf / fp64) if fp64 else None,
-                        "flops_per_factorization": stats["factor_flops"]},
-            "note": ("neither HBM nor tensor bound: in FP64 the block updates are bound by the "
-                     "FP64 pipe (~1/58 of FP32 on GB300); in double-float (~12 FP32 operations "
-                     "per multiply-subtract) the panel updates are bound by the FP32 issue rate "
-                     "and the per-level kernels by launch and memory latency; the HBM fraction "
-                     "is reported for the contract"),
+            "algorithmic_bytes": rl_bytes, "algorithmic_bytes_unit": rl_unit,
+            "ms_per_launch_sequence": rl_ms,
+            "factorization": {"ms": fa_ms, "flops": stats["factor_flops"],
+                              "achieved_tflops_fp64_equivalent_count": achieved_tf,
+                              "fp64_peak_tflops_measured_dgemm": fp64,
+                              "pipe": {32: "fp32", 48: "fp32 (double-float)", 64: "fp64"}[args.precision]},
+            "note": ("sparse 6x6-block LU and triangular solves: neither pipe is saturated; the "
+                     "triangular solves are bound by the latency of their dependent level "
+                     "launches, the factorization by launch/memory latency and the issue rate "
+                     "of its block updates; the HBM fraction is reported for the contract"),
         },
         "phases_s": {k: stats[k] for k in ["assemble_k_s", "assemble_g_s", "factor_s", "path_s",
                                             "lanczos_s"]},
         "lanczos": {"vectors": stats["lanczos_vectors"], "block_size": stats["block_size"],
-                    "block_steps": stats["block_iters"], "refinement_checks": stats["inner_iters"],
+                    "block_steps": stats["block_iters"], "inner_iters": stats["inner_iters"],
+                    "gmres_ir_arnoldi_steps": stats["gmres_ir_iters"],
+                    "gmres_ir_cycles": stats["gmres_ir_cycles"],
                     "trisolve_ms_total": stats["trisolve_ms"], "trisolve_calls": stats["trisolve_calls"]},
         "assembly_elems_per_s": {"K": m.num_elements / stats["assemble_k_s"],
                                  "G": m.num_elements / stats["assemble_g_s"]},
         "eigvals": b.eigvals.tolist(), "eig_rel_drift_between_runs": lam_err,
         "eig_residual_max": float(np.max(b.errors)), "sigma": sigma,
         "eig_rel_err_vs_fp64": vs_fp64, "fp64_variant": fp64_variant,
+        "speedup_over_fp64": ({"value": value / fp64_variant["value"], "target": 3.0}
+                              if fp64_variant else None),
+        "other_variants": variants,
         "clocks": clk,
     }
     line["spmv"] = spmv_roofline(capi, a, m, hbm)

@@ -18,7 +18,8 @@ builds) and packs inputs and outputs into small .npz files:
                         for two seeded meshes and nine output-class flags
 
 Only this container has the reference sources; the fixtures are committed so
-the tests never need them.  Run:  python tests/golden/make_golden.py
+the tests never need them.  Run:  python tests/golden/make_golden.py [part ...]
+(parts: the make_* names without the prefix, e.g. config1; default all).
 """
 from __future__ import annotations
 
@@ -269,7 +270,98 @@ def make_f5():
     print("wrote f5.npz", sorted(k for k in out if "f5_" in k))
 
 
+def sparse_eigs(fx, neig, sigma):
+    """Lowest buckling loads of K x + lam G x = 0 on the free DOFs by a
+    sparse shift-invert eigensolve (scipy ARPACK, tolerance 1e-14) of the
+    reference's own assembled K and G: the dense solve's role for meshes too
+    large for dense FP64 (the symmetric parts, as in dense_eigs)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    n = fx["bcsr_rowp"].size - 1
+    rowp, cols = fx["bcsr_rowp"], fx["bcsr_cols"]
+    K = sp.bsr_matrix((fx["K_after"], cols, rowp), shape=(6 * n, 6 * n)).tocsr()
+    G = sp.bsr_matrix((fx["G"], cols, rowp), shape=(6 * n, 6 * n)).tocsr()
+    perm = fx["amd_perm"]
+    inv = np.empty(n, np.int64)
+    inv[perm] = np.arange(n)
+    bcdof = np.zeros(6 * n, bool)
+    for node, mask in zip(fx["bc_nodes"], fx["bc_mask"]):
+        for k in range(6):
+            if mask >> k & 1:
+                bcdof[6 * inv[node] + k] = True
+    free = np.where(~bcdof)[0]
+    Kf = K[free][:, free]
+    Gf = G[free][:, free]
+    Kf = (0.5 * (Kf + Kf.T)).tocsc()
+    Gf = (0.5 * (Gf + Gf.T)).tocsc()
+    # K x = lam (-G) x, shift-invert about sigma (K - sigma (-G)) = K + sigma G
+    vals = sla.eigsh(Kf, k=2 * neig, M=-Gf, sigma=sigma, which="LM", tol=1e-14,
+                     return_eigenvectors=False, mode="buckling")
+    vals = np.sort(vals[vals > 0])
+    return vals[:neig]
+
+
+def make_config1():
+    """The reference's CPU-runnable workload: the 32 x 64 Quad4 cylinder (2,112
+    nodes, 12,672 DOF).  The reference solves it as its cylinder example does
+    (complete LU of K, GMRES(10, 15, 1e-12) on K + sigma G, 100 Lanczos
+    vectors for 50 eigenvalues), with sigma = 0.95 x the lowest load.  Kept:
+    inputs, the AMD permutation and BCSR pattern, the load path, the
+    reference's eigenvalues and, for each, the residual
+    ||K phi + lambda G phi|| / ||K phi|| of its eigenvector computed as
+    TACSLinearBuckling::checkEigenvector does (src/TACSBuckling.cpp:310-349,
+    the reference's own K, G and eigenvectors), and a sparse shift-invert
+    solve of the reference's K and G (eigvals_sparse).  Matrices, factors
+    and eigenvectors are left out to keep the file small."""
+    m = meshgen.cylinder(32, 64, order=2)
+    neig = 10
+    with tempfile.TemporaryDirectory() as d:
+        ind, outd = os.path.join(d, "in"), os.path.join(d, "out")
+        os.makedirs(ind)
+        os.makedirs(outd)
+        lam_cl = meshgen.classical_cylinder_load(m.E, m.nu, m.meta["t"], 1.0)
+        write_inputs(ind, m, 0.3 * lam_cl, 1000000, 10, 15, 100, 50)
+        subprocess.run([os.path.join(REF_OUT, "golden_gen"), "assembly", ind, outd], check=True)
+        fx = load_dir(outd)
+        fx.update(bc_nodes=m.bc_nodes, bc_mask=m.bc_mask)
+        lam0 = sparse_eigs(fx, neig, 0.3 * lam_cl)
+        sigma = 0.95 * lam0[0]
+        write_inputs(ind, m, sigma, 1000000, 10, 15, 100, 50)
+        subprocess.run([os.path.join(REF_OUT, "golden_gen"), "assembly", ind, outd], check=True)
+        fx = load_dir(outd)
+        fx.update(bc_nodes=m.bc_nodes, bc_mask=m.bc_mask)
+    lam_sparse = sparse_eigs(fx, neig, sigma)
+    # checkEigenvector on the reference's own matrices (row ordering) and vectors
+    import scipy.sparse as sp
+    n = fx["bcsr_rowp"].size - 1
+    rowp, cols = fx["bcsr_rowp"], fx["bcsr_cols"]
+    K = sp.bsr_matrix((fx["K_after"], cols, rowp), shape=(6 * n, 6 * n)).tocsr()
+    G = sp.bsr_matrix((fx["G"], cols, rowp), shape=(6 * n, 6 * n)).tocsr()
+    perm = fx["amd_perm"]
+    check = []
+    for k in range(neig):
+        phi = fx["eigvecs"][k][perm].ravel()      # node order -> row order
+        kp, gp = K @ phi, G @ phi
+        check.append(np.linalg.norm(kp + fx["eigvals"][k] * gp) / np.linalg.norm(kp))
+    out = dict(X=m.X, conn=m.conn, bc_nodes=m.bc_nodes, bc_mask=m.bc_mask, bc_vals=m.bc_vals,
+               rhs=m.rhs, thickness=m.thickness, E=np.float64(m.E), nu=np.float64(m.nu),
+               sigma=np.float64(sigma), lev=np.int32(1000000), gm_m=np.int32(10),
+               gm_restarts=np.int32(15), lanczos=np.int32(100), neig=np.int32(50),
+               amd_perm=fx["amd_perm"], bcsr_rowp=rowp, bcsr_cols=cols, path=fx["path"],
+               eigvals=fx["eigvals"][:neig], eigerr=fx["eigerr"][:neig],
+               check_res=np.array(check), eigvals_sparse=lam_sparse)
+    np.savez_compressed(os.path.join(HERE, "cyl_q4_32x64_lu.npz"), **out)
+    rel = np.abs(out["eigvals"] - lam_sparse) / lam_sparse
+    print("wrote cyl_q4_32x64_lu.npz: reference", out["eigvals"][:5], "sparse", lam_sparse[:5],
+          "rel", rel[:5], "checkEigenvector", out["check_res"][:5])
+
+
 def main():
+    if len(sys.argv) > 1:
+        build_reference()
+        for part in sys.argv[1:]:
+            globals()["make_" + part]()
+        return
     build_reference()
     make_f5()
     make_bdf()
@@ -285,6 +377,7 @@ def main():
     # stiffened panel (Quad9 skin and blade webs, one thickness group per
     # element cell of 20 axial segments x 20 lanes); the complex-step copies
     # and unused matrices are left out to keep the file small
+    make_config1()
     run_case("panel_q9_4x8x1_lu", meshgen.stiffened_panel(4, 8, 1), lev=1000000, gm_m=10,
              gm_restarts=15, lanczos=100, neig=10,
              drop=("K", "K_cs", "K_after_cs", "G_cs", "ilu_K_cs", "eigvecs", "eigvecs_cs",
