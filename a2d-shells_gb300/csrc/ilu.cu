@@ -1,7 +1,6 @@
 // Host-side schedules of the block ILU(k) / LU factorization and of the
 // triangular solves: dependency levels, right-looking update tasks and the
-// head / dense-tail split of the solves.  The kernels are in factor.cu and
-// trisolve.cu.
+// chunk plan of the solves.  The kernels are in factor.cu and trisolve.cu.
 #include <algorithm>
 
 #include "a2ds_internal.h"
@@ -232,214 +231,132 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
   }
 }
 
-// Rows are split at s = the smallest row index among rows of the first
-// narrow factor level (fewer than `narrow` rows); rows [s, n) are the tail,
-// whose last rows [t0, n) (when dense enough) are solved as one dense block.
-// Head solves are row-oriented by levels; the tail pulls its head couplings
-// once, the middle rows [s, t0) push columns level by level (lower), the
-// dense block is solved panel by panel, its values are pushed into the
-// middle rows, the middle pushes D^{-1}-scaled columns in reverse level order
-// (upper), and the head upper solve pulls the final tail values.
-void build_solve_schedule(Factor &f, const std::vector<int> &lev, int narrow) {
+// The chunk plan (ChunkPlan): chunk boundaries, each row's pull ranges,
+// chunk levels of the lower solve (from the first row on) and of the upper
+// solve (from the last row back), and the inverse storage offsets.
+void build_solve_schedule(Factor &f) {
   const int n = f.n;
-  const LevelSchedule &F = f.flv;
-  int first_narrow = F.nlevels;
-  for (int l = 0; l < F.nlevels; l++)
-    if (F.ptr[l + 1] - F.ptr[l] < narrow) {
-      first_narrow = l;
-      break;
+  ChunkPlan &cp = f.cp;
+  cp = ChunkPlan();
+  // chunks: a new one where row i has no L block in column i - 1, or at
+  // CHUNK_MAX rows
+  cp.c0.clear();
+  std::vector<int> chunk_of(n);
+  int cur = 0;
+  for (int i = 0; i < n; i++) {
+    const int d = f.fdiag[i];
+    const bool chained = i > 0 && d > f.frowp[i] && f.fcols[d - 1] == i - 1;
+    if (!chained || cur >= CHUNK_MAX) {
+      cp.c0.push_back(i);
+      cur = 0;
     }
-  int s = n;
-  for (int i = 0; i < n; i++)
-    if (lev[i] >= first_narrow) {
-      s = i;
-      break;
-    }
-  f.tail_s = s;
-  const int d = n - s;
-  // head lower: factor levels restricted to rows < s (empty levels dropped)
-  {
-    LevelSchedule &L = f.lower;
-    std::vector<int> cnt(F.nlevels + 1, 0);
-    for (int i = 0; i < s; i++) cnt[lev[i]]++;
-    std::vector<int> remap(F.nlevels, -1);
-    int nl = 0;
-    for (int l = 0; l < F.nlevels; l++)
-      if (cnt[l]) remap[l] = nl++;
-    L.nlevels = nl;
-    L.ptr.assign(nl + 1, 0);
-    for (int i = 0; i < s; i++) L.ptr[remap[lev[i]] + 1]++;
-    for (int l = 0; l < nl; l++) L.ptr[l + 1] += L.ptr[l];
-    L.rows.resize(s);
-    std::vector<int> fill(L.ptr.begin(), L.ptr.end() - 1);
-    for (int i = 0; i < s; i++) L.rows[fill[remap[lev[i]]]++] = i;
+    cur++;
+    chunk_of[i] = (int)cp.c0.size() - 1;
   }
-  // kernel choice per head level (see SOLVE_LONG_ROW)
-  auto choose = [&](const LevelSchedule &L, bool upper, std::vector<char> &cta) {
-    cta.assign(L.nlevels, 0);
+  cp.c0.push_back(n);
+  const int nc = (int)cp.c0.size() - 1;
+  cp.off.assign(nc, -1);
+  cp.row_lend.resize(n);
+  cp.row_ustart.resize(n);
+  cp.row_single.resize(n);
+  long long off = 0, scr = 0;
+  for (int c = 0; c < nc; c++) {
+    const int a = cp.c0[c], b = cp.c0[c + 1], ns = b - a;
+    cp.max_rows = std::max(cp.max_rows, ns);
+    if (ns >= 2) {
+      const long long sq = (long long)(6 * ns) * (6 * ns);
+      cp.off[c] = off;
+      off += 2 * sq;
+      scr += sq;
+    }
+    for (int i = a; i < b; i++) {
+      int k = f.frowp[i];
+      while (k < f.fdiag[i] && f.fcols[k] < a) k++;
+      cp.row_lend[i] = k;
+      k = f.fdiag[i] + 1;
+      while (k < f.frowp[i + 1] && f.fcols[k] < b) k++;
+      cp.row_ustart[i] = k;
+      cp.row_single[i] = ns == 1;
+    }
+  }
+  cp.inv_size = off;
+  cp.scr_size = scr;
+  // lower levels: 1 + the deepest chunk among the external L columns
+  std::vector<int> lv(nc, 0), uv(nc, 0);
+  int maxl = 0, maxu = 0;
+  for (int c = 0; c < nc; c++) {
+    int l = 0;
+    for (int i = cp.c0[c]; i < cp.c0[c + 1]; i++)
+      for (int k = f.frowp[i]; k < cp.row_lend[i]; k++) l = std::max(l, lv[chunk_of[f.fcols[k]]] + 1);
+    lv[c] = l;
+    maxl = std::max(maxl, l);
+  }
+  // upper levels, from the last chunk back: 1 + the deepest chunk among the
+  // external U columns
+  for (int c = nc - 1; c >= 0; c--) {
+    int l = 0;
+    for (int i = cp.c0[c]; i < cp.c0[c + 1]; i++)
+      for (int k = cp.row_ustart[i]; k < f.frowp[i + 1]; k++)
+        l = std::max(l, uv[chunk_of[f.fcols[k]]] + 1);
+    uv[c] = l;
+    maxu = std::max(maxu, l);
+  }
+  auto fill_levels = [&](const std::vector<int> &lev, int nl, bool upper, ChunkLevels &L) {
+    L.nlevels = n ? nl + 1 : 0;
+    L.row_ptr.assign(L.nlevels + 1, 0);
+    L.ch_ptr.assign(L.nlevels + 1, 0);
+    for (int c = 0; c < nc; c++) {
+      const int ns = cp.c0[c + 1] - cp.c0[c];
+      L.row_ptr[lev[c] + 1] += ns;
+      if (ns >= 2) L.ch_ptr[lev[c] + 1]++;
+    }
+    for (int l = 0; l < L.nlevels; l++) {
+      L.row_ptr[l + 1] += L.row_ptr[l];
+      L.ch_ptr[l + 1] += L.ch_ptr[l];
+    }
+    L.rows.resize(n);
+    L.chunks.resize(L.ch_ptr[L.nlevels]);
+    std::vector<int> fr(L.row_ptr.begin(), L.row_ptr.end() - 1);
+    std::vector<int> fc(L.ch_ptr.begin(), L.ch_ptr.end() - 1);
+    for (int c = 0; c < nc; c++) {
+      const int ns = cp.c0[c + 1] - cp.c0[c];
+      for (int i = cp.c0[c]; i < cp.c0[c + 1]; i++) L.rows[fr[lev[c]]++] = i;
+      if (ns >= 2) L.chunks[fc[lev[c]]++] = c;
+    }
+    L.max_rows.assign(L.nlevels, 1);
+    for (int c = 0; c < nc; c++)
+      L.max_rows[lev[c]] = std::max(L.max_rows[lev[c]], cp.c0[c + 1] - cp.c0[c]);
+    L.cta.assign(L.nlevels, 0);
     for (int l = 0; l < L.nlevels; l++) {
       int maxlen = 0;
-      for (int k = L.ptr[l]; k < L.ptr[l + 1]; k++) {
+      for (int k = L.row_ptr[l]; k < L.row_ptr[l + 1]; k++) {
         const int i = L.rows[k];
-        const int len = upper ? f.frowp[i + 1] - f.fdiag[i] - 1 : f.fdiag[i] - f.frowp[i];
+        const int len = upper ? f.frowp[i + 1] - cp.row_ustart[i] : cp.row_lend[i] - f.frowp[i];
         maxlen = std::max(maxlen, len);
       }
-      cta[l] = (L.ptr[l + 1] - L.ptr[l] < SOLVE_NARROW_ROWS || maxlen > SOLVE_LONG_ROW) ? 1 : 0;
+      L.cta[l] = maxlen > SOLVE_LONG_ROW;
     }
   };
-  choose(f.lower, false, f.lower_cta);
-  // head upper: levels counting only head columns (tail values are final)
-  {
-    std::vector<int> ul(s, 0);
-    int maxl = 0;
-    for (int i = s - 1; i >= 0; i--) {
-      int l = 0;
-      for (int k = f.fdiag[i] + 1; k < f.frowp[i + 1]; k++) {
-        int c = f.fcols[k];
-        if (c < s) l = std::max(l, ul[c] + 1);
-      }
-      ul[i] = l;
-      maxl = std::max(maxl, l);
-    }
-    LevelSchedule &U = f.upper;
-    U.nlevels = s ? maxl + 1 : 0;
-    U.ptr.assign(U.nlevels + 1, 0);
-    for (int i = 0; i < s; i++) U.ptr[ul[i] + 1]++;
-    for (int l = 0; l < U.nlevels; l++) U.ptr[l + 1] += U.ptr[l];
-    U.rows.resize(s);
-    std::vector<int> fill(U.ptr.begin(), U.ptr.end() - 1);
-    for (int i = 0; i < s; i++) U.rows[fill[ul[i]]++] = i;
-  }
-  choose(f.upper, true, f.upper_cta);
-  f.lsplit.assign(d, 0);
-  f.tl_ptr.assign(1, 0);
-  f.tu_ptr.assign(1, 0);
-  f.tl_row.clear();
-  f.tl_pos.clear();
-  f.tl_col.clear();
-  f.tu_row.clear();
-  f.tu_pos.clear();
-  f.tu_col.clear();
-  f.td_row.clear();
-  f.td_pos.clear();
-  f.td_col.clear();
-  f.dense_t0 = n;
-  f.dense_n = 0;
-  if (d == 0) return;
-  // Dense trailing block [t0, n): the largest multiple of DENSE_PANEL block
-  // rows, at most DENSE_MAX and inside the tail, whose factor blocks fill at
-  // least DENSE_MIN_FILL of it.  nnz_from[t] = factor blocks (i, c) with
-  // min(i, c) >= t.
-  {
-    std::vector<long long> nnz_from(n + 1, 0);
-    for (int i = 0; i < n; i++)
-      for (int k = f.frowp[i]; k < f.frowp[i + 1]; k++) nnz_from[std::min(i, f.fcols[k])]++;
-    for (int t = n - 1; t >= 0; t--) nnz_from[t] += nnz_from[t + 1];
-    for (int nd = std::min(DENSE_MAX, d) / DENSE_PANEL * DENSE_PANEL; nd >= DENSE_MIN; nd -= DENSE_PANEL) {
-      const double fill = (double)nnz_from[n - nd] / ((double)nd * nd);
-      if (fill >= DENSE_MIN_FILL) {
-        f.dense_t0 = n - nd;
-        f.dense_n = nd;
-        break;
-      }
-    }
-  }
-  const int t0 = f.dense_t0;
-  // lower tail: pivot columns in [s, t0) push into every later row; levels
-  // over the middle columns, push lists grouped by pivot level
-  std::vector<int> tl(d, 0);
-  int maxl = 0;
-  for (int i = s; i < n; i++) {
-    int k = f.frowp[i];
-    while (k < f.fdiag[i] && f.fcols[k] < s) k++;
-    f.lsplit[i - s] = k;
-    if (i >= t0) continue;
-    int l = 0;
-    for (; k < f.fdiag[i]; k++) l = std::max(l, tl[f.fcols[k] - s] + 1);
-    tl[i - s] = l;
-    maxl = std::max(maxl, l);
-  }
-  if (t0 > s) {
-    std::vector<long long> cnt(maxl + 2, 0);
-    for (int i = s; i < n; i++)
-      for (int k = f.lsplit[i - s]; k < f.fdiag[i] && f.fcols[k] < t0; k++)
-        cnt[tl[f.fcols[k] - s] + 1]++;
-    for (int l = 0; l <= maxl; l++) cnt[l + 1] += cnt[l];
-    const long long tot = cnt[maxl + 1];
-    f.tl_row.resize(tot);
-    f.tl_pos.resize(tot);
-    f.tl_col.resize(tot);
-    std::vector<long long> fill(cnt.begin(), cnt.end() - 1);
-    for (int i = s; i < n; i++)
-      for (int k = f.lsplit[i - s]; k < f.fdiag[i] && f.fcols[k] < t0; k++) {
-        long long p = fill[tl[f.fcols[k] - s]]++;
-        f.tl_row[p] = i;
-        f.tl_pos[p] = k;
-        f.tl_col[p] = f.fcols[k];
-      }
-    f.tl_ptr.resize(maxl + 2);
-    for (int l = 0; l <= maxl + 1; l++) f.tl_ptr[l] = (int)cnt[l];
-  }
-  // upper tail, middle rows [s, t0) only (the dense block is solved whole):
-  // (a) couplings to dense columns, all final after the dense solve: one list;
-  // (b) middle columns in reverse level order
-  for (int i = s; i < t0; i++)
-    for (int k = f.fdiag[i] + 1; k < f.frowp[i + 1]; k++)
-      if (f.fcols[k] >= t0) {
-        f.td_row.push_back(i);
-        f.td_pos.push_back(k);
-        f.td_col.push_back(f.fcols[k]);
-      }
-  std::vector<int> tu(d, 0);
-  maxl = 0;
-  for (int i = t0 - 1; i >= s; i--) {
-    int l = 0;
-    for (int k = f.fdiag[i] + 1; k < f.frowp[i + 1] && f.fcols[k] < t0; k++)
-      l = std::max(l, tu[f.fcols[k] - s] + 1);
-    tu[i - s] = l;
-    maxl = std::max(maxl, l);
-  }
-  if (t0 > s) {
-    std::vector<long long> cnt(maxl + 2, 0);
-    for (int i = s; i < t0; i++)
-      for (int k = f.fdiag[i] + 1; k < f.frowp[i + 1] && f.fcols[k] < t0; k++)
-        cnt[tu[f.fcols[k] - s] + 1]++;
-    for (int l = 0; l <= maxl; l++) cnt[l + 1] += cnt[l];
-    const long long tot = cnt[maxl + 1];
-    f.tu_row.resize(tot);
-    f.tu_pos.resize(tot);
-    f.tu_col.resize(tot);
-    std::vector<long long> fill(cnt.begin(), cnt.end() - 1);
-    for (int i = s; i < t0; i++)
-      for (int k = f.fdiag[i] + 1; k < f.frowp[i + 1] && f.fcols[k] < t0; k++) {
-        long long p = fill[tu[f.fcols[k] - s]]++;
-        f.tu_row[p] = i;
-        f.tu_pos[p] = k;
-        f.tu_col[p] = f.fcols[k];
-      }
-    f.tu_ptr.resize(maxl + 2);
-    for (int l = 0; l <= maxl + 1; l++) f.tu_ptr[l] = (int)cnt[l];
-  }
+  fill_levels(lv, maxl, false, cp.lo);
+  fill_levels(uv, maxu, true, cp.up);
 }
 
 int upload_schedules(Factor &f, cudaStream_t s) {
   int rc;
   if ((rc = f.flv.d_rows.upload(f.flv.rows.data(), f.flv.rows.size(), s))) return rc;
-  if ((rc = f.lower.d_rows.upload(f.lower.rows.data(), f.lower.rows.size(), s))) return rc;
-  if ((rc = f.upper.d_rows.upload(f.upper.rows.data(), f.upper.rows.size(), s))) return rc;
   if ((rc = f.d_task_row.upload(f.task_row.data(), f.task_row.size(), s))) return rc;
   if ((rc = f.d_task_ptr.upload(f.task_ptr.data(), f.task_ptr.size(), s))) return rc;
   if ((rc = f.d_task_jp.upload(f.task_jp.data(), f.task_jp.size(), s))) return rc;
-  if ((rc = f.d_lsplit.upload(f.lsplit.data(), f.lsplit.size(), s))) return rc;
-  if ((rc = f.d_tl_row.upload(f.tl_row.data(), f.tl_row.size(), s))) return rc;
-  if ((rc = f.d_tl_pos.upload(f.tl_pos.data(), f.tl_pos.size(), s))) return rc;
-  if ((rc = f.d_tl_col.upload(f.tl_col.data(), f.tl_col.size(), s))) return rc;
-  if ((rc = f.d_tu_row.upload(f.tu_row.data(), f.tu_row.size(), s))) return rc;
-  if ((rc = f.d_tu_pos.upload(f.tu_pos.data(), f.tu_pos.size(), s))) return rc;
-  if ((rc = f.d_tu_col.upload(f.tu_col.data(), f.tu_col.size(), s))) return rc;
-  if ((rc = f.d_td_row.upload(f.td_row.data(), f.td_row.size(), s))) return rc;
-  if ((rc = f.d_td_pos.upload(f.td_pos.data(), f.td_pos.size(), s))) return rc;
-  if ((rc = f.d_td_col.upload(f.td_col.data(), f.td_col.size(), s))) return rc;
+  const ChunkPlan &cp = f.cp;
+  if ((rc = f.d_ck_c0.upload(cp.c0.data(), cp.c0.size(), s))) return rc;
+  if ((rc = f.d_ck_off.upload(cp.off.data(), cp.off.size(), s))) return rc;
+  if ((rc = f.d_row_lend.upload(cp.row_lend.data(), cp.row_lend.size(), s))) return rc;
+  if ((rc = f.d_row_ustart.upload(cp.row_ustart.data(), cp.row_ustart.size(), s))) return rc;
+  if ((rc = f.d_row_single.upload(cp.row_single.data(), cp.row_single.size(), s))) return rc;
+  if ((rc = f.d_lo_rows.upload(cp.lo.rows.data(), cp.lo.rows.size(), s))) return rc;
+  if ((rc = f.d_lo_chunks.upload(cp.lo.chunks.data(), cp.lo.chunks.size(), s))) return rc;
+  if ((rc = f.d_up_rows.upload(cp.up.rows.data(), cp.up.rows.size(), s))) return rc;
+  if ((rc = f.d_up_chunks.upload(cp.up.chunks.data(), cp.up.chunks.size(), s))) return rc;
   const PanelSchedule &pn = f.pn;
   if ((rc = f.d_pn_prow.upload(pn.prow.data(), pn.prow.size(), s))) return rc;
   if ((rc = f.d_pn_uc.upload(pn.uc.data(), pn.uc.size(), s))) return rc;

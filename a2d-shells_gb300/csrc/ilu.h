@@ -45,6 +45,37 @@ struct PanelSchedule {
   std::vector<int> task_ptr, task_row, task_jpk;
 };
 
+// Chunked triangular solves.  Rows are cut into chunks of consecutive rows:
+// a chunk ends before row i when row i has no L block in column i - 1, or
+// when it reaches CHUNK_MAX rows.  Within a chunk every row may depend on
+// the earlier ones, so its diagonal block is solved as one dense operator
+// (the inverse of its unit-lower part and of its D + U part, built after
+// the numeric factorization); the chunk's other factor blocks point to
+// earlier chunks (lower) or later ones (upper).  Chunks are scheduled by
+// dependency levels over those external columns: one launch pulls the
+// external sums of every row of the level, one applies the chunk inverses.
+// On the AMD-ordered cylinders this gives 16 levels at 256x512 and 43 at
+// 512x1024 (CHUNK_MAX 128), against 1,893 and 3,810 row levels.
+struct ChunkLevels {
+  int nlevels = 0;
+  std::vector<int> row_ptr, rows;   // rows of each level
+  std::vector<int> ch_ptr, chunks;  // chunks of >= 2 rows of each level
+  std::vector<char> cta;            // per level: 1 = one CTA per row (long rows)
+  std::vector<int> max_rows;        // per level: rows of its largest chunk
+};
+struct ChunkPlan {
+  std::vector<int> c0;          // chunk starts (nchunks + 1 entries, last = n)
+  std::vector<long long> off;   // per chunk: offset of its L inverse ((6 ns)^2 values,
+                                // row-major), the U inverse follows; -1 for one row
+  long long inv_size = 0;       // values of all inverses
+  long long scr_size = 0;       // values of all gathered diagonal blocks
+  int max_rows = 0;             // largest chunk
+  std::vector<int> row_lend;    // per row: end of its lower pull (first column >= its chunk)
+  std::vector<int> row_ustart;  // per row: start of its upper pull (first column past its chunk)
+  std::vector<int> row_single;  // per row: 1 if its chunk is the row alone
+  ChunkLevels lo, up;           // up: level 0 solved first (top of the ordering)
+};
+
 // A factorization handle (the TACSSchurPc role on one GPU).
 struct Factor {
   int n = 0, lev_fill = 0, precision = 64;
@@ -53,9 +84,6 @@ struct Factor {
   DBuf<double> F64;
   DBuf<float> F32;
   LevelSchedule flv;           // dependency levels of all rows (factorization)
-  LevelSchedule lower, upper;  // head rows [0, tail_s): row-oriented solves
-  // per head level: 1 = one CTA per row (few or long rows), 0 = one warp per row
-  std::vector<char> lower_cta, upper_cta;
   // right-looking update tasks, grouped by level; within a level the tasks
   // of long target rows (> FACTOR_WARP_COLS blocks) come first
   std::vector<int> task_level_ptr, task_nlong, task_row, task_ptr, task_jp;
@@ -64,19 +92,15 @@ struct Factor {
   PanelSchedule pn;
   DBuf<int> d_pn_prow, d_pn_uc, d_pn_tab, d_pn_tp, d_pn_task_row, d_pn_task_jpk;
   DBuf<int> d_task_row, d_task_ptr, d_task_jp;
-  // dense tail rows [tail_s, n): head pull split and column push lists
-  int tail_s = 0;
-  std::vector<int> lsplit, tl_ptr, tl_row, tl_pos, tl_col, tu_ptr, tu_row, tu_pos, tu_col;
-  std::vector<int> td_row, td_pos, td_col;  // upper couplings of middle rows to dense columns
-  DBuf<int> d_lsplit, d_tl_row, d_tl_pos, d_tl_col, d_tu_row, d_tu_pos, d_tu_col;
-  DBuf<int> d_td_row, d_td_pos, d_td_col;
-  // dense trailing block rows [dense_t0, n), dense_n = n - dense_t0 (a
-  // multiple of DENSE_PANEL, 0 = none): the factor's blocks there copied into
-  // a dense row-major (6 dense_n)^2 array, plus the inverses of its diagonal
-  // panels (unit-lower L and D + U, (6 DENSE_PANEL)^2 each)
-  int dense_t0 = 0, dense_n = 0;
-  DBuf<double> dense64, pinvL64, pinvU64, dwork64;
-  DBuf<float> dense32, pinvL32, pinvU32, dwork32;
+  // Chunked triangular solves (see ChunkPlan); host plan, device copies and
+  // the inverses of the chunks' diagonal blocks (rebuilt after every
+  // numeric factorization)
+  ChunkPlan cp;
+  DBuf<int> d_ck_c0, d_row_lend, d_row_ustart, d_row_single;
+  DBuf<long long> d_ck_off;
+  DBuf<int> d_lo_rows, d_lo_chunks, d_up_rows, d_up_chunks;
+  DBuf<double> cinv64, cscr64;
+  DBuf<float> cinv32, cscr32;
   // algorithmic FP operations of one numeric factorization: 432 per L block
   // (L_ij = A_ij D_j^{-1}), 432 per block update, 432 per diagonal inverse
   double flop_count = 0.0;
@@ -91,15 +115,14 @@ void build_levels(int n, const std::vector<int> &frowp, const std::vector<int> &
                   const std::vector<int> &fdiag, bool upper, LevelSchedule &L,
                   std::vector<int> *level_of = nullptr);
 void build_update_tasks(Factor &f, const std::vector<int> &lev);
-// Split rows into the head (row-oriented level solves) and the dense tail
-// (column-oriented pushes) and build both schedules; lev = factor levels.
-void build_solve_schedule(Factor &f, const std::vector<int> &lev, int narrow);
+// The chunked solve plan of f's pattern (ChunkPlan).
+void build_solve_schedule(Factor &f);
 int upload_schedules(Factor &f, cudaStream_t s);
-// Allocate the dense-block buffers of f for its precision.
-int dense_alloc(Factor &f);
-// Copy the factored values of the dense block out of F and invert its
-// diagonal panels (after the numeric factorization).
-int dense_build(Factor &f, const void *F, cudaStream_t s, long long *launches);
+// Allocate the chunk-inverse buffers of f for its precision.
+int chunk_alloc(Factor &f);
+// Gather every chunk's diagonal block out of the factored values F and
+// invert its unit-lower and D + U parts (after the numeric factorization).
+int chunk_build(Factor &f, const void *F, cudaStream_t s, long long *launches);
 
 // Update kernels: target rows with at most FACTOR_WARP_COLS blocks are
 // updated by a group of 6, 12 or 30 lanes, longer ones by one CTA (column
@@ -118,18 +141,10 @@ constexpr long long PANEL_TABLE_MAX = 1LL << 28;
 // union U columns of a panel staged in shared memory by its phase-2 kernel
 constexpr int PANEL_UC_SMEM = 8192;
 
-// Dense trailing block of the solves: panels of DENSE_PANEL block rows,
-// between DENSE_MIN and DENSE_MAX block rows, used when the factor fills at
-// least DENSE_MIN_FILL of it.
-constexpr int DENSE_PANEL = 32;
-// Head solve levels use one CTA per row when they have fewer than
-// SOLVE_NARROW_ROWS rows or a row longer than SOLVE_LONG_ROW blocks (a warp
-// would walk the long row alone), one warp per row otherwise.
-constexpr int SOLVE_NARROW_ROWS = 48;
+// Largest chunk of the solves (block rows), and the row length above which
+// a pull level uses one CTA per row.
+constexpr int CHUNK_MAX = 128;
 constexpr int SOLVE_LONG_ROW = 24;
-constexpr int DENSE_MIN = 64;
-constexpr int DENSE_MAX = 2048;
-constexpr double DENSE_MIN_FILL = 0.4;
 
 // F (f.precision: 64 double, 48 double-float, 32 float values; 8 bytes per
 // value for 64 and 48) <- pattern-embedded copy of A (+ alpha2 * A2 when

@@ -158,7 +158,7 @@ int factor_setup(Mesh &m, int lev_fill, int precision, Factor &f) {
   std::vector<int> lev;
   build_levels(m.nn, f.frowp, f.fcols, f.fdiag, false, f.flv, &lev);
   build_update_tasks(f, lev);
-  build_solve_schedule(f, lev, 48);
+  build_solve_schedule(f);
   if ((rc = upload_schedules(f, m.stream))) return rc;
   if ((rc = f.d_frowp.upload(f.frowp.data(), f.frowp.size(), m.stream))) return rc;
   if ((rc = f.d_fcols.upload(f.fcols.data(), f.fcols.size(), m.stream))) return rc;
@@ -169,7 +169,7 @@ int factor_setup(Mesh &m, int lev_fill, int precision, Factor &f) {
   } else {
     if ((rc = f.F64.alloc((size_t)f.nnzb() * 36))) return rc;
   }
-  if ((rc = dense_alloc(f))) return rc;
+  if ((rc = chunk_alloc(f))) return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   return 0;
 }
@@ -187,14 +187,6 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   f.flv.nlevels = src.flv.nlevels;
   f.flv.ptr = src.flv.ptr;
   f.flv.rows = src.flv.rows;
-  f.lower.nlevels = src.lower.nlevels;
-  f.lower.ptr = src.lower.ptr;
-  f.lower.rows = src.lower.rows;
-  f.upper.nlevels = src.upper.nlevels;
-  f.upper.ptr = src.upper.ptr;
-  f.upper.rows = src.upper.rows;
-  f.lower_cta = src.lower_cta;
-  f.upper_cta = src.upper_cta;
   f.task_level_ptr = src.task_level_ptr;
   f.task_nlong = src.task_nlong;
   f.task_group = src.task_group;
@@ -202,21 +194,7 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   f.task_row = src.task_row;
   f.task_ptr = src.task_ptr;
   f.task_jp = src.task_jp;
-  f.tail_s = src.tail_s;
-  f.lsplit = src.lsplit;
-  f.tl_ptr = src.tl_ptr;
-  f.tl_row = src.tl_row;
-  f.tl_pos = src.tl_pos;
-  f.tl_col = src.tl_col;
-  f.tu_ptr = src.tu_ptr;
-  f.tu_row = src.tu_row;
-  f.tu_pos = src.tu_pos;
-  f.tu_col = src.tu_col;
-  f.td_row = src.td_row;
-  f.td_pos = src.td_pos;
-  f.td_col = src.td_col;
-  f.dense_t0 = src.dense_t0;
-  f.dense_n = src.dense_n;
+  f.cp = src.cp;
   f.flop_count = src.flop_count;
   if ((rc = upload_schedules(f, m.stream))) return rc;
   if ((rc = f.d_frowp.upload(f.frowp.data(), f.frowp.size(), m.stream))) return rc;
@@ -228,7 +206,7 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   } else {
     if ((rc = f.F64.alloc((size_t)f.nnzb() * 36))) return rc;
   }
-  if ((rc = dense_alloc(f))) return rc;
+  if ((rc = chunk_alloc(f))) return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
   return 0;
 }
@@ -240,7 +218,7 @@ int factor_numeric(Mesh &m, Factor &f, const double *A, const double *A2, double
   if ((rc = factor_scatter(f, m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, F, m.stream))) return rc;
   m.launches++;
   if ((rc = factor_levels(f, F, f.d_status.p, m.stream, &m.launches))) return rc;
-  return dense_build(f, F, m.stream, &m.launches);
+  return chunk_build(f, F, m.stream, &m.launches);
 }
 
 int factor_check(Mesh &m, Factor &f) {

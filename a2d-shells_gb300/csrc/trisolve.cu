@@ -8,18 +8,19 @@
 //
 // Vectors hold R right-hand sides row-major: entry (row, dof, rhs) at
 // (row * 6 + dof) * R + rhs, so one factor block is loaded once and applied
-// to all R vectors.  Rows of the head (levels with many rows) are solved one
-// warp per row (five 6-lane groups stride over the row's blocks), narrow
-// levels one 256-thread block per row, the middle of the tail
-// column-oriented (each final pivot pushes its column into later rows with
-// FP64 atomics), and the trailing separator rows as one dense block, panel
-// by panel.  solve_graph() captures the whole launch sequence once per
-// (factor, x, y, R) and replays it.
+// to all R vectors.  The rows are cut into chunks of consecutive rows
+// (ChunkPlan, ilu.h) scheduled by dependency levels; per level one launch
+// pulls, for every row of the level, the sums over its factor blocks outside
+// its chunk (a warp per row, or a CTA per row on levels with long rows), and
+// one launch applies each chunk's precomputed dense inverse (unit-lower for
+// L, D + U for the upper solve) to its rows.  A one-row chunk needs no
+// inverse: the pull finishes it (times D_i^{-1} in the upper solve).
+// solve_graph() captures the whole launch sequence once per (factor, x, y,
+// R) and replays it.
 #include "a2ds_internal.h"
 #include "ilu.h"
 
 namespace a2ds {
-
 
 // Partial sums of sum_k F_k[ii][:] y[fcols[k]] over k = kb + g, kb + g + step, ...
 template <typename T, typename TV, int R>
@@ -39,64 +40,48 @@ __device__ __forceinline__ void row_partial(int kb, int ke, int g, int step, int
   }
 }
 
-// Forward substitution, one warp per row of a level.
-template <typename T, typename TV, int R>
-__global__ void __launch_bounds__(256) k_lower_warp(const int *__restrict__ rows, int nrows,
-                                                    const int *__restrict__ frowp,
-                                                    const int *__restrict__ fcols,
-                                                    const int *__restrict__ fdiag,
-                                                    const T *__restrict__ F, const TV *x, TV *y) {
+// y_i = src_i - sum_{k in [beg_i, end_i)} F_k y_{fcols[k]} for every row of
+// a level, one warp per row (five groups of six lanes over the blocks).  In
+// the upper solve (UPPER) a row that is its own chunk is finished here:
+// y_i = D_i^{-1} (src_i - sum).  Lower: beg = frowp, end = row_lend, src = x;
+// upper: beg = row_ustart, end = frowp + 1, src = y.
+template <typename T, typename TV, int R, bool UPPER>
+__global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows, int nrows,
+                                                   const int *__restrict__ frowp,
+                                                   const int *__restrict__ bound,
+                                                   const int *__restrict__ single,
+                                                   const int *__restrict__ fcols,
+                                                   const int *__restrict__ fdiag,
+                                                   const T *__restrict__ F, const TV *src, TV *y) {
   __shared__ TV part[8][30][R];
+  __shared__ TV z[8][6][R];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wr = blockIdx.x * 8 + wib;
   if (wr >= nrows) return;  // whole warp leaves together
   const int i = rows[wr];
   const int g = lane / 6, ii = lane - 6 * g;
+  const int kb = UPPER ? bound[i] : frowp[i];
+  const int ke = UPPER ? frowp[i + 1] : bound[i];
   TV acc[R];
 #pragma unroll
   for (int r = 0; r < R; r++) acc[r] = 0;
-  if (lane < 30) row_partial<T, TV, R>(frowp[i], fdiag[i], g, 5, ii, fcols, F, y, acc);
+  if (lane < 30) row_partial<T, TV, R>(kb, ke, g, 5, ii, fcols, F, y, acc);
   if (lane < 30)
 #pragma unroll
     for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
   __syncwarp();
+  const bool fin = UPPER && single[i];
   for (int o = lane; o < 6 * R; o += 32) {
     const int d = o / R, r = o - R * d;
-    TV v = part[wib][d][r] + part[wib][d + 6][r] + part[wib][d + 12][r] + part[wib][d + 18][r] +
-           part[wib][d + 24][r];
+    const TV v = part[wib][d][r] + part[wib][d + 6][r] + part[wib][d + 12][r] +
+                 part[wib][d + 18][r] + part[wib][d + 24][r];
     const size_t idx = ((size_t)i * 6 + d) * R + r;
-    y[idx] = x[idx] - v;
+    if (fin)
+      z[wib][d][r] = src[idx] - v;
+    else
+      y[idx] = src[idx] - v;
   }
-}
-
-// Backward substitution, one warp per row of a level.
-template <typename T, typename TV, int R>
-__global__ void __launch_bounds__(256) k_upper_warp(const int *__restrict__ rows, int nrows,
-                                                    const int *__restrict__ frowp,
-                                                    const int *__restrict__ fcols,
-                                                    const int *__restrict__ fdiag,
-                                                    const T *__restrict__ F, TV *y) {
-  __shared__ TV part[8][30][R];
-  __shared__ TV z[8][6][R];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wr = blockIdx.x * 8 + wib;
-  if (wr >= nrows) return;
-  const int i = rows[wr];
-  const int g = lane / 6, ii = lane - 6 * g;
-  TV acc[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) acc[r] = 0;
-  if (lane < 30) row_partial<T, TV, R>(fdiag[i] + 1, frowp[i + 1], g, 5, ii, fcols, F, y, acc);
-  if (lane < 30)
-#pragma unroll
-    for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
-  __syncwarp();
-  for (int o = lane; o < 6 * R; o += 32) {
-    const int d = o / R, r = o - R * d;
-    TV v = part[wib][d][r] + part[wib][d + 6][r] + part[wib][d + 12][r] + part[wib][d + 18][r] +
-           part[wib][d + 24][r];
-    z[wib][d][r] = y[((size_t)i * 6 + d) * R + r] - v;
-  }
+  if (!fin) return;
   __syncwarp();
   const T *Dinv = F + (size_t)fdiag[i] * 36;
   for (int o = lane; o < 6 * R; o += 32) {
@@ -108,14 +93,16 @@ __global__ void __launch_bounds__(256) k_upper_warp(const int *__restrict__ rows
   }
 }
 
-// Long rows of narrow levels: one 256-thread block per row, 42 groups of
-// six threads stride over the row's blocks.
+// The same for levels with long rows: one 256-thread CTA per row, 42 groups
+// of six threads over the row's blocks.
 template <typename T, typename TV, int R, bool UPPER>
-__global__ void __launch_bounds__(256) k_tri_block(const int *__restrict__ rows, int nrows,
-                                                   const int *__restrict__ frowp,
-                                                   const int *__restrict__ fcols,
-                                                   const int *__restrict__ fdiag,
-                                                   const T *__restrict__ F, const TV *x, TV *y) {
+__global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, int nrows,
+                                                  const int *__restrict__ frowp,
+                                                  const int *__restrict__ bound,
+                                                  const int *__restrict__ single,
+                                                  const int *__restrict__ fcols,
+                                                  const int *__restrict__ fdiag,
+                                                  const T *__restrict__ F, const TV *src, TV *y) {
   __shared__ TV part[252][R];
   __shared__ TV z[6][R];
   const int rr = blockIdx.x;
@@ -123,8 +110,8 @@ __global__ void __launch_bounds__(256) k_tri_block(const int *__restrict__ rows,
   const int i = rows[rr];
   const int t = threadIdx.x;
   const int g = t / 6, ii = t - 6 * g;
-  const int kb = UPPER ? fdiag[i] + 1 : frowp[i];
-  const int ke = UPPER ? frowp[i + 1] : fdiag[i];
+  const int kb = UPPER ? bound[i] : frowp[i];
+  const int ke = UPPER ? frowp[i + 1] : bound[i];
   if (t < 252) {
     TV acc[R];
 #pragma unroll
@@ -134,17 +121,18 @@ __global__ void __launch_bounds__(256) k_tri_block(const int *__restrict__ rows,
     for (int r = 0; r < R; r++) part[t][r] = acc[r];
   }
   __syncthreads();
+  const bool fin = UPPER && single[i];
   for (int o = t; o < 6 * R; o += blockDim.x) {
     const int d = o / R, r = o - R * d;
     TV v = 0;
     for (int gg = 0; gg < 42; gg++) v += part[6 * gg + d][r];
     const size_t idx = ((size_t)i * 6 + d) * R + r;
-    if (UPPER)
-      z[d][r] = y[idx] - v;
+    if (fin)
+      z[d][r] = src[idx] - v;
     else
-      y[idx] = x[idx] - v;
+      y[idx] = src[idx] - v;
   }
-  if (!UPPER) return;
+  if (!fin) return;
   __syncthreads();
   const T *Dinv = F + (size_t)fdiag[i] * 36;
   for (int o = t; o < 6 * R; o += blockDim.x) {
@@ -155,112 +143,6 @@ __global__ void __launch_bounds__(256) k_tri_block(const int *__restrict__ rows,
     y[((size_t)i * 6 + d) * R + r] = v;
   }
 }
-
-// ------------------------------------------------------------ tail solves
-// Rows [s, n) are the trailing separators, where levels hold a handful of
-// long rows.  Their head couplings are pulled once; then, tail level by tail
-// level, the columns of final pivots are pushed into the later rows.
-
-// y_i = x_i - sum_{j < s} L_ij y_j for every tail row i (one warp per row).
-template <typename T, typename TV, int R>
-__global__ void __launch_bounds__(256) k_tail_pull(int s, int d, const int *__restrict__ frowp,
-                                                   const int *__restrict__ fcols,
-                                                   const int *__restrict__ lsplit,
-                                                   const T *__restrict__ F, const TV *x, TV *y) {
-  __shared__ TV part[8][30][R];
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rr = blockIdx.x * 8 + wib;
-  if (rr >= d) return;
-  const int i = s + rr;
-  const int g = lane / 6, ii = lane - 6 * g;
-  TV acc[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) acc[r] = 0;
-  if (lane < 30) row_partial<T, TV, R>(frowp[i], lsplit[rr], g, 5, ii, fcols, F, y, acc);
-  if (lane < 30)
-#pragma unroll
-    for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
-  __syncwarp();
-  for (int o = lane; o < 6 * R; o += 32) {
-    const int dd = o / R, r = o - R * dd;
-    TV v = part[wib][dd][r] + part[wib][dd + 6][r] + part[wib][dd + 12][r] +
-           part[wib][dd + 18][r] + part[wib][dd + 24][r];
-    const size_t idx = ((size_t)i * 6 + dd) * R + r;
-    y[idx] = x[idx] - v;
-  }
-}
-
-// One tail level's column pushes; thread (entry e, rhs r).  Entry e is
-// (target row i, factor position p, pivot row j).  PUSH_L: y_i -= L_ij y_j.
-// PUSH_U: y_i -= U_ij D_j^{-1} y_j (y_j itself is scaled by D_j^{-1} only
-// after all tail levels, by k_tail_finalize).  PUSH_U_FINAL: y_i -= U_ij y_j
-// with y_j already final (dense-block columns).
-enum { PUSH_L = 0, PUSH_U = 1, PUSH_U_FINAL = 2 };
-template <typename T, typename TV, int R, int MODE>
-__global__ void __launch_bounds__(256) k_tail_push(const int *__restrict__ erow,
-                                                   const int *__restrict__ epos,
-                                                   const int *__restrict__ ecol, int ne,
-                                                   const int *__restrict__ fdiag,
-                                                   const T *__restrict__ F, TV *y) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int e = t / R, r = t - R * (t / R);
-  if (e >= ne) return;
-  const int i = erow[e], p = epos[e], j = ecol[e];
-  const T *A = F + (size_t)p * 36;
-  TV w[6];
-#pragma unroll
-  for (int b = 0; b < 6; b++) w[b] = y[((size_t)j * 6 + b) * R + r];
-  if (MODE == PUSH_U) {
-    const T *Dinv = F + (size_t)fdiag[j] * 36;
-    TV v[6];
-#pragma unroll
-    for (int a = 0; a < 6; a++) {
-      TV acc = 0;
-#pragma unroll
-      for (int b = 0; b < 6; b++) acc += (TV)Dinv[6 * a + b] * w[b];
-      v[a] = acc;
-    }
-#pragma unroll
-    for (int a = 0; a < 6; a++) w[a] = v[a];
-  }
-#pragma unroll
-  for (int a = 0; a < 6; a++) {
-    TV acc = 0;
-#pragma unroll
-    for (int b = 0; b < 6; b++) acc += (TV)A[6 * a + b] * w[b];
-    atomicAdd(&y[((size_t)i * 6 + a) * R + r], -acc);
-  }
-}
-
-// y_j = D_j^{-1} z_j for tail rows j in [s, s + d); thread (row, rhs).
-template <typename T, typename TV, int R>
-__global__ void k_tail_finalize(int s, int d, const int *__restrict__ fdiag,
-                                const T *__restrict__ F, TV *y) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int rr = t / R, r = t - R * (t / R);
-  if (rr >= d) return;
-  const int j = s + rr;
-  const T *Dinv = F + (size_t)fdiag[j] * 36;
-  TV z[6];
-#pragma unroll
-  for (int b = 0; b < 6; b++) z[b] = y[((size_t)j * 6 + b) * R + r];
-#pragma unroll
-  for (int a = 0; a < 6; a++) {
-    TV v = 0;
-#pragma unroll
-    for (int b = 0; b < 6; b++) v += (TV)Dinv[6 * a + b] * z[b];
-    y[((size_t)j * 6 + a) * R + r] = v;
-  }
-}
-
-// ------------------------------------------------------ dense trailing block
-// The last dense_n block rows are solved as a dense (6 dense_n)^2 system,
-// DENSE_PANEL block rows (PB6 unknowns) at a time: w = P_pp y_p with the
-// precomputed inverse of the diagonal panel, then the rows beyond the panel
-// (below it for L, above it for U) subtract M[rows, panel] w.  Two launches
-// per panel instead of one per row, and the work of a panel is spread over
-// the whole GPU.
-constexpr int PB6 = 6 * DENSE_PANEL;
 
 // Sum of v[r] over the warp for every r, spread over the lanes: halving
 // exchanges (offsets 16, 8, ...) leave each lane one partial sum for RHS
@@ -290,289 +172,218 @@ __device__ __forceinline__ TV warp_reduce_scatter(TV (&v)[R], int lane, int &rhs
   return sum;
 }
 
-// Stage a PB6 x R vector (row-major, [c][r]) in shared memory as [r][c], so
-// that lanes reading consecutive c hit consecutive banks.
-template <typename TV, int R>
-__device__ __forceinline__ void stage_panel_vec(TV *sv, const TV *v) {
-  for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) sv[(k % R) * PB6 + k / R] = v[k];
-}
-
-// acc[q][r] = sum_c row_q[c] sv[r][c] over this lane's columns (lane + 32 j).
-template <typename T, typename TV, int R, int NQ>
-__device__ __forceinline__ void panel_rows_dot(const T *const (&rows)[NQ], const TV *sv, int lane,
-                                               TV (&acc)[NQ][R]) {
-  T m[NQ][6];
-#pragma unroll
-  for (int q = 0; q < NQ; q++)
-#pragma unroll
-    for (int j = 0; j < 6; j++) m[q][j] = rows[q] ? rows[q][lane + 32 * j] : T(0);
-#pragma unroll
-  for (int q = 0; q < NQ; q++)
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      TV s = 0;
-#pragma unroll
-      for (int j = 0; j < 6; j++) s += (TV)m[q][j] * sv[r * PB6 + lane + 32 * j];
-      acc[q][r] = s;
-    }
-}
-
-// w = P v, P = PB6 x PB6 row-major, v and w PB6 x R; one warp per row of P.
-template <typename T, typename TV, int R>
-__global__ void __launch_bounds__(256) k_dense_panel_apply(const T *__restrict__ P, const TV *v,
-                                                           TV *__restrict__ w) {
-  static_assert(PB6 == 6 * 32, "a panel row is six warp-wide segments");
-  __shared__ TV sv[PB6 * R];
-  stage_panel_vec<TV, R>(sv, v);
+// y_c <- Inv_c y_c for every chunk c of a level (one CTA per chunk): the
+// chunk's rows (6 ns x R values, the pulled sums) are staged in shared
+// memory, then each warp takes rows of the inverse (row-major, 6 ns wide;
+// lower: only columns up to the row's block, upper: from it on), lanes over
+// the columns, and a reduce-scatter over the R right-hand sides.
+template <typename T, typename TV, int R, bool UPPER>
+__global__ void __launch_bounds__(256) k_chunk_apply(const int *__restrict__ chunks,
+                                                     const int *__restrict__ c0,
+                                                     const long long *__restrict__ off,
+                                                     const T *__restrict__ inv, TV *y) {
+  extern __shared__ unsigned char smem_raw[];
+  TV *sv = reinterpret_cast<TV *>(smem_raw);  // [r][col], 6 ns x R
+  const int c = chunks[blockIdx.x];
+  const int a = c0[c], ns = c0[c + 1] - a, w = 6 * ns;
+  const T *Inv = inv + off[c] + (UPPER ? (long long)w * w : 0);
+  TV *yc = y + (size_t)a * 6 * R;
+  for (int k = threadIdx.x; k < w * R; k += blockDim.x) sv[(k % R) * w + k / R] = yc[k];
   __syncthreads();
-  const int row = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (row >= PB6) return;
-  const T *rows[1] = {P + (size_t)row * PB6};
-  TV acc[1][R];
-  panel_rows_dot<T, TV, R, 1>(rows, sv, lane, acc);
-  int rhs;
-  const TV sum = warp_reduce_scatter<TV, R>(acc[0], lane, rhs);
-  if ((lane & (32 / R - 1)) == 0) w[(size_t)row * R + rhs] = sum;
-}
-
-// Rows [r0, r0 + nrows) of the dense segment yD: y -= M[rows, c0 : c0 + PB6] w;
-// CTA 0 also stores w as the panel's final values (yD rows c0 ..).  Each
-// warp takes DENSE_ROWS_PER_WARP rows, two at a time (their twelve loads
-// issued together); M is the dense block, leading dimension ld.
-constexpr int DENSE_ROWS_PER_WARP = 4;
-template <typename T, typename TV, int R>
-__global__ void __launch_bounds__(256) k_dense_panel_update(const T *__restrict__ M, int ld,
-                                                            int r0, int nrows, int c0,
-                                                            const TV *__restrict__ w, TV *yD) {
-  __shared__ TV sw[PB6 * R];
-  stage_panel_vec<TV, R>(sw, w);
-  if (blockIdx.x == 0)
-    for (int k = threadIdx.x; k < PB6 * R; k += blockDim.x) yD[(size_t)c0 * R + k] = w[k];
-  __syncthreads();
-  const int warp = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-#pragma unroll 1
-  for (int q = 0; q < DENSE_ROWS_PER_WARP; q += 2) {
-    const int rr = warp * DENSE_ROWS_PER_WARP + q;
-    if (rr >= nrows) break;
-    const T *rows[2] = {M + (size_t)(r0 + rr) * ld + c0,
-                        rr + 1 < nrows ? M + (size_t)(r0 + rr + 1) * ld + c0 : nullptr};
-    TV acc[2][R];
-    panel_rows_dot<T, TV, R, 2>(rows, sw, lane, acc);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int row = warp; row < w; row += nw) {
+    const int blk = row / 6;
+    const int cb = UPPER ? 6 * blk : 0, ce = UPPER ? w : 6 * blk + 6;
+    const T *Ir = Inv + (size_t)row * w;
+    TV acc[R];
 #pragma unroll
-    for (int d = 0; d < 2; d++) {
-      int rhs;
-      const TV sum = warp_reduce_scatter<TV, R>(acc[d], lane, rhs);
-      if (rr + d < nrows && (lane & (32 / R - 1)) == 0)
-        yD[(size_t)(r0 + rr + d) * R + rhs] -= sum;
+    for (int r = 0; r < R; r++) acc[r] = 0;
+    for (int col = cb + lane; col < ce; col += 32) {
+      const TV m = (TV)Ir[col];
+#pragma unroll
+      for (int r = 0; r < R; r++) acc[r] += m * sv[r * w + col];
     }
+    int rhs;
+    const TV sum = warp_reduce_scatter<TV, R>(acc, lane, rhs);
+    if ((lane & (32 / R - 1)) == 0) yc[(size_t)row * R + rhs] = sum;
   }
 }
 
-// Copy the factor's blocks of the dense block rows into the dense array
-// (zeroed beforehand); one warp per block row.
+// Dense copy of every multi-row chunk's diagonal block out of the factor
+// (scratch zeroed beforehand; chunk c's (6 ns)^2 block at off[c] / 2, since
+// the inverse storage holds two blocks per chunk), one CTA per chunk, one
+// warp per row: the row's blocks inside its chunk are [row_lend, row_ustart).
 template <typename T>
-__global__ void k_dense_scatter(int t0, int nd, const int *__restrict__ frowp,
-                                const int *__restrict__ fcols, const T *__restrict__ F,
-                                T *__restrict__ M) {
-  const int rr = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (rr >= nd) return;
-  const int i = t0 + rr, ld = 6 * nd;
-  int k0 = frowp[i];
-  const int k1 = frowp[i + 1];
-  while (k0 < k1 && fcols[k0] < t0) k0++;  // columns are sorted
-  const int nb = k1 - k0;
-  for (int idx = lane; idx < nb * 36; idx += 32) {
-    const int k = k0 + idx / 36, e = idx % 36;
-    const int a = e / 6, b = e % 6;
-    M[(size_t)(6 * rr + a) * ld + 6 * (fcols[k] - t0) + b] = F[(size_t)k * 36 + e];
+__global__ void __launch_bounds__(256) k_chunk_gather(const int *__restrict__ chunks,
+                                                      const int *__restrict__ c0,
+                                                      const long long *__restrict__ off,
+                                                      const int *__restrict__ fcols,
+                                                      const int *__restrict__ row_lend,
+                                                      const int *__restrict__ row_ustart,
+                                                      const T *__restrict__ F,
+                                                      T *__restrict__ Mall) {
+  const int ch = chunks[blockIdx.x];
+  const int a = c0[ch], ns = c0[ch + 1] - a, w = 6 * ns;
+  T *M = Mall + off[ch] / 2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int r = warp; r < ns; r += nw) {
+    const int i = a + r, k0 = row_lend[i], k1 = row_ustart[i];
+    for (int idx = lane; idx < (k1 - k0) * 36; idx += 32) {
+      const int k = k0 + idx / 36, e = idx % 36;
+      const int ea = e / 6, eb = e % 6;
+      M[(size_t)(6 * r + ea) * w + 6 * (fcols[k] - a) + eb] = F[(size_t)k * 36 + e];
+    }
   }
 }
 
-// Inverse of every diagonal panel, thread (panel, column c).  Lower: the
-// unit block-lower L_pp, forward substitution on e_c.  Upper: D + U_pp with
-// the stored D_i^{-1}: z_i = D_i^{-1} (e_c - sum_{j > i} U_ij z_j), backward.
+// Inverses of every multi-row chunk's diagonal block, one CTA per chunk and
+// one thread per column c of the identity.  Lower: the unit block-lower L
+// (forward substitution).  Upper: D + U with the stored D_i^{-1}:
+// z_i = D_i^{-1} (e_c - sum_{j > i} U_ij z_j), backward.
 template <typename T, bool UPPER>
-__global__ void k_dense_panel_inverse(const T *__restrict__ M, int ld, int npanels,
-                                      T *__restrict__ Pinv) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int p = t / PB6, c = t % PB6;
-  if (p >= npanels) return;
-  const T *Mp = M + (size_t)p * PB6 * ld + (size_t)p * PB6;
-  T *X = Pinv + (size_t)p * PB6 * PB6;
-  if (!UPPER) {
-    for (int i = 0; i < DENSE_PANEL; i++)
-      for (int a = 0; a < 6; a++) {
-        const int r = 6 * i + a;
-        T v = (r == c) ? T(1) : T(0);
-        for (int q = 0; q < 6 * i; q++) v -= Mp[(size_t)r * ld + q] * X[(size_t)q * PB6 + c];
-        X[(size_t)r * PB6 + c] = v;
-      }
-  } else {
-    for (int i = DENSE_PANEL - 1; i >= 0; i--) {
-      T z[6];
-      for (int a = 0; a < 6; a++) {
-        const int r = 6 * i + a;
-        T v = (r == c) ? T(1) : T(0);
-        for (int q = 6 * (i + 1); q < PB6; q++) v -= Mp[(size_t)r * ld + q] * X[(size_t)q * PB6 + c];
-        z[a] = v;
-      }
-      for (int a = 0; a < 6; a++) {
-        T v = 0;
-        for (int b = 0; b < 6; b++) v += Mp[(size_t)(6 * i + a) * ld + 6 * i + b] * z[b];
-        X[(size_t)(6 * i + a) * PB6 + c] = v;
+__global__ void __launch_bounds__(256) k_chunk_inverse(const int *__restrict__ chunks,
+                                                       const int *__restrict__ c0,
+                                                       const long long *__restrict__ off,
+                                                       const T *__restrict__ Mall,
+                                                       T *__restrict__ inv) {
+  const int ch = chunks[blockIdx.x];
+  const int ns = c0[ch + 1] - c0[ch], w = 6 * ns;
+  const T *M = Mall + off[ch] / 2;
+  T *X = inv + off[ch] + (UPPER ? (long long)w * w : 0);
+  for (int c = threadIdx.x; c < w; c += blockDim.x) {
+    if (!UPPER) {
+      for (int i = 0; i < ns; i++)
+        for (int a = 0; a < 6; a++) {
+          const int r = 6 * i + a;
+          T v = (r == c) ? T(1) : T(0);
+          const T *Mr = M + (size_t)r * w;
+          for (int q = 0; q < 6 * i; q++) v -= Mr[q] * X[(size_t)q * w + c];
+          X[(size_t)r * w + c] = v;
+        }
+    } else {
+      for (int i = ns - 1; i >= 0; i--) {
+        T z[6];
+        for (int a = 0; a < 6; a++) {
+          const int r = 6 * i + a;
+          T v = (r == c) ? T(1) : T(0);
+          const T *Mr = M + (size_t)r * w;
+          for (int q = 6 * (i + 1); q < w; q++) v -= Mr[q] * X[(size_t)q * w + c];
+          z[a] = v;
+        }
+        for (int a = 0; a < 6; a++) {
+          const T *Dr = M + (size_t)(6 * i + a) * w + 6 * i;
+          T v = 0;
+          for (int b = 0; b < 6; b++) v += Dr[b] * z[b];
+          X[(size_t)(6 * i + a) * w + c] = v;
+        }
       }
     }
   }
 }
 
-template <typename T>
-struct DenseBufs;
-template <>
-struct DenseBufs<double> {
-  static double *M(const Factor &f) { return f.dense64.p; }
-  static double *L(const Factor &f) { return f.pinvL64.p; }
-  static double *U(const Factor &f) { return f.pinvU64.p; }
-  static double *W(const Factor &f) { return f.dwork64.p; }
-};
-template <>
-struct DenseBufs<float> {
-  static float *M(const Factor &f) { return f.dense32.p; }
-  static float *L(const Factor &f) { return f.pinvL32.p; }
-  static float *U(const Factor &f) { return f.pinvU32.p; }
-  static float *W(const Factor &f) { return f.dwork32.p; }
-};
+// ------------------------------------------------------------ launchers
+// Shared memory of k_chunk_apply for the largest chunk: 6 CHUNK_MAX x R
+// values, above the default 48 KB for wide blocks of FP64 vectors.
+template <typename T, typename TV, int R>
+static int chunk_apply_config() {
+  const int smem = 6 * CHUNK_MAX * R * (int)sizeof(TV);
+  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  return 0;
+}
 
-int dense_alloc(Factor &f) {
-  if (f.dense_n <= 0) return 0;
-  const size_t nd6 = (size_t)6 * f.dense_n, np = (size_t)f.dense_n / DENSE_PANEL;
+template <typename T, typename TV>
+static int chunk_apply_config_all() {
   int rc;
+  if ((rc = chunk_apply_config<T, TV, 1>()) || (rc = chunk_apply_config<T, TV, 2>()) ||
+      (rc = chunk_apply_config<T, TV, 4>()) || (rc = chunk_apply_config<T, TV, 8>()) ||
+      (rc = chunk_apply_config<T, TV, 16>()))
+    return rc;
+  return 0;
+}
+
+int chunk_alloc(Factor &f) {
+  const ChunkPlan &cp = f.cp;
+  int rc;
+  // (function attributes are set here, outside any stream capture)
+  if ((rc = f.precision == 32 ? chunk_apply_config_all<float, float>()
+                              : chunk_apply_config_all<double, double>()))
+    return rc;
   if (f.precision == 32) {
-    if ((rc = f.dense32.alloc(nd6 * nd6)) || (rc = f.pinvL32.alloc(np * PB6 * PB6)) ||
-        (rc = f.pinvU32.alloc(np * PB6 * PB6)) || (rc = f.dwork32.alloc((size_t)PB6 * 16)))
+    if ((rc = f.cinv32.alloc((size_t)cp.inv_size)) || (rc = f.cscr32.alloc((size_t)cp.scr_size)))
       return rc;
   } else {
-    if ((rc = f.dense64.alloc(nd6 * nd6)) || (rc = f.pinvL64.alloc(np * PB6 * PB6)) ||
-        (rc = f.pinvU64.alloc(np * PB6 * PB6)) || (rc = f.dwork64.alloc((size_t)PB6 * 16)))
+    if ((rc = f.cinv64.alloc((size_t)cp.inv_size)) || (rc = f.cscr64.alloc((size_t)cp.scr_size)))
       return rc;
   }
   return 0;
 }
 
 template <typename T>
-static int dense_build_t(Factor &f, const T *F, cudaStream_t s, long long *launches) {
-  const int nd = f.dense_n, ld = 6 * nd, np = nd / DENSE_PANEL;
-  T *M = DenseBufs<T>::M(f);
-  A2DS_CUDA_TRY(cudaMemsetAsync(M, 0, (size_t)ld * ld * sizeof(T), s));
-  k_dense_scatter<T><<<(nd * 32 + 255) / 256, 256, 0, s>>>(f.dense_t0, nd, f.d_frowp.p,
-                                                           f.d_fcols.p, F, M);
-  k_dense_panel_inverse<T, false><<<(np * PB6 + 127) / 128, 128, 0, s>>>(M, ld, np,
-                                                                          DenseBufs<T>::L(f));
-  k_dense_panel_inverse<T, true><<<(np * PB6 + 127) / 128, 128, 0, s>>>(M, ld, np,
-                                                                         DenseBufs<T>::U(f));
+static int chunk_build_t(Factor &f, const T *F, T *inv, T *scr, cudaStream_t s,
+                         long long *launches) {
+  const int nch = (int)f.cp.lo.chunks.size();
+  if (nch == 0) return 0;
+  A2DS_CUDA_TRY(cudaMemsetAsync(scr, 0, (size_t)f.cp.scr_size * sizeof(T), s));
+  k_chunk_gather<T><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p, f.d_fcols.p,
+                                        f.d_row_lend.p, f.d_row_ustart.p, F, scr);
+  k_chunk_inverse<T, false><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p, scr,
+                                                 inv);
+  k_chunk_inverse<T, true><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p, scr,
+                                                inv);
   if (launches) *launches += 3;
   A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
-int dense_build(Factor &f, const void *F, cudaStream_t s, long long *launches) {
-  if (f.dense_n <= 0) return 0;
-  if (f.precision == 32) return dense_build_t<float>(f, (const float *)F, s, launches);
-  return dense_build_t<double>(f, (const double *)F, s, launches);
+int chunk_build(Factor &f, const void *F, cudaStream_t s, long long *launches) {
+  if (f.precision == 32)
+    return chunk_build_t<float>(f, (const float *)F, f.cinv32.p, f.cscr32.p, s, launches);
+  return chunk_build_t<double>(f, (const double *)F, f.cinv64.p, f.cscr64.p, s, launches);
 }
 
-static int dense_update_grid(int nrows) {
-  const int per_cta = 8 * DENSE_ROWS_PER_WARP;
-  return std::max(1, (nrows + per_cta - 1) / per_cta);
-}
+template <typename T>
+static const T *chunk_inverses(const Factor &f);
+template <>
+const double *chunk_inverses<double>(const Factor &f) { return f.cinv64.p; }
+template <>
+const float *chunk_inverses<float>(const Factor &f) { return f.cinv32.p; }
 
-template <typename T, typename TV, int R>
-static void dense_solve(const Factor &f, TV *y, cudaStream_t s, long long &nl) {
-  const int nd = f.dense_n, ld = 6 * nd, np = nd / DENSE_PANEL;
-  const T *M = DenseBufs<T>::M(f);
-  TV *w = DenseBufs<TV>::W(f);
-  TV *yD = y + (size_t)f.dense_t0 * 6 * R;
-  for (int p = 0; p < np; p++) {  // L: forward
-    k_dense_panel_apply<T, TV, R><<<PB6 / 8, 256, 0, s>>>(
-        DenseBufs<T>::L(f) + (size_t)p * PB6 * PB6, yD + (size_t)p * PB6 * R, w);
-    const int r0 = (p + 1) * PB6, nr = ld - r0;
-    k_dense_panel_update<T, TV, R><<<dense_update_grid(nr), 256, 0, s>>>(M, ld, r0, nr,
-                                                                         p * PB6, w, yD);
-    nl += 2;
+template <typename T, typename TV, int R, bool UPPER>
+static void solve_level(const Factor &f, const T *F, const TV *src, TV *y, int l, cudaStream_t s,
+                        long long &nl) {
+  const ChunkLevels &L = UPPER ? f.cp.up : f.cp.lo;
+  const int *rows = (UPPER ? f.d_up_rows.p : f.d_lo_rows.p) + L.row_ptr[l];
+  const int nrows = L.row_ptr[l + 1] - L.row_ptr[l];
+  const int *bound = UPPER ? f.d_row_ustart.p : f.d_row_lend.p;
+  if (L.cta[l])
+    k_pull_cta<T, TV, R, UPPER><<<nrows, 256, 0, s>>>(rows, nrows, f.d_frowp.p, bound,
+                                                      f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p,
+                                                      F, src, y);
+  else
+    k_pull_warp<T, TV, R, UPPER><<<(nrows + 7) / 8, 256, 0, s>>>(
+        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, src, y);
+  nl++;
+  const int nch = L.ch_ptr[l + 1] - L.ch_ptr[l];
+  if (nch > 0) {
+    // staging for this level's largest chunk; small chunks take 64 threads
+    const int mr = L.max_rows[l];
+    const size_t smem = (size_t)6 * mr * R * sizeof(TV);
+    k_chunk_apply<T, TV, R, UPPER><<<nch, mr <= 16 ? 64 : 256, smem, s>>>(
+        (UPPER ? f.d_up_chunks.p : f.d_lo_chunks.p) + L.ch_ptr[l], f.d_ck_c0.p, f.d_ck_off.p,
+        chunk_inverses<T>(f), y);
+    nl++;
   }
-  for (int p = np - 1; p >= 0; p--) {  // D + U: backward
-    k_dense_panel_apply<T, TV, R><<<PB6 / 8, 256, 0, s>>>(
-        DenseBufs<T>::U(f) + (size_t)p * PB6 * PB6, yD + (size_t)p * PB6 * R, w);
-    const int nr = p * PB6;
-    k_dense_panel_update<T, TV, R><<<dense_update_grid(nr), 256, 0, s>>>(M, ld, 0, nr,
-                                                                         p * PB6, w, yD);
-    nl += 2;
-  }
 }
 
-// ------------------------------------------------------------ launchers
 template <typename T, typename TV, int R>
 static int solve_levels_r(const Factor &f, const T *F, const TV *x, TV *y, cudaStream_t s,
                           long long *launches) {
-  const LevelSchedule &Lo = f.lower, &Up = f.upper;
   long long nl = 0;
-  for (int lv = 0; lv < Lo.nlevels; lv++) {
-    const int cnt = Lo.ptr[lv + 1] - Lo.ptr[lv];
-    if (f.lower_cta[lv])
-      k_tri_block<T, TV, R, false><<<cnt, 256, 0, s>>>(Lo.d_rows.p + Lo.ptr[lv], cnt,
-                                                       f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
-                                                       x, y);
-    else
-      k_lower_warp<T, TV, R><<<(cnt + 7) / 8, 256, 0, s>>>(Lo.d_rows.p + Lo.ptr[lv], cnt,
-                                                           f.d_frowp.p, f.d_fcols.p,
-                                                           f.d_fdiag.p, F, x, y);
-    nl++;
-  }
-  const int ts = f.tail_s, d = f.n - f.tail_s;
-  if (d > 0) {
-    k_tail_pull<T, TV, R><<<(d + 7) / 8, 256, 0, s>>>(ts, d, f.d_frowp.p, f.d_fcols.p,
-                                                      f.d_lsplit.p, F, x, y);
-    nl++;
-    for (size_t lv = 0; lv + 1 < f.tl_ptr.size(); lv++) {
-      const int e0 = f.tl_ptr[lv], ne = f.tl_ptr[lv + 1] - e0;
-      if (ne <= 0) continue;
-      k_tail_push<T, TV, R, PUSH_L><<<(ne * R + 255) / 256, 256, 0, s>>>(
-          f.d_tl_row.p + e0, f.d_tl_pos.p + e0, f.d_tl_col.p + e0, ne, f.d_fdiag.p, F, y);
-      nl++;
-    }
-    if (f.dense_n > 0) {
-      dense_solve<T, TV, R>(f, y, s, nl);
-      const int ne = (int)f.td_row.size();
-      if (ne > 0) {
-        k_tail_push<T, TV, R, PUSH_U_FINAL><<<(ne * R + 255) / 256, 256, 0, s>>>(
-            f.d_td_row.p, f.d_td_pos.p, f.d_td_col.p, ne, f.d_fdiag.p, F, y);
-        nl++;
-      }
-    }
-    for (size_t lv = 0; lv + 1 < f.tu_ptr.size(); lv++) {
-      const int e0 = f.tu_ptr[lv], ne = f.tu_ptr[lv + 1] - e0;
-      if (ne <= 0) continue;
-      k_tail_push<T, TV, R, PUSH_U><<<(ne * R + 255) / 256, 256, 0, s>>>(
-          f.d_tu_row.p + e0, f.d_tu_pos.p + e0, f.d_tu_col.p + e0, ne, f.d_fdiag.p, F, y);
-      nl++;
-    }
-    const int dm = f.dense_t0 - ts;  // middle rows: finalized here (dense rows are final)
-    if (dm > 0) {
-      k_tail_finalize<T, TV, R><<<(dm * R + 127) / 128, 128, 0, s>>>(ts, dm, f.d_fdiag.p, F, y);
-      nl++;
-    }
-  }
-  for (int lv = 0; lv < Up.nlevels; lv++) {
-    const int cnt = Up.ptr[lv + 1] - Up.ptr[lv];
-    if (f.upper_cta[lv])
-      k_tri_block<T, TV, R, true><<<cnt, 256, 0, s>>>(Up.d_rows.p + Up.ptr[lv], cnt,
-                                                      f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F,
-                                                      y, y);
-    else
-      k_upper_warp<T, TV, R><<<(cnt + 7) / 8, 256, 0, s>>>(Up.d_rows.p + Up.ptr[lv], cnt,
-                                                           f.d_frowp.p, f.d_fcols.p,
-                                                           f.d_fdiag.p, F, y);
-    nl++;
-  }
+  for (int l = 0; l < f.cp.lo.nlevels; l++) solve_level<T, TV, R, false>(f, F, x, y, l, s, nl);
+  for (int l = 0; l < f.cp.up.nlevels; l++) solve_level<T, TV, R, true>(f, F, y, y, l, s, nl);
   if (launches) *launches += nl;
   A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
