@@ -50,7 +50,7 @@ def build(force: bool = False) -> str:
     newest = max(os.path.getmtime(f) for f in SOURCES + headers)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         tmp = LIB + f".tmp{os.getpid()}"
-        cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=gnu99", "-fopenmp", "-o", tmp] + \
+        cmd = ["gcc", "-O3", "-fPIC", "-shared", "-std=gnu99", "-fopenmp", "-o", tmp] + \
             SOURCES + ["-lm"]
         subprocess.run(cmd, check=True)
         os.replace(tmp, LIB)
@@ -335,3 +335,238 @@ class CpuBuckling:
         self.path = self._from_rows(path)
         self.eigvals = lam
         return lam
+
+
+# ------------------------------------------- multi-threaded CPU solve
+def _declare_par(lib):
+    lib.orc_nd_order.argtypes = [ctypes.c_int, PI, PI, P, ctypes.c_int, PI]
+    lib.orc_symbolic_lu.argtypes = [ctypes.c_int, PI, PI, PI, PI]
+    lib.orc_symbolic_lu.restype = ctypes.c_longlong
+    lib.orc_factor_levels.argtypes = [ctypes.c_int, PI, PI, PI, ctypes.c_int, PI, PI]
+    lib.orc_factor_levels.restype = ctypes.c_int
+    lib.orc_factor_par.argtypes = [ctypes.c_int, PI, PI, PI, ctypes.c_int, PI, PI, P]
+    lib.orc_factor_par.restype = ctypes.c_int
+    lib.orc_apply_factor_par.argtypes = [ctypes.c_int, PI, PI, PI, P, ctypes.c_int, PI, PI,
+                                         ctypes.c_int, PI, PI, ctypes.c_int, P, P]
+    lib.orc_spmm.argtypes = [ctypes.c_int, PI, PI, P, ctypes.c_int, P, P, P]
+    lib.omp_get_max_threads.restype = ctypes.c_int
+
+
+def node_graph(conn, nn):
+    """Node-to-node CSR (with the diagonal, sorted) of an element mesh."""
+    conn = np.asarray(conn, np.int64)
+    npe = conn.shape[1]
+    a = np.repeat(conn, npe, axis=1).ravel()
+    b = np.tile(conn, (1, npe)).ravel()
+    key = np.unique(a * nn + b)
+    r, c = key // nn, key % nn
+    rowp = np.zeros(nn + 1, np.int32)
+    np.add.at(rowp, r + 1, 1)
+    return np.cumsum(rowp).astype(np.int32), c.astype(np.int32)
+
+
+class CpuPlan:
+    """Host set-up of the multi-threaded CPU solve: nested-dissection
+    ordering (cpu_parallel.c), the BCSR pattern in that ordering, the
+    complete-LU pattern from the elimination tree and the dependency levels
+    of its triangular solves.  Needs nothing but the oracle library."""
+
+    def __init__(self, mesh):
+        lib = load()
+        _declare_solver(lib)
+        _declare_par(lib)
+        self.lib = lib
+        nn = mesh.num_nodes
+        grp, grc = node_graph(mesh.conn, nn)
+        perm = np.empty(nn, np.int32)
+        X = np.ascontiguousarray(mesh.X, np.float64)
+        lib.orc_nd_order(nn, _pi(grp), _pi(grc), _p(X), 64, _pi(perm))
+        iperm = np.empty(nn, np.int32)
+        iperm[perm] = np.arange(nn, dtype=np.int32)
+        # pattern in the row ordering
+        r = iperm[np.repeat(np.arange(nn), np.diff(grp))].astype(np.int64)
+        c = iperm[grc].astype(np.int64)
+        key = np.unique(r * nn + c)
+        rowp = np.zeros(nn + 1, np.int32)
+        np.add.at(rowp, (key // nn) + 1, 1)
+        self.perm, self.iperm = perm, iperm
+        self.rowp = np.cumsum(rowp).astype(np.int32)
+        self.cols = (key % nn).astype(np.int32)
+        nf = lib.orc_symbolic_lu(nn, _pi(self.rowp), _pi(self.cols), None, None)
+        self.frowp = np.zeros(nn + 1, np.int32)
+        self.fcols = np.zeros(nf, np.int32)
+        lib.orc_symbolic_lu(nn, _pi(self.rowp), _pi(self.cols), _pi(self.frowp), _pi(self.fcols))
+        self.fdiag = np.empty(nn, np.int32)
+        for i in range(0, nn, 65536):  # position of the diagonal in each row
+            j = np.arange(i, min(nn, i + 65536))
+            lens = self.frowp[j + 1] - self.frowp[j]
+            rows = np.repeat(j, lens)
+            pos = np.arange(self.frowp[i], self.frowp[j[-1] + 1])
+            hit = self.fcols[pos] == rows
+            self.fdiag[rows[hit]] = pos[hit]
+        self.levels = {}
+        for upper in (0, 1):
+            nl = lib.orc_factor_levels(nn, _pi(self.frowp), _pi(self.fcols), _pi(self.fdiag),
+                                       upper, None, None)
+            ptr = np.zeros(nl + 1, np.int32)
+            rows = np.zeros(nn, np.int32)
+            lib.orc_factor_levels(nn, _pi(self.frowp), _pi(self.fcols), _pi(self.fdiag), upper,
+                                  _pi(ptr), _pi(rows))
+            self.levels[upper] = (nl, ptr, rows)
+        self.n = nn
+        self.bc_rows = iperm[mesh.bc_nodes].astype(np.int32)
+        self.bc_masks = np.ascontiguousarray(mesh.bc_mask, np.int32)
+        mask = np.zeros((nn, 6), bool)
+        for rr, mk in zip(self.bc_rows, self.bc_masks):
+            for k in range(6):
+                if mk >> k & 1:
+                    mask[rr, k] = True
+        self.bc_dofs = mask.ravel()
+
+    @property
+    def threads(self):
+        return int(self.lib.omp_get_max_threads())
+
+    def factor(self, vals):
+        lib, n = self.lib, self.n
+        F = np.zeros((self.fcols.size, 6, 6))
+        lib.orc_factor_fill(n, _pi(self.rowp), _pi(self.cols), _p(np.ascontiguousarray(vals)),
+                            _pi(self.frowp), _pi(self.fcols), _p(F))
+        nl, ptr, rows = self.levels[0]
+        rc = lib.orc_factor_par(n, _pi(self.frowp), _pi(self.fcols), _pi(self.fdiag), nl,
+                                _pi(ptr), _pi(rows), _p(F))
+        if rc:
+            raise RuntimeError(f"singular diagonal block in row {rc - 1}")
+        return F
+
+    def apply(self, F, X):
+        """(LU)^{-1} X for X of shape (6 n, p), row-major (row, dof, rhs)."""
+        X = np.ascontiguousarray(X)
+        p = X.shape[1] if X.ndim == 2 else 1
+        Y = np.empty_like(X)
+        (nlo, plo, rlo), (nup, pup, rup) = self.levels[0], self.levels[1]
+        self.lib.orc_apply_factor_par(self.n, _pi(self.frowp), _pi(self.fcols), _pi(self.fdiag),
+                                      _p(F), nlo, _pi(plo), _pi(rlo), nup, _pi(pup), _pi(rup), p,
+                                      _p(X), _p(Y))
+        return Y
+
+    def spmm(self, A, X, B=None):
+        X = np.ascontiguousarray(X)
+        p = X.shape[1] if X.ndim == 2 else 1
+        Y = np.empty_like(X)
+        self.lib.orc_spmm(self.n, _pi(self.rowp), _pi(self.cols), _p(A), p, _p(X),
+                          None if B is None else _p(np.ascontiguousarray(B)), _p(Y))
+        return Y
+
+    def assemble(self, mesh, kind, path_nodes=None):
+        return assemble(mesh, kind, self.perm, self.rowp, self.cols, path_nodes, False,
+                        self.bc_rows, self.bc_masks)
+
+    def refined_solve(self, A, F, X, rtol, max_steps):
+        Y = self.apply(F, X)
+        xn = np.linalg.norm(X, axis=0)
+        for _ in range(max_steps):
+            R = self.spmm(A, Y, X)
+            if np.all(np.linalg.norm(R, axis=0) <= rtol * xn):
+                break
+            Y += self.apply(F, R)
+        return Y
+
+
+def cpu_buckling_solve(mesh, plan: CpuPlan, sigma, neig=10, block=4, max_lanczos=200,
+                       eig_tol=1e-8, seed=0):
+    """The buckling solve on the host cores with the reference's numerics
+    (element assembly, IKJ block LU, block triangular solves, SpMV) in the
+    scheme of the GPU's all-FP64 solve: K at the zero state, its factor and
+    the load path with FP64 refinement, G along the path, the factor of
+    K + sigma G, and block shift-invert Lanczos (block `block`, two
+    classical Gram-Schmidt passes in the K inner product, Cholesky-QR twice,
+    Ritz convergence ||B_j y_j|| <= eig_tol |mu|).  Returns (eigenvalues,
+    phase times, Lanczos vectors)."""
+    import time
+    t = {}
+    n6 = 6 * plan.n
+    lib = plan.lib
+    t0 = time.perf_counter()
+    K = plan.assemble(mesh, STIFFNESS)
+    t["assemble_k"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    FK = plan.factor(K)
+    t["factor_k"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = np.zeros((plan.n, 6))
+    b[:] = mesh.rhs[plan.perm]
+    for rr, mk in zip(plan.bc_rows, plan.bc_masks):
+        for k in range(6):
+            if mk >> k & 1:
+                b[rr, k] = 0.0
+    u = plan.refined_solve(K, FK, b.reshape(n6, 1), 1e-13, 4)
+    path = np.empty((plan.n, 6))
+    path[plan.perm] = u.reshape(plan.n, 6)
+    t["path"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    G = plan.assemble(mesh, GEOMETRIC, path)
+    t["assemble_g"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    A = np.ascontiguousarray(K + sigma * G)
+    lib.orc_apply_bcs(_pi(plan.rowp), _pi(plan.cols), _p(A), plan.bc_rows.size,
+                      _pi(plan.bc_rows), _pi(plan.bc_masks))
+    FA = plan.factor(A)
+    t["factor_a"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    p = block
+    rng = np.random.default_rng(seed)
+    bcd = plan.bc_dofs
+
+    def korth(W, KW):
+        for _ in range(2):
+            M = W.T @ KW
+            M = 0.5 * (M + M.T)
+            R = np.linalg.cholesky(M).T
+            Ri = np.linalg.inv(R)
+            W[:] = W @ Ri
+            KW[:] = KW @ Ri
+            yield R
+
+    def cholqr2(W, KW):
+        Rs = list(korth(W, KW))
+        return Rs[1] @ Rs[0]
+
+    Q0 = rng.uniform(-1, 1, (n6, p))
+    Q0[bcd] = 0.0
+    Q, KQ = [Q0], [plan.spmm(K, Q0)]
+    cholqr2(Q[0], KQ[0])
+    nbmax = max_lanczos // p
+    T = np.zeros(((nbmax + 1) * p, (nbmax + 1) * p))
+    lam_of = lambda mu: -mu * sigma / (1.0 - mu)
+    rtol = max(1e-12, min(1e-9, 0.1 * eig_tol))
+    lam = None
+    for j in range(nbmax):
+        W = plan.refined_solve(A, FA, KQ[j], rtol, 2)
+        W[bcd] = 0.0
+        Qs = np.stack(Q)          # (j+1, n6, p)
+        KQs = np.stack(KQ)
+        H1 = np.einsum("bnc,nd->bcd", KQs, W)
+        W -= np.einsum("bnc,bcd->nd", Qs, H1)
+        H2 = np.einsum("bnc,nd->bcd", KQs, W)
+        W -= np.einsum("bnc,bcd->nd", Qs, H2)
+        H = H1 + H2
+        KW = plan.spmm(K, W)
+        B = cholqr2(W, KW)
+        D = 0.5 * (H[j] + H[j].T)
+        T[j * p:(j + 1) * p, j * p:(j + 1) * p] = D
+        T[(j + 1) * p:(j + 2) * p, j * p:(j + 1) * p] = B
+        T[j * p:(j + 1) * p, (j + 1) * p:(j + 2) * p] = B.T
+        Q.append(W)
+        KQ.append(KW)
+        md = (j + 1) * p
+        if md < neig:
+            continue
+        mu, V = np.linalg.eigh(T[:md, :md])
+        order = np.argsort(np.abs(lam_of(mu)))[:neig]
+        est = np.linalg.norm(B @ V[j * p:(j + 1) * p, order], axis=0)
+        lam = lam_of(mu[order])
+        if np.all(est <= eig_tol * np.abs(mu[order])):
+            break
+    t["lanczos"] = time.perf_counter() - t0
+    return lam, t, (j + 1) * p

@@ -152,6 +152,9 @@ static int inv6(const double *A, double *Ainv) {
   return 0;
 }
 
+/* the 6x6 inverse above, for the multi-threaded factorization (cpu_parallel.c) */
+int orc_inv6(const double *A, double *Ainv) { return inv6(A, Ainv); }
+
 /* Copy A (pattern rowp/cols) into the factor pattern F (frowp/fcols). */
 void orc_factor_fill(int n, const int *rowp, const int *cols, const double *A, const int *frowp,
                      const int *fcols, double *F) {
