@@ -48,6 +48,7 @@ EXPORTS = [
     "a2ds_bcsr_create", "a2ds_bcsr_destroy", "a2ds_bcsr_get", "a2ds_bcsr_set_values",
     "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
     "a2ds_add_mat_xpt_sens_inner_product", "a2ds_add_adjoint_res_xpt_sens_product",
+    "a2ds_add_mat_dv_sens_inner_product",
     "a2ds_eval_mat_sv_sens_inner_product", "a2ds_eig_sens_xpts",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_time_mult",
@@ -147,6 +148,8 @@ def load(build: bool = False):
     lib.a2ds_eig_sens_xpts.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
     lib.a2ds_add_mat_xpt_sens_inner_product.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D,
                                                         P_D, P_D, ctypes.c_double, P_D]
+    lib.a2ds_add_mat_dv_sens_inner_product.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D,
+                                                       P_D, P_D, P_D]
     lib.a2ds_add_adjoint_res_xpt_sens_product.argtypes = [VP, ctypes.c_double, P_D, P_D,
                                                           ctypes.c_double, P_D]
     lib.a2ds_eval_mat_sv_sens_inner_product.argtypes = [VP, ctypes.c_int, P_D, P_D, P_D,
@@ -297,6 +300,16 @@ class Assembler:
         _check(self.lib.a2ds_add_mat_xpt_sens_inner_product(
             self.h, int(mat_type), float(scale), _d(ps), _d(ph), _d(v), float(dh), _d(dfdX)))
         return dfdX
+
+    def add_mat_dv_sens_inner_product(self, scale, mat_type, psi, phi, dfdx, vars_=None):
+        """dfdx[g] += scale * d(psi^T M phi)/dt_g per thickness group, M = K at
+        vars_ or G along vars_ (TACSElement::addMatDVSensInnerProduct, exact
+        here)."""
+        assert dfdx.dtype == np.float64 and dfdx.flags.c_contiguous
+        ps, ph, v = self._vec6(psi), self._vec6(phi), self._vec6(vars_)
+        _check(self.lib.a2ds_add_mat_dv_sens_inner_product(
+            self.h, int(mat_type), float(scale), _d(ps), _d(ph), _d(v), _d(dfdx)))
+        return dfdx
 
     def _vec6(self, a):
         a = _f64(a)

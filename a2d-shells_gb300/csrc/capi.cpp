@@ -362,6 +362,48 @@ int a2ds_add_mat_xpt_sens_inner_product(a2ds_mesh mesh, int mat_type, double sca
   A2DS_GUARD_END
 }
 
+int a2ds_add_mat_dv_sens_inner_product(a2ds_mesh mesh, int mat_type, double scale,
+                                       const double *psi, const double *phi,
+                                       const double *vars, double *dfdx) {
+  A2DS_GUARD_BEGIN
+  int rc = check_mesh(mesh, true);
+  if (rc) return rc;
+  if (!psi || !phi || !dfdx) return fail(A2DS_ERR_ARG, "null argument");
+  int mode;
+  if (mat_type == A2DS_STIFFNESS_MATRIX)
+    mode = MODE_K;
+  else if (mat_type == A2DS_GEOMETRIC_STIFFNESS_MATRIX)
+    mode = MODE_G;
+  else
+    return fail(A2DS_ERR_ARG, "mat_type must be STIFFNESS (0) or GEOMETRIC_STIFFNESS (2)");
+  Mesh &m = mesh->m;
+  const int ng = (int)m.tvals.size();
+  DBuf<double> dpsi, dphi, dd;
+  if ((rc = m.to_rows(psi, dpsi)) || (rc = m.to_rows(phi, dphi)) || (rc = dd.alloc(ng)))
+    return rc;
+  const double *dst = nullptr;
+  if (vars) {
+    if ((rc = m.to_rows(vars, m.d_state))) return rc;
+    dst = m.d_state.p;
+  }
+  A2DS_CUDA_TRY(cudaMemsetAsync(dd.p, 0, ng * sizeof(double), m.stream));
+  ElemLaunch L = m.launch_params(mode, dst, nullptr, nullptr);
+  L.dconst = 1;  // element matrices with dC/dt: exact, they are linear in C
+  L.cout = dd.p;
+  L.cx = dpsi.p;
+  L.cy = dphi.p;
+  L.ccoef = scale;
+  if ((rc = launch_element_kernel(L, m.stream))) return rc;
+  m.launches++;
+  std::vector<double> h(ng);
+  A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), dd.p, ng * sizeof(double), cudaMemcpyDeviceToHost,
+                                m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  for (int g = 0; g < ng; g++) dfdx[g] += h[g];
+  return 0;
+  A2DS_GUARD_END
+}
+
 int a2ds_add_adjoint_res_xpt_sens_product(a2ds_mesh mesh, double scale, const double *psi,
                                           const double *vars, double dh, double *dfdX) {
   A2DS_GUARD_BEGIN

@@ -99,8 +99,8 @@ struct Factor {
   DBuf<int> d_ck_c0, d_row_lend, d_row_ustart, d_row_single;
   DBuf<long long> d_ck_off;
   DBuf<int> d_lo_rows, d_lo_chunks, d_up_rows, d_up_chunks;
-  DBuf<double> cinv64, cscr64;
-  DBuf<float> cinv32, cscr32;
+  DBuf<double> cinv64, cscr64;  // FP64 inverses (all precisions) and gathered blocks
+  DBuf<float> cinv32;           // FP32 copy of the inverses for FP32 factors
   // algorithmic FP operations of one numeric factorization: 432 per L block
   // (L_ij = A_ij D_j^{-1}), 432 per block update, 432 per diagonal inverse
   double flop_count = 0.0;

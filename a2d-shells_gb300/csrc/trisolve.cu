@@ -209,29 +209,29 @@ __global__ void __launch_bounds__(256) k_chunk_apply(const int *__restrict__ chu
   }
 }
 
-// Dense copy of every multi-row chunk's diagonal block out of the factor
+// Dense FP64 copy of every multi-row chunk's diagonal block out of the factor
 // (scratch zeroed beforehand; chunk c's (6 ns)^2 block at off[c] / 2, since
 // the inverse storage holds two blocks per chunk), one CTA per chunk, one
 // warp per row: the row's blocks inside its chunk are [row_lend, row_ustart).
-template <typename T>
+template <typename TF>
 __global__ void __launch_bounds__(256) k_chunk_gather(const int *__restrict__ chunks,
                                                       const int *__restrict__ c0,
                                                       const long long *__restrict__ off,
                                                       const int *__restrict__ fcols,
                                                       const int *__restrict__ row_lend,
                                                       const int *__restrict__ row_ustart,
-                                                      const T *__restrict__ F,
-                                                      T *__restrict__ Mall) {
+                                                      const TF *__restrict__ F,
+                                                      double *__restrict__ Mall) {
   const int ch = chunks[blockIdx.x];
   const int a = c0[ch], ns = c0[ch + 1] - a, w = 6 * ns;
-  T *M = Mall + off[ch] / 2;
+  double *M = Mall + off[ch] / 2;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int r = warp; r < ns; r += nw) {
     const int i = a + r, k0 = row_lend[i], k1 = row_ustart[i];
     for (int idx = lane; idx < (k1 - k0) * 36; idx += 32) {
       const int k = k0 + idx / 36, e = idx % 36;
       const int ea = e / 6, eb = e % 6;
-      M[(size_t)(6 * r + ea) * w + 6 * (fcols[k] - a) + eb] = F[(size_t)k * 36 + e];
+      M[(size_t)(6 * r + ea) * w + 6 * (fcols[k] - a) + eb] = (double)F[(size_t)k * 36 + e];
     }
   }
 }
@@ -304,6 +304,8 @@ static int chunk_apply_config_all() {
   return 0;
 }
 
+// The inverses are always computed in FP64 (gathered blocks widened); an
+// FP32 factor keeps an FP32 copy for its solves.
 int chunk_alloc(Factor &f) {
   const ChunkPlan &cp = f.cp;
   int rc;
@@ -311,37 +313,43 @@ int chunk_alloc(Factor &f) {
   if ((rc = f.precision == 32 ? chunk_apply_config_all<float, float>()
                               : chunk_apply_config_all<double, double>()))
     return rc;
-  if (f.precision == 32) {
-    if ((rc = f.cinv32.alloc((size_t)cp.inv_size)) || (rc = f.cscr32.alloc((size_t)cp.scr_size)))
-      return rc;
-  } else {
-    if ((rc = f.cinv64.alloc((size_t)cp.inv_size)) || (rc = f.cscr64.alloc((size_t)cp.scr_size)))
-      return rc;
-  }
+  if ((rc = f.cinv64.alloc((size_t)cp.inv_size)) || (rc = f.cscr64.alloc((size_t)cp.scr_size)))
+    return rc;
+  if (f.precision == 32 && (rc = f.cinv32.alloc((size_t)cp.inv_size))) return rc;
   return 0;
 }
 
-template <typename T>
-static int chunk_build_t(Factor &f, const T *F, T *inv, T *scr, cudaStream_t s,
-                         long long *launches) {
+__global__ void k_narrow(float *__restrict__ y, const double *__restrict__ x, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+template <typename TF>
+static int chunk_build_t(Factor &f, const TF *F, cudaStream_t s, long long *launches) {
   const int nch = (int)f.cp.lo.chunks.size();
   if (nch == 0) return 0;
-  A2DS_CUDA_TRY(cudaMemsetAsync(scr, 0, (size_t)f.cp.scr_size * sizeof(T), s));
-  k_chunk_gather<T><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p, f.d_fcols.p,
-                                        f.d_row_lend.p, f.d_row_ustart.p, F, scr);
-  k_chunk_inverse<T, false><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p, scr,
-                                                 inv);
-  k_chunk_inverse<T, true><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p, scr,
-                                                inv);
+  double *scr = f.cscr64.p, *inv = f.cinv64.p;
+  A2DS_CUDA_TRY(cudaMemsetAsync(scr, 0, (size_t)f.cp.scr_size * sizeof(double), s));
+  k_chunk_gather<TF><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                         f.d_fcols.p, f.d_row_lend.p, f.d_row_ustart.p, F, scr);
+  k_chunk_inverse<double, false><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                                      scr, inv);
+  k_chunk_inverse<double, true><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                                     scr, inv);
   if (launches) *launches += 3;
+  if (f.precision == 32) {
+    const size_t n = (size_t)f.cp.inv_size;
+    k_narrow<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(f.cinv32.p, inv, n);
+    if (launches) *launches += 1;
+  }
   A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
 int chunk_build(Factor &f, const void *F, cudaStream_t s, long long *launches) {
-  if (f.precision == 32)
-    return chunk_build_t<float>(f, (const float *)F, f.cinv32.p, f.cscr32.p, s, launches);
-  return chunk_build_t<double>(f, (const double *)F, f.cinv64.p, f.cscr64.p, s, launches);
+  if (f.precision == 32) return chunk_build_t<float>(f, (const float *)F, s, launches);
+  return chunk_build_t<double>(f, (const double *)F, s, launches);
 }
 
 template <typename T>

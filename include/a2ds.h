@@ -173,6 +173,20 @@ int a2ds_add_mat_xpt_sens_inner_product(a2ds_mesh mesh, int mat_type, double sca
                                         const double *psi, const double *phi,
                                         const double *vars, double dh, double *dfdX);
 
+/* The assembler-level thickness inner product of the reference's
+   (commented) TACSLinearBuckling::evalEigenDVSens (src/TACSBuckling.cpp:
+   397-403, assembler->addMatDVSensInnerProduct), element by element
+   TACSElement::addMatDVSensInnerProduct (src/elements/TACSElement.cpp:
+   355-432): dfdx[g] += scale * sum over the elements of thickness group g of
+   d(psi^T M(vars) phi)/dt for M = K (at vars) or G (along vars).  Exact:
+   the element matrices are linear in the constitutive matrix, so the
+   derivative is the element matrix with dC/dt (the reference takes central
+   differences with step 1e-7).  psi, phi, vars: num_nodes x 6 (vars NULL =
+   zero); dfdx: num_groups values (a2ds_mesh_set_thickness), added into. */
+int a2ds_add_mat_dv_sens_inner_product(a2ds_mesh mesh, int mat_type, double scale,
+                                       const double *psi, const double *phi,
+                                       const double *vars, double *dfdx);
+
 /* The adjoint-residual coordinate product of the same body
    (addAdjointResXptSensProducts, src/TACSBuckling.cpp:486), element by
    element TACSElement::addAdjResXptProduct (src/elements/TACSElement.cpp:

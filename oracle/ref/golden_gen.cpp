@@ -198,7 +198,7 @@ static void run_elements(const std::string &out) {
     const int nv = 6 * nn;
     SplitMix rng(20261203ull + 7919ull * (uint64_t)e);
     std::vector<TacsScalar> Xall, Vall, Kall, Gall, Rall, Jall, JRall, params;
-    std::vector<TacsScalar> PSall, PHall, KXall, GXall, KUall, GUall, RXall;
+    std::vector<TacsScalar> PSall, PHall, KXall, GXall, KUall, GUall, RXall, KDall, GDall;
     SplitMix rng_x(977ull + 31ull * (uint64_t)e);  // psi, phi of the coordinate products
     for (int s = 0; s < nsamples; s++) {
       double h = rng.uniform(0.02, 0.6);
@@ -272,6 +272,20 @@ static void run_elements(const std::string &out) {
         elem->addAdjResXptProduct(0, 0.0, 1.0, psi.data(), X.data(), vars.data(), zero.data(),
                                   zero.data(), RX.data());
       }
+      // Thickness inner products d(psi^T M phi)/dt of K and G
+      // (TACSElement::addMatDVSensInnerProduct, TACSElement.cpp:355-432: the
+      // element's one design variable, central differences with dh = 1e-7
+      // in the real build, complex step in the complex build); last, since
+      // the G evaluations of a nonlinear instantiation move its temperature
+      TacsScalar kd = 0.0, gd = 0.0;
+      if (temp == 0.0) {
+        elem->addMatDVSensInnerProduct(TACS_STIFFNESS_MATRIX, 0, 0.0, 1.0, psi.data(),
+                                       phi.data(), X.data(), vars.data(), 1, &kd);
+        elem->addMatDVSensInnerProduct(TACS_GEOMETRIC_STIFFNESS_MATRIX, 0, 0.0, 1.0, psi.data(),
+                                       phi.data(), X.data(), vars.data(), 1, &gd);
+      }
+      KDall.push_back(kd);
+      GDall.push_back(gd);
       KUall.insert(KUall.end(), KU.begin(), KU.end());
       GUall.insert(GUall.end(), GU.begin(), GU.end());
       RXall.insert(RXall.end(), RX.begin(), RX.end());
@@ -306,6 +320,8 @@ static void run_elements(const std::string &out) {
     save_d(out, pre + "KU", KUall.data(), {nsamples, nv});
     save_d(out, pre + "GU", GUall.data(), {nsamples, nv});
     save_d(out, pre + "RX", RXall.data(), {nsamples, nn, 3});
+    save_d(out, pre + "KD", KDall.data(), {nsamples});
+    save_d(out, pre + "GD", GDall.data(), {nsamples});
   }
   tr->decref();
 }

@@ -146,3 +146,73 @@ class DenseShell:
         dG = (mats[0][1] - mats[1][1]) / (2 * h)
         num = phi @ dK @ phi + lam * (phi @ dG @ phi) - lam * (psi @ dK @ u)
         return -num / float(phi @ G @ phi)
+
+
+def thickness_sens_groups(m, u, lam, phi, K, G, rel_step=1e-6):
+    """dlam/dt_g for every thickness group of a mesh with per-element
+    thickness m.thickness and groups m.dv_group (linear elements): the same
+    formula as DenseShell.thickness_sens with the element matrices of group
+    g's elements differentiated in their thickness (central differences of
+    the oracle's element routines, step rel_step * t_e), the adjoint psi
+    shared by all groups.  Dense FP64; returns one value per group id up to
+    max(dv_group)."""
+    ds = DenseShell(m)
+    fr = ds.free
+    X = m.X
+    ng = int(np.max(m.dv_group)) + 1
+    # G(phi) phi with per-element thickness
+    g = np.zeros(ds.N)
+    for e, c in enumerate(m.conn):
+        d = _dofs(c)
+        mat = Material.iso(m.E, m.nu, float(m.thickness[e]))
+        g[d] += element_matrix(ds.order, 0, GEOMETRIC, mat, X[c], phi[d]) @ phi[d]
+    psi = np.zeros(ds.N)
+    psi[fr] = np.linalg.solve(K[np.ix_(fr, fr)], g[fr])
+    num = np.zeros(ng)
+    z = np.zeros(6 * ds.order ** 2)
+    for e, c in enumerate(m.conn):
+        d = _dofs(c)
+        t0 = float(m.thickness[e])
+        h = rel_step * t0
+        dK = dG = 0.0
+        for sgn in (1.0, -1.0):
+            mat = Material.iso(m.E, m.nu, t0 + sgn * h)
+            dK = dK + sgn * element_matrix(ds.order, 0, STIFFNESS, mat, X[c], z) / (2 * h)
+            dG = dG + sgn * element_matrix(ds.order, 0, GEOMETRIC, mat, X[c], u[d]) / (2 * h)
+        num[m.dv_group[e]] += (phi[d] @ dK @ phi[d] + lam * (phi[d] @ dG @ phi[d])
+                               - lam * (psi[d] @ dK @ u[d]))
+    return -num / float(phi @ G @ phi)
+
+
+def mesh_matrices(m, u):
+    """Dense K (zero state) and G (along u) of a mesh with per-element
+    thickness, without Dirichlet rows."""
+    N = 6 * m.X.shape[0]
+    K, G = np.zeros((N, N)), np.zeros((N, N))
+    z = np.zeros(6 * m.order ** 2)
+    for e, c in enumerate(m.conn):
+        d = _dofs(c)
+        mat = Material.iso(m.E, m.nu, float(m.thickness[e]))
+        K[np.ix_(d, d)] += element_matrix(m.order, 0, STIFFNESS, mat, m.X[c], z)
+        G[np.ix_(d, d)] += element_matrix(m.order, 0, GEOMETRIC, mat, m.X[c], u[d])
+    return K, G
+
+
+def dense_buckling_groups(m):
+    """Path, lowest loads and eigenvectors of a per-element-thickness mesh
+    (dense FP64): (u, lam, phi, K, G) on the full DOF vector."""
+    import scipy.linalg as sla
+    ds = DenseShell(m)
+    fr = ds.free
+    K, _ = mesh_matrices(m, np.zeros(ds.N))
+    f = m.rhs.ravel()
+    u = np.zeros(ds.N)
+    u[fr] = np.linalg.solve(K[np.ix_(fr, fr)], f[fr])
+    K, G = mesh_matrices(m, u)
+    Kf, Gf = K[np.ix_(fr, fr)], G[np.ix_(fr, fr)]
+    mu, V = sla.eigh(-0.5 * (Gf + Gf.T), 0.5 * (Kf + Kf.T))
+    order = np.argsort(-np.abs(mu))
+    lam = 1.0 / mu[order]
+    phi = np.zeros((ds.N, lam.size))
+    phi[fr] = V[:, order]
+    return u, lam, phi, K, G
