@@ -15,8 +15,8 @@ nonlinear preloaded state R(u, X) = s f the same formula holds with the
 tangent K_T(u) in place of K and psi^T R' in place of psi^T (K u)'.
 The thickness derivative (the documented evalEigenDVSens formula,
 src/TACSBuckling.cpp:359-382) uses the same adjoint with the element
-matrices differentiated in the shell thickness (central differences of the
-oracle's element routines), for a one-thickness mesh.
+matrices differentiated exactly in the shell thickness (they are
+t M1 + t^3 M3), for one thickness or per design group.
 Sizes: a few hundred nodes (dense matrices).
 """
 from __future__ import annotations
@@ -126,36 +126,45 @@ class DenseShell:
             out[c] += v.reshape(nn, 3)
         return -out / float(phi @ G @ phi)
 
-    def thickness_sens(self, X, u, lam, phi, K, G, rel_step=1e-6):
+    def thickness_sens(self, X, u, lam, phi, K, G):
         """dlam/dt for the mesh's single thickness t (linear elements):
         -[phi^T K' phi + lam phi^T G'(u) phi - lam psi^T K' u] / phi^T G phi,
-        K psi = G(phi) phi, ' = d/dt by central differences of the element
-        matrices (they are polynomial in t)."""
+        K psi = G(phi) phi, ' = d/dt of the element matrices, exact
+        (_dt_element: they are t M1 + t^3 M3)."""
         fr = self.free
         t0 = float(self.mat.t)
-        h = rel_step * t0
         g = self.matrix(X, GEOMETRIC, phi) @ phi
         psi = np.zeros(self.N)
         psi[fr] = np.linalg.solve(K[np.ix_(fr, fr)], g[fr])
-        mats = []
-        for tt in (t0 + h, t0 - h):
-            self.mat = Material.iso(self.m.E, self.m.nu, tt)
-            mats.append((self.matrix(X, STIFFNESS, np.zeros(self.N)), self.matrix(X, GEOMETRIC, u)))
-        self.mat = Material.iso(self.m.E, self.m.nu, t0)
-        dK = (mats[0][0] - mats[1][0]) / (2 * h)
-        dG = (mats[0][1] - mats[1][1]) / (2 * h)
-        num = phi @ dK @ phi + lam * (phi @ dG @ phi) - lam * (psi @ dK @ u)
+        z = np.zeros(6 * self.order ** 2)
+        num = 0.0
+        for c in self.m.conn:
+            d = _dofs(c)
+            dK = _dt_element(self.order, STIFFNESS, self.m.E, self.m.nu, t0, X[c], z)
+            dG = _dt_element(self.order, GEOMETRIC, self.m.E, self.m.nu, t0, X[c], u[d])
+            num += phi[d] @ dK @ phi[d] + lam * (phi[d] @ dG @ phi[d]) - lam * (psi[d] @ dK @ u[d])
         return -num / float(phi @ G @ phi)
 
 
-def thickness_sens_groups(m, u, lam, phi, K, G, rel_step=1e-6):
+def _dt_element(order, kind, E, nu, t, X, v):
+    """d M_e/dt of an element matrix, exactly: with no thickness offset the
+    shell's constitutive matrix is t x (membrane, shear, drilling) plus
+    t^3 x (bending), so M_e(t) = t M1 + t^3 M3 and M1, M3 follow from the
+    matrices at t = 1 and t = 2; dM/dt = M1 + 3 t^2 M3."""
+    M1t = element_matrix(order, 0, kind, Material.iso(E, nu, 1.0), X, v)
+    M2t = element_matrix(order, 0, kind, Material.iso(E, nu, 2.0), X, v)
+    M3 = (M2t - 2.0 * M1t) / 6.0
+    M1 = M1t - M3
+    return M1 + 3.0 * t * t * M3
+
+
+def thickness_sens_groups(m, u, lam, phi, K, G):
     """dlam/dt_g for every thickness group of a mesh with per-element
-    thickness m.thickness and groups m.dv_group (linear elements): the same
-    formula as DenseShell.thickness_sens with the element matrices of group
-    g's elements differentiated in their thickness (central differences of
-    the oracle's element routines, step rel_step * t_e), the adjoint psi
-    shared by all groups.  Dense FP64; returns one value per group id up to
-    max(dv_group)."""
+    thickness m.thickness and groups m.dv_group (linear elements): the
+    formula of DenseShell.thickness_sens with the element matrices of group
+    g's elements differentiated in their thickness (exactly, _dt_element),
+    the adjoint psi shared by all groups.  Dense FP64; returns one value per
+    group id up to max(dv_group)."""
     ds = DenseShell(m)
     fr = ds.free
     X = m.X
@@ -172,13 +181,9 @@ def thickness_sens_groups(m, u, lam, phi, K, G, rel_step=1e-6):
     z = np.zeros(6 * ds.order ** 2)
     for e, c in enumerate(m.conn):
         d = _dofs(c)
-        t0 = float(m.thickness[e])
-        h = rel_step * t0
-        dK = dG = 0.0
-        for sgn in (1.0, -1.0):
-            mat = Material.iso(m.E, m.nu, t0 + sgn * h)
-            dK = dK + sgn * element_matrix(ds.order, 0, STIFFNESS, mat, X[c], z) / (2 * h)
-            dG = dG + sgn * element_matrix(ds.order, 0, GEOMETRIC, mat, X[c], u[d]) / (2 * h)
+        t = float(m.thickness[e])
+        dK = _dt_element(ds.order, STIFFNESS, m.E, m.nu, t, X[c], z)
+        dG = _dt_element(ds.order, GEOMETRIC, m.E, m.nu, t, X[c], u[d])
         num[m.dv_group[e]] += (phi[d] @ dK @ phi[d] + lam * (phi[d] @ dG @ phi[d])
                                - lam * (psi[d] @ dK @ u[d]))
     return -num / float(phi @ G @ phi)

@@ -1,0 +1,161 @@
+"""Eigenvalue sensitivities on the GPU against the reference's element
+derivatives and the dense CPU restatement of the sensitivity formulas.
+
+* d(psi^T K phi)/dt and d(psi^T G phi)/dt of one element (the reference's
+  TACSElement::addMatDVSensInnerProduct, complex-step build, fixtures
+  tests/golden/elements_*.npz): 1e-9 for K, 1e-7 for G (the reference's G
+  is its own central difference of the nonlinear tangent; its real-mode and
+  complex-step G products differ by up to 2.3e-7).
+* dlambda/dt_g (a2ds_eig_sens_thickness) against oracle/sens.py's dense
+  restatement of the documented formula (src/TACSBuckling.cpp:359-382, the
+  load-path adjoint included): 1e-6 of the largest |dlambda/dt_g| (the
+  spec bound), for a one-thickness cylinder and for every one of the
+  400 groups of the stiffened panel; central differences of whole solves
+  (step 1e-6 t_g) on 10 seeded panel groups.
+* dlambda/ds_p for 8 of the 64 radial shape parameters (a2ds_eig_sens_xpts
+  contracted with dX/ds_p) against the dense restatement of
+  evalEigenXptSens: 1e-6 of the largest |dlambda/ds_p|, on a cylinder with a
+  large imperfection so that the lowest load is simple (the derivative of a
+  double eigenvalue's members is not defined).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import oracle.sens as osens
+from conftest import GOLDEN
+from a2ds import capi
+from a2ds import mesh as meshgen
+
+TYPES = [("TACSQuad4Shell", 2, 0), ("TACSQuad4NonlinearShell", 2, 1),
+         ("TACSQuad9Shell", 3, 0), ("TACSQuad9NonlinearShell", 3, 1)]
+
+
+def one_element(X, order, nl, E, nu, t, alpha, temp):
+    nn = order * order
+    a = capi.Assembler(X.reshape(nn, 3), np.arange(nn, dtype=np.int32)[None, :], nonlinear=nl)
+    a.set_material(E, nu, alpha, temp)
+    a.set_thickness([t])
+    a.initialize(capi.A2DS_NATURAL_ORDER)
+    return a
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,order,nl", TYPES)
+def test_element_thickness_products_vs_reference(name, order, nl):
+    f = np.load(os.path.join(GOLDEN, f"elements_{name}.npz"))
+    nn = order * order
+    checked = 0
+    for s in range(f["X"].shape[0]):
+        E, nu, t, alpha, temp, _ = f["params"][s]
+        if temp != 0.0:
+            continue
+        a = one_element(f["X"][s], order, nl, E, nu, t, alpha, temp)
+        v = f["vars"][s].reshape(nn, 6)
+        psi, phi = f["xs_psi"][s].reshape(nn, 6), f["xs_phi"][s].reshape(nn, 6)
+        kd = a.add_mat_dv_sens_inner_product(1.0, capi.A2DS_STIFFNESS_MATRIX, psi, phi,
+                                             np.zeros(1), vars_=v)[0]
+        gd = a.add_mat_dv_sens_inner_product(1.0, capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, psi, phi,
+                                             np.zeros(1), vars_=v)[0]
+        assert abs(kd - f["KD_cs"][s]) <= 1e-9 * abs(f["KD_cs"][s]), (name, s, kd, f["KD_cs"][s])
+        assert abs(gd - f["GD_cs"][s]) <= 1e-7 * abs(f["GD_cs"][s]), (name, s, gd, f["GD_cs"][s])
+        checked += 1
+    assert checked >= 4
+
+
+def gpu_assembler(m, X=None, tvals=None, groups=None):
+    a = capi.Assembler(m.X if X is None else X, m.conn)
+    a.set_material(m.E, m.nu)
+    if tvals is None:
+        a.set_thickness(m.thickness[:1])
+    else:
+        a.set_thickness(np.asarray(tvals, float), groups)
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    return a
+
+
+def lowest_load_solver(a, m, sigma):
+    b = capi.LinearBuckling(a, sigma, max_lanczos=120, num_eigvals=2, eig_tol=1e-13,
+                            precision=64, block_size=2)
+    lam = b.solve(m.rhs)
+    return b, lam
+
+
+@pytest.mark.gpu
+def test_thickness_sensitivity_vs_dense_oracle():
+    m = meshgen.cylinder(4, 8, imperfection=50.0)
+    ds = osens.DenseShell(m)
+    u = ds.state(m.X)
+    lam, phi, K, G = ds.buckling(m.X, u)
+    ref = ds.thickness_sens(m.X, u, lam[0], phi[:, 0], K, G)
+    b, lamg = lowest_load_solver(gpu_assembler(m), m, 0.9 * lam[0])
+    assert abs(lamg[0] - lam[0]) <= 1e-9 * abs(lam[0])
+    d = b.eig_sens_thickness(0, 1)[0]
+    assert abs(d - ref) <= 1e-6 * abs(ref), (d, ref)
+
+
+@pytest.fixture(scope="module")
+def panel():
+    m = meshgen.stiffened_panel(4, 8, 1)
+    u, lam, phi, K, G = osens.dense_buckling_groups(m)
+    tv = m.meta["tvals"]
+    a = gpu_assembler(m, tvals=tv, groups=m.dv_group)
+    b, lamg = lowest_load_solver(a, m, 0.9 * lam[0])
+    return m, tv, lam, lamg, b, (u, phi, K, G)
+
+
+@pytest.mark.gpu
+def test_panel_thickness_sensitivities_all_groups_vs_dense_oracle(panel):
+    m, tv, lam, lamg, b, (u, phi, K, G) = panel
+    assert abs(lamg[0] - lam[0]) <= 1e-9 * abs(lam[0])
+    ref = osens.thickness_sens_groups(m, u, lam[0], phi[:, 0], K, G)
+    d = b.eig_sens_thickness(0, tv.size)
+    assert d.size == 400
+    used = np.unique(m.dv_group)
+    assert np.all(d[np.setdiff1d(np.arange(tv.size), used)] == 0.0)
+    assert np.max(np.abs(d[:ref.size] - ref)) <= 1e-6 * np.max(np.abs(ref)), \
+        np.max(np.abs(d[:ref.size] - ref)) / np.max(np.abs(ref))
+
+
+@pytest.mark.gpu
+def test_panel_thickness_sensitivities_10_seeded_groups_vs_finite_difference(panel):
+    """Central differences of whole GPU solves, step 1e-6 t_g, on 10 seeded
+    groups (the stiffened-panel workload's check).  The differences carry
+    the eigenvalue's solve noise over the step (~1e-12 relative / 1e-6):
+    the absolute term; the 1e-6 bound itself is shown against the dense
+    restatement above, which differentiates exactly."""
+    m, tv, lam, lamg, b, _ = panel
+    d = b.eig_sens_thickness(0, tv.size)
+    used = np.unique(m.dv_group)
+    rng = np.random.default_rng(20261203)
+    for g in rng.choice(used, 10, replace=False):
+        h = 1e-6 * tv[g]
+        out = []
+        for sgn in (1.0, -1.0):
+            t2 = tv.copy()
+            t2[g] += sgn * h
+            out.append(lowest_load_solver(gpu_assembler(m, tvals=t2, groups=m.dv_group), m,
+                                          0.9 * lam[0])[1][0])
+        fd = (out[0] - out[1]) / (2 * h)
+        assert abs(d[g] - fd) <= 1e-6 * abs(fd) + 2e-6 * abs(lamg[0]) / tv[g], (g, d[g], fd)
+
+
+@pytest.mark.gpu
+def test_shape_sensitivities_8_parameters_vs_dense_oracle():
+    m = meshgen.cylinder(8, 16, imperfection=50.0)
+    ds = osens.DenseShell(m)
+    u = ds.state(m.X)
+    lam, phi, K, G = ds.buckling(m.X, u)
+    assert abs(lam[1] - lam[0]) > 1e-3 * abs(lam[0])  # a simple lowest load
+    refX = ds.xpt_sens(m.X, u, lam[0], phi[:, 0], K, G)
+    b, lamg = lowest_load_solver(gpu_assembler(m), m, 0.9 * lam[0])
+    assert abs(lamg[0] - lam[0]) <= 1e-9 * abs(lam[0])
+    dX = b.eval_eigen_xpt_sens(0)
+    modes = meshgen.radial_shape_modes(m)
+    ps = np.random.default_rng(20261203).choice(64, 8, replace=False)
+    ref = np.array([np.sum(refX * modes[p]) for p in ps])
+    got = np.array([np.sum(dX * modes[p]) for p in ps])
+    assert np.max(np.abs(got - ref)) <= 1e-6 * np.max(np.abs(ref)), (ps, got, ref)
