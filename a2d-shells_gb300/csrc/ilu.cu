@@ -327,18 +327,31 @@ void build_solve_schedule(Factor &f) {
     for (int c = 0; c < nc; c++)
       L.max_rows[lev[c]] = std::max(L.max_rows[lev[c]], cp.c0[c + 1] - cp.c0[c]);
     L.cta.assign(L.nlevels, 0);
+    L.split.assign(L.nlevels, 1);
     for (int l = 0; l < L.nlevels; l++) {
       int maxlen = 0;
+      bool single = false;
       for (int k = L.row_ptr[l]; k < L.row_ptr[l + 1]; k++) {
         const int i = L.rows[k];
         const int len = upper ? f.frowp[i + 1] - cp.row_ustart[i] : cp.row_lend[i] - f.frowp[i];
         maxlen = std::max(maxlen, len);
+        single = single || cp.row_single[i];
       }
       L.cta[l] = maxlen > SOLVE_LONG_ROW;
+      // long rows of levels with few rows: split over CTAs (atomic partial
+      // sums), except upper rows that are their own chunk (finished by
+      // D^{-1} after the full sum)
+      const int nr = L.row_ptr[l + 1] - L.row_ptr[l];
+      if (L.cta[l] && nr < 4 * 152 && !(upper && single))
+        L.split[l] = std::min(32, std::max(1, maxlen / SOLVE_SPLIT_BLOCKS));
     }
   };
   fill_levels(lv, maxl, false, cp.lo);
   fill_levels(uv, maxu, true, cp.up);
+  for (int c = 0; c < nc; c++) {
+    const int ns = cp.c0[c + 1] - cp.c0[c];
+    if (ns >= 2) (ns <= 10 ? cp.small : cp.big).push_back(c);
+  }
 }
 
 int upload_schedules(Factor &f, cudaStream_t s) {
@@ -357,6 +370,8 @@ int upload_schedules(Factor &f, cudaStream_t s) {
   if ((rc = f.d_lo_chunks.upload(cp.lo.chunks.data(), cp.lo.chunks.size(), s))) return rc;
   if ((rc = f.d_up_rows.upload(cp.up.rows.data(), cp.up.rows.size(), s))) return rc;
   if ((rc = f.d_up_chunks.upload(cp.up.chunks.data(), cp.up.chunks.size(), s))) return rc;
+  if ((rc = f.d_ck_small.upload(cp.small.data(), cp.small.size(), s))) return rc;
+  if ((rc = f.d_ck_big.upload(cp.big.data(), cp.big.size(), s))) return rc;
   const PanelSchedule &pn = f.pn;
   if ((rc = f.d_pn_prow.upload(pn.prow.data(), pn.prow.size(), s))) return rc;
   if ((rc = f.d_pn_uc.upload(pn.uc.data(), pn.uc.size(), s))) return rc;

@@ -62,6 +62,7 @@ struct ChunkLevels {
   std::vector<int> ch_ptr, chunks;  // chunks of >= 2 rows of each level
   std::vector<char> cta;            // per level: 1 = one CTA per row (long rows)
   std::vector<int> max_rows;        // per level: rows of its largest chunk
+  std::vector<int> split;           // per level: CTAs sharing each long row (1 = none)
 };
 struct ChunkPlan {
   std::vector<int> c0;          // chunk starts (nchunks + 1 entries, last = n)
@@ -74,6 +75,7 @@ struct ChunkPlan {
   std::vector<int> row_ustart;  // per row: start of its upper pull (first column past its chunk)
   std::vector<int> row_single;  // per row: 1 if its chunk is the row alone
   ChunkLevels lo, up;           // up: level 0 solved first (top of the ordering)
+  std::vector<int> small, big;  // multi-row chunks of at most / more than 10 rows
 };
 
 // A factorization handle (the TACSSchurPc role on one GPU).
@@ -98,7 +100,7 @@ struct Factor {
   ChunkPlan cp;
   DBuf<int> d_ck_c0, d_row_lend, d_row_ustart, d_row_single;
   DBuf<long long> d_ck_off;
-  DBuf<int> d_lo_rows, d_lo_chunks, d_up_rows, d_up_chunks;
+  DBuf<int> d_lo_rows, d_lo_chunks, d_up_rows, d_up_chunks, d_ck_small, d_ck_big;
   DBuf<double> cinv64, cscr64;  // FP64 inverses (all precisions) and gathered blocks
   DBuf<float> cinv32;           // FP32 copy of the inverses for FP32 factors
   // algorithmic FP operations of one numeric factorization: 432 per L block
@@ -145,6 +147,8 @@ constexpr int PANEL_UC_SMEM = 8192;
 // a pull level uses one CTA per row.
 constexpr int CHUNK_MAX = 128;
 constexpr int SOLVE_LONG_ROW = 24;
+// factor blocks per CTA when a level's long rows are split over CTAs
+constexpr int SOLVE_SPLIT_BLOCKS = 384;
 
 // F (f.precision: 64 double, 48 double-float, 32 float values; 8 bytes per
 // value for 64 and 48) <- pattern-embedded copy of A (+ alpha2 * A2 when

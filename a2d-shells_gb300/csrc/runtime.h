@@ -42,7 +42,8 @@ struct Mesh {
 
   // buckling-solve state kept for sensitivities / stats
   std::vector<double> stats;
-  void *solver = nullptr;  // BucklingState*
+  void *solver = nullptr;   // BucklingState*
+  void *preload = nullptr;  // PreloadState* (Newton load stepping)
 
   int build_pattern();
   int upload();

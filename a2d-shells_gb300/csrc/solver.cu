@@ -404,6 +404,7 @@ struct BucklingState {
   // the path solve uses its leading n6 x 1)
   IrWork ir;
   DBuf<float> gw32;
+  bool preloaded = false;  // K holds K_T(u) and path the preload state u
   std::vector<double> lam, err, ritz;  // converged data
   int nconv = 0;
   double sigma = 0.0;
@@ -443,9 +444,12 @@ struct BucklingState {
   }
 };
 
+struct PreloadState;
+static void release_preload(Mesh &m);
 void release_solver(Mesh &m) {
   delete (BucklingState *)m.solver;
   m.solver = nullptr;
+  release_preload(m);
 }
 
 static double now() {
@@ -704,6 +708,18 @@ static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const doubl
   }
 }
 
+// A = K (or K_T) solves with the factor f and FP64 refinement: GMRES-IR for
+// an FP32 factor, iterative refinement for FP64 and double-float factors.
+static int solve_k(Mesh &m, BucklingState &S, Factor &f, const double *Avals, const double *b,
+                   double *x, double rtol, int *inner) {
+  if (f.precision == 32) {
+    auto pc = [&](const double *V, double *Z) { return S.precond(m, f, V, Z, 1); };
+    return fgmres_block_solve(m, S.ir, pc, Avals, b, x, 1, rtol, GMRES_IR_MSUB, GMRES_IR_CYCLES,
+                              inner);
+  }
+  return refined_block_solve(m, S, f, Avals, b, x, 1, rtol, 4, inner);
+}
+
 // K-orthonormalise the block W (with KW = K W): one Cholesky-QR pass,
 // W <- W R^{-1}, KW <- KW R^{-1}, W^T K W = R^T R.  Returns R (host).
 static int cholqr_pass(Mesh &m, BucklingState &S, double *W, double *KW, int p,
@@ -888,6 +904,43 @@ static int gmres_device(Mesh &m, Factor *pc, const double *Avals, const double *
   if (res_norm) *res_norm = resnorm;
   return flag ? 0 : fail(A2DS_ERR_NOCONV, "GMRES did not reach the tolerance (residual " +
                                              std::to_string(resnorm) + ")");
+}
+
+// ------------------------------------------------------ nonlinear preload
+// Newton load stepping on R(u) = s f with the exact tangent (the reference
+// has the building blocks, assembleRes / assembleJacobian and TACSSchurPc,
+// but no driver): state and buffers, kept per mesh between calls.
+struct PreloadState {
+  Factor ft;  // complete LU of K_T(u)
+  int precision = 0;
+  DBuf<double> KT, R, u, f, r, du, ubc;
+  DBuf<double> xb, yb;
+  DBuf<float> w32;
+  IrWork ir;
+};
+
+static void release_preload(Mesh &m) {
+  delete (PreloadState *)m.preload;
+  m.preload = nullptr;
+}
+
+// r = R - s f, then the Dirichlet rows r = u - u_bc (the assembler's BC
+// residual); ubc holds 6 values per Dirichlet entry.
+__global__ void k_newton_residual(double *r, const double *R, const double *f, double s,
+                                  size_t n6) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n6;
+       i += (size_t)gridDim.x * blockDim.x)
+    r[i] = R[i] - s * f[i];
+}
+__global__ void k_newton_bc(double *r, const double *u, const int *bc_rows, const int *bc_masks,
+                            const double *ubc, int nbc) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbc * 6) return;
+  const int b = t / 6, k = t % 6;
+  if (bc_masks[b] & (1 << k)) {
+    const size_t i = (size_t)bc_rows[b] * 6 + k;
+    r[i] = u[i] - ubc[t];
+  }
 }
 
 }  // namespace a2ds
@@ -1352,6 +1405,7 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   int rc;
   if ((rc = prepare_solve(m, opts, &Sp))) return rc;
   BucklingState &S = *Sp;
+  S.preloaded = false;
   const int nev = opts->num_eigvals, p = opts->block_size;
   const size_t n6 = (size_t)m.nn * 6;
   Blas B{m.stream};
@@ -1399,14 +1453,8 @@ int a2ds_buckling_solve(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const do
   // for the path and on K + sigma G inside the shift-invert operator
   const bool direct = opts->lev_fill >= m.nn;
   GmresWork gw;
-  if (direct && S.fk.precision == 32) {
-    auto pc = [&](const double *V, double *Z) { return S.precond(m, S.fk, V, Z, 1); };
-    if ((rc = fgmres_block_solve(m, S.ir, pc, S.K.p, S.rhs.p, S.path.p, 1, 1e-13, GMRES_IR_MSUB,
-                                 GMRES_IR_CYCLES, &inner)))
-      return rc;
-  } else if (direct) {
-    if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.rhs.p, S.path.p, 1, 1e-13, 4, &inner)))
-      return rc;
+  if (direct) {
+    if ((rc = solve_k(m, S, S.fk, S.K.p, S.rhs.p, S.path.p, 1e-13, &inner))) return rc;
   } else {
     int it = 0;
     double rn = 0.0;
@@ -1458,6 +1506,7 @@ int a2ds_eigen_shift_invert(a2ds_mesh mesh, const a2ds_buckling_opts *opts, a2ds
   BucklingState *Sp = nullptr;
   int rc;
   if ((rc = prepare_solve(m, opts, &Sp))) return rc;
+  Sp->preloaded = false;
   BucklingState &S = *Sp;
   const int nev = opts->num_eigvals, p = opts->block_size;
   const size_t n6 = (size_t)m.nn * 6;
@@ -1536,7 +1585,7 @@ static int path_adjoint(Mesh &m, BucklingState &S, const double *phi, double *ps
   }
   int inner = 0;
   if (S.lev_fill >= m.nn) {
-    if ((rc = refined_block_solve(m, S, S.fk, S.K.p, S.t.p, psi, 1, 1e-13, 4, &inner))) return rc;
+    if ((rc = solve_k(m, S, S.fk, S.K.p, S.t.p, psi, 1e-13, &inner))) return rc;
   } else {
     GmresWork gw;
     double rn = 0.0;
@@ -1552,6 +1601,8 @@ int a2ds_eig_sens_thickness(a2ds_mesh mesh, int n, double *dlam_dt) {
   BucklingState *Sp = (BucklingState *)m.solver;
   if (!Sp || Sp->lam.empty())
     return fail(A2DS_ERR_STATE, "eigenvalue sensitivities need a preceding a2ds_buckling_solve");
+  if (Sp->preloaded)
+    return fail(A2DS_ERR_STATE, "the last solve was about a preloaded state: use a2ds_preload_xpt_sens");
   BucklingState &S = *Sp;
   if (n < 0 || n >= (int)S.lam.size()) return fail(A2DS_ERR_ARG, "eigenvalue index out of range");
   if (m.alpha * m.temperature != 0.0)
@@ -1599,6 +1650,8 @@ int a2ds_eig_sens_xpts(a2ds_mesh mesh, int n, double dh, double *dlam_dX) {
   BucklingState *Sp = (BucklingState *)m.solver;
   if (!Sp || Sp->lam.empty())
     return fail(A2DS_ERR_STATE, "eigenvalue sensitivities need a preceding a2ds_buckling_solve");
+  if (Sp->preloaded)
+    return fail(A2DS_ERR_STATE, "the last solve was about a preloaded state: use a2ds_preload_xpt_sens");
   BucklingState &S = *Sp;
   if (n < 0 || n >= (int)S.lam.size()) return fail(A2DS_ERR_ARG, "eigenvalue index out of range");
   if (m.alpha * m.temperature != 0.0)
@@ -1628,6 +1681,194 @@ int a2ds_eig_sens_xpts(a2ds_mesh mesh, int n, double dh, double *dlam_dX) {
   if ((rc = m.fd_sens(L, dh, 0, dlam_dX))) return rc;
   const double s = -1.0 / phiGphi;
   for (size_t i = 0; i < (size_t)m.nn * 3; i++) dlam_dX[i] *= s;
+  return 0;
+}
+
+int a2ds_newton_preload(a2ds_mesh mesh, const double *rhs, double load, int nsteps, double rtol,
+                        int max_newton, int precision, double *u_out, int *iters,
+                        double *rel_out) {
+  if (!mesh || !rhs || !u_out) return fail(A2DS_ERR_ARG, "null argument");
+  Mesh &m = mesh->m;
+  if (!m.initialized) return fail(A2DS_ERR_STATE, "mesh not initialized");
+  if (nsteps < 1 || max_newton < 1 || !(rtol > 0.0) || !std::isfinite(load))
+    return fail(A2DS_ERR_ARG, "need nsteps >= 1, max_newton >= 1, rtol > 0 and a finite load");
+  if (precision != 64 && precision != 48 && precision != 32)
+    return fail(A2DS_ERR_ARG, "precision must be 64, 48 or 32");
+  const size_t n6 = (size_t)m.nn * 6, nv = (size_t)m.nnzb * 36;
+  const int nbc = (int)m.bc_rows.size();
+  int rc;
+  PreloadState *P = (PreloadState *)m.preload;
+  if (!P || P->precision != precision) {
+    release_preload(m);
+    P = new PreloadState();
+    m.preload = P;
+    P->precision = precision;
+    if ((rc = factor_setup(m, m.nn, precision, P->ft))) return rc;
+  }
+  if ((rc = P->KT.alloc(nv)) || (rc = P->R.alloc(n6)) || (rc = P->u.alloc(n6)) ||
+      (rc = P->r.alloc(n6)) || (rc = P->du.alloc(n6)) || (rc = P->xb.alloc(n6)) ||
+      (rc = P->yb.alloc(n6)) || (precision == 32 && (rc = P->w32.alloc(n6))))
+    return rc;
+  if ((rc = m.to_rows(rhs, P->f))) return rc;
+  if (nbc) {
+    k_zero_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(P->f.p, m.d_bc_rows.p,
+                                                           m.d_bc_masks.p, nbc);
+    m.launches++;
+    if ((rc = P->ubc.upload(m.bc_vals.data(), m.bc_vals.size(), m.stream))) return rc;
+  }
+  A2DS_CUDA_TRY(cudaMemsetAsync(P->u.p, 0, n6 * sizeof(double), m.stream));
+  Blas B{m.stream};
+  B.launches = &m.launches;
+  const double fn = sqrt(B.dot(P->f.p, P->f.p, n6));
+  if (!(fn > 0.0)) return fail(A2DS_ERR_ARG, "zero load vector");
+  auto pc = [&](const double *V, double *Z) {
+    return precondition_block(m, P->ft, V, Z, 1, P->w32.p, P->xb.p, P->yb.p);
+  };
+  double rel = 0.0;
+  for (int k = 1; k <= nsteps; k++) {
+    const double s = load * k / nsteps;
+    int it = 0;
+    for (;; it++) {
+      if ((rc = m.assemble_device(MODE_KR, P->u.p, P->KT.p, P->R.p, A2DS_SCATTER_ATOMIC)))
+        return rc;
+      k_newton_residual<<<grid_for(n6), 256, 0, m.stream>>>(P->r.p, P->R.p, P->f.p, s, n6);
+      m.launches++;
+      if (nbc) {
+        k_newton_bc<<<(nbc * 6 + 255) / 256, 256, 0, m.stream>>>(
+            P->r.p, P->u.p, m.d_bc_rows.p, m.d_bc_masks.p, P->ubc.p, nbc);
+        m.launches++;
+      }
+      rel = sqrt(B.dot(P->r.p, P->r.p, n6)) / (fabs(s) * fn);
+      if (!std::isfinite(rel)) return fail(A2DS_ERR_NUMERIC, "Newton residual is not finite");
+      if (rel <= rtol) break;
+      if (it == max_newton) {
+        char msg[160];
+        snprintf(msg, sizeof msg,
+                 "Newton did not converge in load step %d: relative residual %.3e", k, rel);
+        return fail(A2DS_ERR_NOCONV, msg);
+      }
+      if ((rc = factor_numeric(m, P->ft, P->KT.p, nullptr, 0.0)) ||
+          (rc = factor_check(m, P->ft)))
+        return rc;
+      int inner = 0;
+      if ((rc = fgmres_block_solve(m, P->ir, pc, P->KT.p, P->r.p, P->du.p, 1, 1e-12,
+                                   GMRES_IR_MSUB, GMRES_IR_CYCLES, &inner)))
+        return rc;
+      B.axpby(P->u.p, -1.0, P->du.p, 1.0, n6);  // u <- u - du
+    }
+    if (iters) iters[k - 1] = it;
+  }
+  if (rel_out) *rel_out = rel;
+  return m.from_rows(P->u.p, u_out);
+}
+
+int a2ds_preload_buckling(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const double *u,
+                          double *eigvals, double *errors, double *eigvecs) {
+  if (!mesh || !opts || !u || !eigvals) return fail(A2DS_ERR_ARG, "null argument");
+  Mesh &m = mesh->m;
+  double t0 = now();
+  long long launches0 = m.launches;
+  BucklingState *Sp = nullptr;
+  int rc;
+  if ((rc = prepare_solve(m, opts, &Sp))) return rc;
+  BucklingState &S = *Sp;
+  S.preloaded = false;
+  Blas B{m.stream};
+  B.launches = &m.launches;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[0], m.stream));
+  DBuf<double> du;
+  if ((rc = m.to_rows(u, du))) return rc;
+  A2DS_CUDA_TRY(cudaMemcpyAsync(S.path.p, du.p, (size_t)m.nn * 6 * sizeof(double),
+                                cudaMemcpyDeviceToDevice, m.stream));
+  double ta = now();
+  if ((rc = m.assemble_device(MODE_K, S.path.p, S.K.p, nullptr, A2DS_SCATTER_ATOMIC))) return rc;
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  const double t_k = now() - ta;
+  ta = now();
+  if ((rc = m.assemble_device(MODE_G, S.path.p, S.G.p, nullptr, A2DS_SCATTER_ATOMIC))) return rc;
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  const double t_g = now() - ta;
+  const bool direct = opts->lev_fill >= m.nn;
+  GmresWork gw;
+  int inner = 0;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[4], m.stream));
+  if (!direct) {  // GMRES inside the operator is preconditioned by the factor of K_T
+    if ((rc = factor_numeric(m, S.fk, S.K.p, nullptr, 0.0)) || (rc = factor_check(m, S.fk)))
+      return rc;
+  }
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[5], m.stream));
+  PhaseOut po;
+  if ((rc = shift_invert_phase(m, S, opts, B, direct, gw, inner, eigvals, errors, eigvecs, po)))
+    return rc;
+  S.nconv = po.converged ? opts->num_eigvals : 0;
+  S.preloaded = true;
+  A2DS_CUDA_TRY(cudaEventRecord(S.ev[1], m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  float ms_solve = 0.f, ms_fa = 0.f, ms_fk = 0.f;
+  cudaEventElapsedTime(&ms_solve, S.ev[0], S.ev[1]);
+  cudaEventElapsedTime(&ms_fa, S.ev[2], S.ev[3]);
+  cudaEventElapsedTime(&ms_fk, S.ev[4], S.ev[5]);
+  m.stats = {now() - t0, t_k, t_g, po.t_fa, 0.0, po.t_lan, (double)po.mdim, (double)inner,
+             (double)(m.launches - launches0), (double)ms_solve, (double)ms_fa, (double)ms_fk,
+             (double)S.fk.nnzb(), (double)S.fk.flv.nlevels, (double)S.fk.flops(),
+             (double)opts->block_size, (double)po.nsteps, S.solve_ms(), (double)(S.ntev / 2),
+             (double)S.ir.iters, (double)S.ir.cycles};
+  if (!po.converged)
+    return fail(A2DS_ERR_NOCONV, "Lanczos did not converge within max_lanczos (results returned are the current Ritz pairs)");
+  return 0;
+}
+
+int a2ds_preload_xpt_sens(a2ds_mesh mesh, int n, double dh, double *dlam_dX) {
+  if (!mesh || !dlam_dX) return fail(A2DS_ERR_ARG, "null argument");
+  Mesh &m = mesh->m;
+  BucklingState *Sp = (BucklingState *)m.solver;
+  if (!Sp || !Sp->preloaded || Sp->lam.empty())
+    return fail(A2DS_ERR_STATE, "needs a preceding a2ds_preload_buckling on this mesh");
+  BucklingState &S = *Sp;
+  if (n < 0 || n >= (int)S.lam.size()) return fail(A2DS_ERR_ARG, "eigenvalue index out of range");
+  if (dh == 0.0) dh = 1e-7;
+  const size_t n6 = (size_t)m.nn * 6;
+  const double lam = S.lam[n];
+  int rc;
+  std::vector<double> phi(n6), u(n6), g(n6), g2(n6), psi(n6);
+  if ((rc = m.from_rows(S.phi.p + (size_t)n * n6, phi.data())) ||
+      (rc = m.from_rows(S.path.p, u.data())))
+    return rc;
+  // phi^T G phi (phi vanishes on the Dirichlet DOFs)
+  Blas B{m.stream};
+  B.launches = &m.launches;
+  if ((rc = launch_spmv_f64(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, S.phi.p + (size_t)n * n6, S.r.p,
+                            m.stream)))
+    return rc;
+  const double phiGphi = B.dot(S.phi.p + (size_t)n * n6, S.r.p, n6);
+  if (!(phiGphi != 0.0) || !std::isfinite(phiGphi))
+    return fail(A2DS_ERR_NUMERIC, "phi^T G phi vanishes");
+  // adjoint: K_T(u) psi = d/du [phi^T (K_T(u) + lam G(u)) phi]
+  if ((rc = a2ds_eval_mat_sv_sens_inner_product(mesh, A2DS_STIFFNESS_MATRIX, phi.data(),
+                                                phi.data(), u.data(), dh, g.data())) ||
+      (rc = a2ds_eval_mat_sv_sens_inner_product(mesh, A2DS_GEOMETRIC_STIFFNESS_MATRIX,
+                                                phi.data(), phi.data(), u.data(), dh,
+                                                g2.data())))
+    return rc;
+  for (size_t i = 0; i < n6; i++) g[i] += lam * g2[i];
+  if ((rc = factor_numeric(m, S.fk, S.K.p, nullptr, 0.0)) || (rc = factor_check(m, S.fk)))
+    return rc;
+  DBuf<double> dg;
+  if ((rc = m.to_rows(g.data(), dg))) return rc;
+  int inner = 0;
+  if ((rc = solve_k(m, S, S.fk, S.K.p, dg.p, S.t.p, 1e-13, &inner))) return rc;
+  if ((rc = m.from_rows(S.t.p, psi.data()))) return rc;
+  std::fill(dlam_dX, dlam_dX + (size_t)m.nn * 3, 0.0);
+  if ((rc = a2ds_add_mat_xpt_sens_inner_product(mesh, A2DS_STIFFNESS_MATRIX, 1.0, phi.data(),
+                                                phi.data(), u.data(), dh, dlam_dX)) ||
+      (rc = a2ds_add_mat_xpt_sens_inner_product(mesh, A2DS_GEOMETRIC_STIFFNESS_MATRIX, lam,
+                                                phi.data(), phi.data(), u.data(), dh,
+                                                dlam_dX)) ||
+      (rc = a2ds_add_adjoint_res_xpt_sens_product(mesh, -1.0, psi.data(), u.data(), dh,
+                                                  dlam_dX)))
+    return rc;
+  const double sc = -1.0 / phiGphi;
+  for (size_t i = 0; i < (size_t)m.nn * 3; i++) dlam_dX[i] *= sc;
   return 0;
 }
 

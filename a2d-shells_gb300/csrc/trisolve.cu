@@ -94,7 +94,9 @@ __global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows,
 }
 
 // The same for levels with long rows: one 256-thread CTA per row, 42 groups
-// of six threads over the row's blocks.
+// of six threads over the row's blocks.  With split > 1 a row's blocks are
+// shared by gridDim.y CTAs that subtract their partial sums from y_i with
+// atomic adds (y_i already holds src_i; not for rows finished with D_i^{-1}).
 template <typename T, typename TV, int R, bool UPPER>
 __global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, int nrows,
                                                   const int *__restrict__ frowp,
@@ -110,8 +112,14 @@ __global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, 
   const int i = rows[rr];
   const int t = threadIdx.x;
   const int g = t / 6, ii = t - 6 * g;
-  const int kb = UPPER ? bound[i] : frowp[i];
-  const int ke = UPPER ? frowp[i + 1] : bound[i];
+  int kb = UPPER ? bound[i] : frowp[i];
+  int ke = UPPER ? frowp[i + 1] : bound[i];
+  const int split = gridDim.y;
+  if (split > 1) {
+    const int per = (ke - kb + split - 1) / split;
+    kb += per * blockIdx.y;
+    ke = min(ke, kb + per);
+  }
   if (t < 252) {
     TV acc[R];
 #pragma unroll
@@ -127,12 +135,14 @@ __global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, 
     TV v = 0;
     for (int gg = 0; gg < 42; gg++) v += part[6 * gg + d][r];
     const size_t idx = ((size_t)i * 6 + d) * R + r;
-    if (fin)
+    if (split > 1)
+      atomicAdd(&y[idx], -v);
+    else if (fin)
       z[d][r] = src[idx] - v;
     else
       y[idx] = src[idx] - v;
   }
-  if (!fin) return;
+  if (!fin || split > 1) return;
   __syncthreads();
   const T *Dinv = F + (size_t)fdiag[i] * 36;
   for (int o = t; o < 6 * R; o += blockDim.x) {
@@ -178,7 +188,7 @@ __device__ __forceinline__ TV warp_reduce_scatter(TV (&v)[R], int lane, int &rhs
 // lower: only columns up to the row's block, upper: from it on), lanes over
 // the columns, and a reduce-scatter over the R right-hand sides.
 template <typename T, typename TV, int R, bool UPPER>
-__global__ void __launch_bounds__(256) k_chunk_apply(const int *__restrict__ chunks,
+__global__ void __launch_bounds__(1024) k_chunk_apply(const int *__restrict__ chunks,
                                                      const int *__restrict__ c0,
                                                      const long long *__restrict__ off,
                                                      const T *__restrict__ inv, TV *y) {
@@ -236,45 +246,57 @@ __global__ void __launch_bounds__(256) k_chunk_gather(const int *__restrict__ ch
   }
 }
 
-// Inverses of every multi-row chunk's diagonal block, one CTA per chunk and
-// one thread per column c of the identity.  Lower: the unit block-lower L
-// (forward substitution).  Upper: D + U with the stored D_i^{-1}:
-// z_i = D_i^{-1} (e_c - sum_{j > i} U_ij z_j), backward.
+// Inverses of every multi-row chunk's diagonal block (chunks[] of this
+// launch), one CTA per chunk and one thread per column c of the identity.
+// Lower: the unit block-lower L, forward substitution; its inverse is
+// block-lower, so column c starts at c's block row.  Upper: D + U with the
+// stored D_i^{-1}: z_i = D_i^{-1} (e_c - sum_{j > i} U_ij z_j), backward;
+// block-upper, so column c ends at c's block row.  The six rows of a block
+// row are formed together (one load of X[q][c] for six products).
 template <typename T, bool UPPER>
-__global__ void __launch_bounds__(256) k_chunk_inverse(const int *__restrict__ chunks,
-                                                       const int *__restrict__ c0,
-                                                       const long long *__restrict__ off,
-                                                       const T *__restrict__ Mall,
-                                                       T *__restrict__ inv) {
+__global__ void k_chunk_inverse(const int *__restrict__ chunks, const int *__restrict__ c0,
+                                const long long *__restrict__ off, const T *__restrict__ Mall,
+                                T *__restrict__ inv) {
   const int ch = chunks[blockIdx.x];
   const int ns = c0[ch + 1] - c0[ch], w = 6 * ns;
   const T *M = Mall + off[ch] / 2;
   T *X = inv + off[ch] + (UPPER ? (long long)w * w : 0);
   for (int c = threadIdx.x; c < w; c += blockDim.x) {
+    const int bc = c / 6;
     if (!UPPER) {
-      for (int i = 0; i < ns; i++)
-        for (int a = 0; a < 6; a++) {
-          const int r = 6 * i + a;
-          T v = (r == c) ? T(1) : T(0);
-          const T *Mr = M + (size_t)r * w;
-          for (int q = 0; q < 6 * i; q++) v -= Mr[q] * X[(size_t)q * w + c];
-          X[(size_t)r * w + c] = v;
+      for (int i = 0; i < ns; i++) {
+        T v[6];
+#pragma unroll
+        for (int a = 0; a < 6; a++) v[a] = (6 * i + a == c) ? T(1) : T(0);
+        if (i > bc) {
+          for (int q = 6 * bc; q < 6 * i; q++) {
+            const T xq = X[(size_t)q * w + c];
+#pragma unroll
+            for (int a = 0; a < 6; a++) v[a] -= M[(size_t)(6 * i + a) * w + q] * xq;
+          }
         }
+#pragma unroll
+        for (int a = 0; a < 6; a++) X[(size_t)(6 * i + a) * w + c] = v[a];
+      }
     } else {
       for (int i = ns - 1; i >= 0; i--) {
         T z[6];
-        for (int a = 0; a < 6; a++) {
-          const int r = 6 * i + a;
-          T v = (r == c) ? T(1) : T(0);
-          const T *Mr = M + (size_t)r * w;
-          for (int q = 6 * (i + 1); q < w; q++) v -= Mr[q] * X[(size_t)q * w + c];
-          z[a] = v;
+#pragma unroll
+        for (int a = 0; a < 6; a++) z[a] = (6 * i + a == c) ? T(1) : T(0);
+        if (i <= bc) {
+          for (int q = 6 * (i + 1); q < 6 * bc + 6; q++) {
+            const T xq = X[(size_t)q * w + c];
+#pragma unroll
+            for (int a = 0; a < 6; a++) z[a] -= M[(size_t)(6 * i + a) * w + q] * xq;
+          }
         }
+#pragma unroll
         for (int a = 0; a < 6; a++) {
           const T *Dr = M + (size_t)(6 * i + a) * w + 6 * i;
           T v = 0;
+#pragma unroll
           for (int b = 0; b < 6; b++) v += Dr[b] * z[b];
-          X[(size_t)(6 * i + a) * w + c] = v;
+          X[(size_t)(6 * i + a) * w + c] = i <= bc ? v : T(0);
         }
       }
     }
@@ -333,11 +355,21 @@ static int chunk_build_t(Factor &f, const TF *F, cudaStream_t s, long long *laun
   A2DS_CUDA_TRY(cudaMemsetAsync(scr, 0, (size_t)f.cp.scr_size * sizeof(double), s));
   k_chunk_gather<TF><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
                                          f.d_fcols.p, f.d_row_lend.p, f.d_row_ustart.p, F, scr);
-  k_chunk_inverse<double, false><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
+  // small chunks: 64 threads; large ones: a thread per column (6 CHUNK_MAX)
+  const int ns_ = (int)f.cp.small.size(), nb_ = (int)f.cp.big.size();
+  if (ns_) {
+    k_chunk_inverse<double, false><<<ns_, 64, 0, s>>>(f.d_ck_small.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                                       scr, inv);
+    k_chunk_inverse<double, true><<<ns_, 64, 0, s>>>(f.d_ck_small.p, f.d_ck_c0.p, f.d_ck_off.p,
                                                       scr, inv);
-  k_chunk_inverse<double, true><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
-                                                     scr, inv);
-  if (launches) *launches += 3;
+  }
+  if (nb_) {
+    k_chunk_inverse<double, false><<<nb_, 6 * CHUNK_MAX, 0, s>>>(f.d_ck_big.p, f.d_ck_c0.p,
+                                                                 f.d_ck_off.p, scr, inv);
+    k_chunk_inverse<double, true><<<nb_, 6 * CHUNK_MAX, 0, s>>>(f.d_ck_big.p, f.d_ck_c0.p,
+                                                                f.d_ck_off.p, scr, inv);
+  }
+  if (launches) *launches += 1 + 2 * (ns_ > 0) + 2 * (nb_ > 0);
   if (f.precision == 32) {
     const size_t n = (size_t)f.cp.inv_size;
     k_narrow<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(f.cinv32.p, inv, n);
@@ -367,9 +399,8 @@ static void solve_level(const Factor &f, const T *F, const TV *src, TV *y, int l
   const int nrows = L.row_ptr[l + 1] - L.row_ptr[l];
   const int *bound = UPPER ? f.d_row_ustart.p : f.d_row_lend.p;
   if (L.cta[l])
-    k_pull_cta<T, TV, R, UPPER><<<nrows, 256, 0, s>>>(rows, nrows, f.d_frowp.p, bound,
-                                                      f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p,
-                                                      F, src, y);
+    k_pull_cta<T, TV, R, UPPER><<<dim3(nrows, L.split[l]), 256, 0, s>>>(
+        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, src, y);
   else
     k_pull_warp<T, TV, R, UPPER><<<(nrows + 7) / 8, 256, 0, s>>>(
         rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, src, y);
@@ -379,7 +410,7 @@ static void solve_level(const Factor &f, const T *F, const TV *src, TV *y, int l
     // staging for this level's largest chunk; small chunks take 64 threads
     const int mr = L.max_rows[l];
     const size_t smem = (size_t)6 * mr * R * sizeof(TV);
-    k_chunk_apply<T, TV, R, UPPER><<<nch, mr <= 16 ? 64 : 256, smem, s>>>(
+    k_chunk_apply<T, TV, R, UPPER><<<nch, mr <= 16 ? 64 : (mr <= 48 ? 256 : 1024), smem, s>>>(
         (UPPER ? f.d_up_chunks.p : f.d_lo_chunks.p) + L.ch_ptr[l], f.d_ck_c0.p, f.d_ck_off.p,
         chunk_inverses<T>(f), y);
     nl++;
@@ -390,7 +421,11 @@ template <typename T, typename TV, int R>
 static int solve_levels_r(const Factor &f, const T *F, const TV *x, TV *y, cudaStream_t s,
                           long long *launches) {
   long long nl = 0;
-  for (int l = 0; l < f.cp.lo.nlevels; l++) solve_level<T, TV, R, false>(f, F, x, y, l, s, nl);
+  // the lower pulls subtract from y in place (split rows add atomically)
+  if ((const void *)x != (const void *)y)
+    A2DS_CUDA_TRY(cudaMemcpyAsync(y, x, (size_t)f.n * 6 * R * sizeof(TV),
+                                  cudaMemcpyDeviceToDevice, s));
+  for (int l = 0; l < f.cp.lo.nlevels; l++) solve_level<T, TV, R, false>(f, F, y, y, l, s, nl);
   for (int l = 0; l < f.cp.up.nlevels; l++) solve_level<T, TV, R, true>(f, F, y, y, l, s, nl);
   if (launches) *launches += nl;
   A2DS_CUDA_TRY(cudaGetLastError());
