@@ -48,7 +48,8 @@ EXPORTS = [
     "a2ds_bcsr_create", "a2ds_bcsr_destroy", "a2ds_bcsr_get", "a2ds_bcsr_set_values",
     "a2ds_assemble_mat", "a2ds_assemble_mat_ex", "a2ds_assemble_res", "a2ds_assemble_jacobian",
     "a2ds_add_mat_xpt_sens_inner_product", "a2ds_add_adjoint_res_xpt_sens_product",
-    "a2ds_add_mat_dv_sens_inner_product",
+    "a2ds_add_mat_dv_sens_inner_product", "a2ds_newton_preload", "a2ds_preload_buckling",
+    "a2ds_preload_xpt_sens",
     "a2ds_eval_mat_sv_sens_inner_product", "a2ds_eig_sens_xpts",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
     "a2ds_bcsr_time_mult",
@@ -144,6 +145,10 @@ def load(build: bool = False):
     lib.a2ds_eigen_shift_invert.argtypes = [VP, ctypes.POINTER(BucklingOpts), VP, VP, P_D, P_D,
                                             P_D]
     lib.a2ds_eig_sens_thickness.argtypes = [VP, ctypes.c_int, P_D]
+    lib.a2ds_newton_preload.argtypes = [VP, P_D, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int, P_D, P_I, P_D]
+    lib.a2ds_preload_buckling.argtypes = [VP, ctypes.POINTER(BucklingOpts), P_D, P_D, P_D, P_D]
+    lib.a2ds_preload_xpt_sens.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
     lib.a2ds_bcsr_time_mult.argtypes = [VP, ctypes.c_int, ctypes.c_int, P_D]
     lib.a2ds_eig_sens_xpts.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
     lib.a2ds_add_mat_xpt_sens_inner_product.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D,
@@ -544,6 +549,25 @@ class LinearBuckling:
         self.eigvals, self.errors, self.eigvecs = lam, err, vecs
         _check(rc)
         return lam
+
+    def solve_preloaded(self, u, want_vectors=True):
+        """Buckling about the preloaded state u: K_T(u) x + lam G(u) x = 0
+        (a2ds_preload_buckling)."""
+        n, k = self.a.num_nodes, self.opts.num_eigvals
+        uu = _f64(u)
+        lam, err = np.zeros(k), np.zeros(k)
+        vecs = np.zeros((k, n, 6)) if want_vectors else None
+        rc = self.lib.a2ds_preload_buckling(self.a.h, ctypes.byref(self.opts), _d(uu), _d(lam),
+                                            _d(err), _d(vecs))
+        self.eigvals, self.errors, self.eigvecs = lam, err, vecs
+        _check(rc)
+        return lam
+
+    def eval_preload_xpt_sens(self, n, dh=1e-7):
+        """dlambda_n/dX about the preloaded state (a2ds_preload_xpt_sens)."""
+        out = np.zeros((self.a.num_nodes, 3))
+        _check(self.lib.a2ds_preload_xpt_sens(self.a.h, int(n), float(dh), _d(out)))
+        return out
 
     def stats(self):
         out = np.zeros(len(STAT_NAMES))

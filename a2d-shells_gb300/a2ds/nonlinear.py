@@ -8,8 +8,8 @@ TACSAssembler::assembleRes / assembleJacobian (src/TACSAssembler.cpp:4000,
 This module is the driver on top of the GB300 library:
 
 * `newton_preload`: equal load increments s_k = load * k / nsteps; at each,
-  full Newton on R(u) = s_k f with the exact tangent K_T(u) (assembleJacobian)
-  factored on the GPU each step;
+  full Newton on R(u) = s_k f with the exact tangent K_T(u) factored on the
+  GPU each step (the C ABI's a2ds_newton_preload);
 * `preload_buckling`: the eigenproblem K_T(u) x + lam G(u) x = 0 about the
   converged preload u, with G(u) the geometric stiffness along u (stated
   definition), solved by the library's shift-invert Lanczos;
@@ -36,38 +36,24 @@ def _bc_mask_vector(assembler: capi.Assembler, bc_nodes, bc_mask):
     return fixed
 
 
-def newton_preload(assembler: capi.Assembler, rhs, bc_nodes, bc_mask, load: float,
+def newton_preload(assembler: capi.Assembler, rhs, bc_nodes=None, bc_mask=None, load: float = 1.0,
                    nsteps: int = 10, rtol: float = 1e-10, max_newton: int = 25,
                    precision: int = 64):
     """Newton load stepping to `load` times the nodal load vector `rhs`
-    (node-major num_nodes x 6).  Returns (u, iterations per step, final
-    relative residual).  Raises RuntimeError if a step does not converge."""
-    f = np.asarray(rhs, float).reshape(-1, 6).copy()
-    fixed = _bc_mask_vector(assembler, bc_nodes, bc_mask)
-    f[fixed] = 0.0
+    (node-major num_nodes x 6) on the GPU (a2ds_newton_preload; the
+    Dirichlet set is the assembler's, bc_nodes / bc_mask are accepted for
+    the caller's bookkeeping only).  Returns (u, iterations per step, final
+    relative residual).  Raises A2dsError (A2DS_ERR_NOCONV) if a step does
+    not converge."""
+    import ctypes
+    f = capi._f64(np.asarray(rhs, float).reshape(-1, 6))
     u = np.zeros_like(f)
-    KT = assembler.create_mat()
-    pc = None
-    its = []
-    rel = 0.0
-    for k in range(1, nsteps + 1):
-        fk = load * k / nsteps * f
-        fn = max(np.linalg.norm(fk), 1e-300)
-        for it in range(max_newton + 1):
-            res = assembler.assemble_jacobian(KT, u)  # R(u); Dirichlet rows u - u_bc
-            r = res - fk
-            rel = np.linalg.norm(r) / fn
-            if rel <= rtol:
-                its.append(it)
-                break
-            if it == max_newton:
-                raise RuntimeError(f"Newton did not converge in load step {k}: "
-                                   f"relative residual {rel:.3e}")
-            if pc is None:
-                pc = capi.SchurPc(KT, 1000000, precision)
-            pc.factor(KT)
-            u = u - pc.apply_factor(r)
-    return u, its, rel
+    its = np.zeros(nsteps, np.int32)
+    rel = ctypes.c_double()
+    capi._check(assembler.lib.a2ds_newton_preload(
+        assembler.h, capi._d(f), float(load), int(nsteps), float(rtol), int(max_newton),
+        int(precision), capi._d(u), capi._i(its), ctypes.byref(rel)))
+    return u, its.tolist(), rel.value
 
 
 def preload_buckling(assembler: capi.Assembler, u, sigma: float, num_eigvals: int = 5,

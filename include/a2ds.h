@@ -365,6 +365,44 @@ int a2ds_eigen_shift_invert(a2ds_mesh mesh, const a2ds_buckling_opts *opts, a2ds
    steps and restart cycles of the GMRES-IR solves with FP32 factors). */
 int a2ds_buckling_stats(a2ds_mesh mesh, int n, double *out);
 
+/* ------------------------------------------------ nonlinear preload
+   The reference has the building blocks of buckling about a nonlinear
+   preloaded state -- TACSAssembler::assembleRes / assembleJacobian
+   (src/TACSAssembler.cpp:4000, 4084), TACSSchurPc and the nonlinear shell
+   elements (TACSQuad{4,9}NonlinearShell, src/elements/shell/
+   TACSShellElementDefs.h:27-33) -- but no driver (its continuation and
+   integrator classes are not built).  These entries are that driver.
+
+   Newton load stepping: equal increments s_k = load k / nsteps of the
+   nodal load vector rhs (num_nodes x 6; Dirichlet entries ignored), at each
+   full Newton on R(u) = s_k rhs with the exact tangent K_T(u) (complete LU
+   in `precision` 64, 48 or 32 on the GPU, FP64 GMRES-IR solves to 1e-12)
+   until ||R(u) - s_k rhs|| <= rtol ||s_k rhs|| (Dirichlet rows u - u_bc).
+   u_out: num_nodes x 6; iters: nsteps values (Newton steps per increment,
+   may be NULL); *rel_out: the final relative residual (may be NULL).
+   A2DS_ERR_NOCONV if an increment needs more than max_newton steps. */
+int a2ds_newton_preload(a2ds_mesh mesh, const double *rhs, double load, int nsteps, double rtol,
+                        int max_newton, int precision, double *u_out, int *iters,
+                        double *rel_out);
+
+/* Buckling about the preloaded state u (num_nodes x 6): the num_eigvals
+   smallest-magnitude lambda of K_T(u) x + lambda G(u) x = 0, G(u) the
+   geometric stiffness along u, by the same block shift-invert Lanczos as
+   a2ds_buckling_solve (EPBucklingShiftInvert + SEP::solve,
+   src/bpmat/GSEP.cpp:200-244, 485-596).  Outputs as a2ds_buckling_solve. */
+int a2ds_preload_buckling(a2ds_mesh mesh, const a2ds_buckling_opts *opts, const double *u,
+                          double *eigvals, double *errors, double *eigvecs);
+
+/* dlambda_n/dX (num_nodes x 3) of a2ds_preload_buckling's n-th load, the
+   formula of the reference's (commented) evalEigenXptSens
+   (src/TACSBuckling.cpp:457-497) with the preload's Newton system:
+     dlambda/dX = -[phi^T K_T' phi + lambda phi^T G' phi - psi^T R'] / phi^T G phi,
+     K_T(u) psi = d/du [phi^T (K_T(u) + lambda G(u)) phi],
+   ' = d/dX at fixed u (R' the residual's coordinate derivative at fixed
+   loads); element derivatives by central differences with step dh (0 =
+   1e-7), element states recomputed from u and X on the GPU. */
+int a2ds_preload_xpt_sens(a2ds_mesh mesh, int n, double dh, double *dlam_dX);
+
 /* ---------------------------------------------- eigenvalue sensitivities
    The derivative of buckling load lambda_n with respect to each thickness
    group, dlambda/dt_g = -phi^T (dK/dt_g + lambda dG/dt_g) phi / (phi^T G phi)

@@ -41,8 +41,10 @@
 namespace a2ds_tacs {
 
 typedef double TacsScalar;
+#ifndef MPI_COMM_WORLD
 typedef int MPI_Comm;  // single process: the communicator argument is ignored
 static const MPI_Comm MPI_COMM_WORLD = 0;
+#endif
 
 enum ElementMatrixType {
   TACS_STIFFNESS_MATRIX = A2DS_STIFFNESS_MATRIX,
@@ -233,14 +235,108 @@ inline TacsScalar TACSBVec::norm() const {
 class TACSAssembler;
 
 /* ------------------------------------------------------------- matrices */
+// BCSRMat (src/bpmat/BCSRMat.h:34-204) on one process, 6x6 blocks, rows in
+// the assembler's matrix ordering.  Two kinds, as in the reference: a view
+// of an assembled matrix (TACSSchurMat::getBCSRMat), and a factor built as
+// BCSRMat(comm, A, levFill, fill) (the ILU(levFill) pattern of A; copyValues
+// then factor, applyFactor).  Raw vectors (mult, applyFactor) are in the
+// row ordering, 6 values per row, as the reference's BCSRMat takes them.
+class BCSRMat : public TACSObject {
+ public:
+  // a view of an a2ds_bcsr (the handle stays owned by its TACSSchurMat)
+  BCSRMat(a2ds_mesh mesh, a2ds_bcsr A) : mesh_(mesh), A_(A) {}
+  // BCSRMat(comm, A, levFill, fill): the factor object of A's pattern
+  BCSRMat(MPI_Comm, BCSRMat *A, int levFill, double fill)
+      : mesh_(A->mesh_), A_(A->A_), factor_(true) {
+    (void)fill;
+    a2ds_report("BCSRMat", a2ds_pc_create(A_, levFill, 64, &pc_));
+  }
+  ~BCSRMat() {
+    if (pc_) a2ds_pc_destroy(pc_);
+  }
+  // getArrays(&bsize, &nrows, &ncols, &rowp, &cols, &A): host copies kept
+  // by this object until the next call
+  void getArrays(int *bsize, int *nrows, int *ncols, const int **rowp, const int **cols,
+                 TacsScalar **A) {
+    int n = 0, nz = 0;
+    int rc = factor_ ? a2ds_pc_get(pc_, &n, &nz, nullptr, nullptr, nullptr)
+                     : a2ds_bcsr_get(A_, &n, &nz, nullptr, nullptr, nullptr);
+    rowp_.assign(n + 1, 0);
+    cols_.assign(nz, 0);
+    vals_.assign((size_t)nz * 36, 0.0);
+    if (!rc)
+      rc = factor_ ? a2ds_pc_get(pc_, nullptr, nullptr, rowp_.data(), cols_.data(), vals_.data())
+                   : a2ds_bcsr_get(A_, nullptr, nullptr, rowp_.data(), cols_.data(),
+                                   vals_.data());
+    a2ds_report("BCSRMat::getArrays", rc);
+    if (bsize) *bsize = 6;
+    if (nrows) *nrows = n;
+    if (ncols) *ncols = n;
+    if (rowp) *rowp = rowp_.data();
+    if (cols) *cols = cols_.data();
+    if (A) *A = vals_.data();
+  }
+  // y = A x (BCSRMatVecMult6)
+  void mult(TacsScalar *x, TacsScalar *y) {
+    a2ds_report("BCSRMat::mult", a2ds_bcsr_mult_rows(A_, x, y));
+  }
+  // factor object: the values to factor next (BCSRMat::copyValues)
+  void copyValues(BCSRMat *B) { from_ = B->A_; }
+  // BCSRMatFactor6 of the copied values (the matrix it was built from if none)
+  int factor() {
+    if (!factor_) return a2ds_report("BCSRMat::factor", A2DS_ERR_STATE);
+    return a2ds_report("BCSRMat::factor", a2ds_pc_factor(pc_, from_));
+  }
+  // y = (LU)^-1 x, BCSRMatApplyLower6 / Upper6 on row-ordered vectors
+  void applyFactor(TacsScalar *x, TacsScalar *y) {
+    if (!factor_) {
+      a2ds_report("BCSRMat::applyFactor", A2DS_ERR_STATE);
+      return;
+    }
+    int n = 0;
+    a2ds_bcsr_get(A_, &n, nullptr, nullptr, nullptr, nullptr);
+    std::vector<int> perm(n);
+    a2ds_mesh_get_ordering(mesh_, perm.data());
+    std::vector<double> xn((size_t)n * 6), yn((size_t)n * 6);
+    for (int r = 0; r < n; r++)
+      for (int k = 0; k < 6; k++) xn[(size_t)perm[r] * 6 + k] = x[(size_t)r * 6 + k];
+    a2ds_report("BCSRMat::applyFactor", a2ds_pc_apply(pc_, xn.data(), yn.data()));
+    for (int r = 0; r < n; r++)
+      for (int k = 0; k < 6; k++) y[(size_t)r * 6 + k] = yn[(size_t)perm[r] * 6 + k];
+  }
+  a2ds_bcsr handle() const { return A_; }
+
+ private:
+  a2ds_mesh mesh_;
+  a2ds_bcsr A_;
+  a2ds_bcsr from_ = nullptr;
+  a2ds_pc pc_ = nullptr;
+  bool factor_ = false;
+  std::vector<int> rowp_, cols_;
+  std::vector<double> vals_;
+};
+
 class TACSMat : public TACSObject {};
 class TACSSchurMat : public TACSMat {
  public:
   explicit TACSSchurMat(TACSAssembler *assembler);
   ~TACSSchurMat() {
+    if (B_) B_->decref();
     if (h_) a2ds_bcsr_destroy(h_);
   }
   a2ds_bcsr handle() const { return h_; }
+  // TACSSchurMat::getBCSRMat(&B, &E, &F, &C): on one process B is the whole
+  // matrix and E, F, C are empty (NULL here)
+  void getBCSRMat(BCSRMat **B, BCSRMat **E, BCSRMat **F, BCSRMat **C) {
+    if (!B_) {
+      B_ = new BCSRMat(mesh_, h_);
+      B_->incref();
+    }
+    if (B) *B = B_;
+    if (E) *E = nullptr;
+    if (F) *F = nullptr;
+    if (C) *C = nullptr;
+  }
   // BCSRMat::mult through TACSSchurMat::mult, node-major vectors
   void mult(TACSBVec *x, TACSBVec *y) {
     a2ds_report("TACSSchurMat::mult",
@@ -256,6 +352,8 @@ class TACSSchurMat : public TACSMat {
 
  private:
   a2ds_bcsr h_ = nullptr;
+  a2ds_mesh mesh_ = nullptr;
+  BCSRMat *B_ = nullptr;
 };
 
 /* ------------------------------------------------- preconditioner, KSM */
@@ -360,26 +458,63 @@ class TACSAssembler : public TACSObject {
     MULTICOLOR_ORDER = A2DS_MULTICOLOR_ORDER
   };
 
+  // TACSAssembler(comm, varsPerNode, numOwnedNodes, numElements,
+  // numDependentNodes) (src/TACSAssembler.h:81), then setElementConnectivity,
+  // setElements and setNodes as the reference's drivers call them; the
+  // device mesh is created when all three are given (at the latest by
+  // initialize).  One process: 6 variables per node, no dependent nodes.
+  TACSAssembler(MPI_Comm, int varsPerNode, int numOwnedNodes, int numElements,
+                int numDependentNodes = 0)
+      : nn_(numOwnedNodes), ne_(numElements), npe_(0), vars_((size_t)numOwnedNodes * 6, 0.0) {
+    if (varsPerNode != 6 || numDependentNodes != 0) {
+      fprintf(stderr, "TACSAssembler: 6 variables per node and no dependent nodes\n");
+      fail_ = A2DS_ERR_ARG;
+    }
+  }
   // Mesh with one element object per element (elems[e], shared objects
   // allowed), node-major X, tensor-order connectivity, 0-based component
-  // ids (for .f5 output; may be NULL).
+  // ids (for .f5 output; may be NULL): the sequence above in one call.
   TACSAssembler(int num_nodes, int num_elements, int nodes_per_elem, const int *conn,
                 const double *X, TACSElement *const *elems, const int *elem_component)
-      : nn_(num_nodes), ne_(num_elements), npe_(nodes_per_elem), vars_(num_nodes * 6, 0.0),
+      : nn_(num_nodes), ne_(num_elements), npe_(nodes_per_elem),
+        conn_(conn, conn + (size_t)num_elements * nodes_per_elem), vars_(num_nodes * 6, 0.0),
         comp_(elem_component ? elem_component : nullptr,
               elem_component ? elem_component + num_elements : nullptr),
         X_(X, X + (size_t)num_nodes * 3) {
     elems_.assign(elems, elems + num_elements);
     for (TACSElement *e : elems_) e->incref();
-    int nl = elems_.empty() ? 0 : elems_[0]->nonlinear();
-    fail_ = a2ds_report("TACSAssembler",
-                        a2ds_mesh_create(num_nodes, num_elements, nodes_per_elem, conn, X, nl,
-                                         &mesh_));
-    if (!fail_) fail_ = set_material_and_thickness();
+    fail_ = create_mesh();
   }
   ~TACSAssembler() {
     for (TACSElement *e : elems_) e->decref();
     if (mesh_) a2ds_mesh_destroy(mesh_);
+  }
+  // setElementConnectivity(ptr, conn) (TACSAssembler.h:88): ptr[e+1] -
+  // ptr[e] nodes per element, all 4 (Quad4) or all 9 (Quad9)
+  int setElementConnectivity(const int *ptr, const int *conn) {
+    if (mesh_) return a2ds_report("TACSAssembler::setElementConnectivity", A2DS_ERR_STATE);
+    const int npe = ne_ > 0 ? ptr[1] - ptr[0] : 0;
+    for (int e = 0; e < ne_; e++)
+      if (ptr[e + 1] - ptr[e] != npe || (npe != 4 && npe != 9))
+        return a2ds_report("TACSAssembler::setElementConnectivity", A2DS_ERR_ARG);
+    npe_ = npe;
+    conn_.assign(conn + ptr[0], conn + ptr[ne_]);
+    return maybe_create();
+  }
+  // setElements(elements) (TACSAssembler.h:90)
+  int setElements(TACSElement **elements) {
+    if (mesh_) return a2ds_report("TACSAssembler::setElements", A2DS_ERR_STATE);
+    for (TACSElement *e : elems_) e->decref();
+    elems_.assign(elements, elements + ne_);
+    for (TACSElement *e : elems_) e->incref();
+    return maybe_create();
+  }
+  // setNodes(X) (TACSAssembler.h:156): node-major coordinates, before the
+  // mesh exists (the device mesh keeps its coordinates)
+  int setNodes(TACSBVec *X) {
+    if (mesh_) return a2ds_report("TACSAssembler::setNodes", A2DS_ERR_STATE);
+    X_ = X->values();
+    return maybe_create();
   }
   int getNumNodes() const { return nn_; }
   int getNumElements() const { return ne_; }
@@ -404,15 +539,23 @@ class TACSAssembler : public TACSObject {
           }
       }
     }
-    return a2ds_report("TACSAssembler::addBCs",
-                       a2ds_mesh_add_bcs(mesh_, nnodes, nodes, masks.data(), v6.data()));
+    return addBCsMasked(nnodes, nodes, masks.data(), v6.data());
   }
-  // one a2ds_mesh_add_bcs entry per (node, mask, values): the loader's form
+  // one a2ds_mesh_add_bcs entry per (node, mask, values): the loader's form;
+  // kept until the device mesh exists
   int addBCsMasked(int n, const int *nodes, const int *masks, const double *vals6) {
+    if (!mesh_) {
+      bc_nodes_.insert(bc_nodes_.end(), nodes, nodes + n);
+      bc_masks_.insert(bc_masks_.end(), masks, masks + n);
+      bc_vals_.insert(bc_vals_.end(), vals6, vals6 + (size_t)n * 6);
+      return 0;
+    }
     return a2ds_report("TACSAssembler::addBCs", a2ds_mesh_add_bcs(mesh_, n, nodes, masks, vals6));
   }
   int initialize(OrderingType order = TACS_AMD_ORDER) {
     if (initialized_) return 0;
+    if (fail_) return fail_;
+    if (!mesh_ && (fail_ = create_mesh())) return fail_;
     int rc = a2ds_report("TACSAssembler::initialize", a2ds_mesh_initialize(mesh_, (int)order));
     if (!rc) initialized_ = true;
     return rc;
@@ -454,18 +597,28 @@ class TACSAssembler : public TACSObject {
     if (!rc) rc = a2ds_assemble_res(mesh_, vars_.data(), res->values().data());
     return a2ds_report("TACSAssembler::assembleRes", rc);
   }
-  // assembleJacobian(1, 0, 0, res, A): the tangent and residual at the
-  // current variables
+  // assembleJacobian(alpha, beta, gamma, res, A, matOr, lambda)
+  // (TACSAssembler.cpp:4084): res = R(u) and A = alpha dR/du at the current
+  // variables, Dirichlet rows the identity.  The static shell path has no
+  // velocity or acceleration variables, so beta and gamma (damping and
+  // mass terms) must be 0; lambda scales auxiliary element loads, of which
+  // this path has none; matOr: the normal orientation only.
   int assembleJacobian(TacsScalar alpha, TacsScalar beta, TacsScalar gamma, TACSBVec *res,
-                       TACSMat *A) {
-    if (alpha != 1.0 || beta != 0.0 || gamma != 0.0) {
-      fprintf(stderr, "TACSAssembler::assembleJacobian: only alpha = 1, beta = gamma = 0\n");
+                       TACSMat *A, int matOr = 0, TacsScalar lambda = 1.0) {
+    (void)lambda;
+    if (beta != 0.0 || gamma != 0.0 || matOr != 0) {
+      fprintf(stderr, "TACSAssembler::assembleJacobian: beta = gamma = 0 and the normal "
+                      "orientation only (static shells)\n");
       return A2DS_ERR_ARG;
     }
     int rc = sync_temperature();
+    a2ds_bcsr h = mat_handle(A);
     if (!rc)
-      rc = a2ds_assemble_jacobian(mesh_, vars_.data(), res ? res->values().data() : nullptr,
-                                  mat_handle(A));
+      rc = a2ds_assemble_jacobian(mesh_, vars_.data(), res ? res->values().data() : nullptr, h);
+    if (!rc && alpha != 1.0) {
+      rc = a2ds_bcsr_axpy(h, alpha - 1.0, h);     // A <- alpha A
+      if (!rc) rc = a2ds_bcsr_apply_bcs(h);         // identity Dirichlet rows again
+    }
     return a2ds_report("TACSAssembler::assembleJacobian", rc);
   }
 
@@ -511,8 +664,36 @@ class TACSAssembler : public TACSObject {
     return a2ds_report("TACSAssembler", rc);
   }
 
+  int maybe_create() {
+    if (fail_) return fail_;
+    if (npe_ && !elems_.empty() && X_.size() == (size_t)nn_ * 3) fail_ = create_mesh();
+    return fail_;
+  }
+  int create_mesh() {
+    if (mesh_) return 0;
+    if (!npe_ || elems_.size() != (size_t)ne_ || X_.size() != (size_t)nn_ * 3) {
+      fprintf(stderr, "TACSAssembler: connectivity, elements and nodes must all be set\n");
+      return A2DS_ERR_STATE;
+    }
+    const int nl = elems_[0]->nonlinear();
+    int rc = a2ds_report("TACSAssembler",
+                         a2ds_mesh_create(nn_, ne_, npe_, conn_.data(), X_.data(), nl, &mesh_));
+    if (!rc) rc = set_material_and_thickness();
+    if (!rc && !bc_nodes_.empty()) {
+      rc = a2ds_report("TACSAssembler::addBCs",
+                       a2ds_mesh_add_bcs(mesh_, (int)bc_nodes_.size(), bc_nodes_.data(),
+                                         bc_masks_.data(), bc_vals_.data()));
+      bc_nodes_.clear();
+      bc_masks_.clear();
+      bc_vals_.clear();
+    }
+    return rc;
+  }
+
   int nn_, ne_, npe_;
   a2ds_mesh mesh_ = nullptr;
+  std::vector<int> conn_, bc_nodes_, bc_masks_;
+  std::vector<double> bc_vals_;
   int fail_ = 0;
   bool initialized_ = false;
   double temperature_ = 0.0;
@@ -523,7 +704,7 @@ class TACSAssembler : public TACSObject {
   std::vector<TACSShellConstitutive *> cons_;
 };
 
-inline TACSSchurMat::TACSSchurMat(TACSAssembler *assembler) {
+inline TACSSchurMat::TACSSchurMat(TACSAssembler *assembler) : mesh_(assembler->handle()) {
   a2ds_report("TACSSchurMat", a2ds_bcsr_create(assembler->handle(), &h_));
 }
 
@@ -541,9 +722,9 @@ class TACSLinearBuckling : public TACSObject {
       : assembler_(nullptr) {
     GMRES *solver = dynamic_cast<GMRES *>(ksm);
     a2ds_hold(assembler_, assembler);
-    (void)gmat;
-    (void)kmat;
-    (void)aux_mat;
+    a2ds_hold(gmat_, dynamic_cast<TACSSchurMat *>(gmat));
+    a2ds_hold(kmat_, dynamic_cast<TACSSchurMat *>(kmat));
+    a2ds_hold(aux_, dynamic_cast<TACSSchurMat *>(aux_mat));
     a2ds_buckling_default_opts(&opts_);
     opts_.sigma = sigma;
     opts_.max_lanczos = max_lanczos;
@@ -562,6 +743,9 @@ class TACSLinearBuckling : public TACSObject {
   }
   ~TACSLinearBuckling() {
     if (assembler_) assembler_->decref();
+    if (gmat_) gmat_->decref();
+    if (kmat_) kmat_->decref();
+    if (aux_) aux_->decref();
   }
   // GB300 settings without a counterpart in the reference
   void setBlockSize(int p) { opts_.block_size = p; }
@@ -582,10 +766,48 @@ class TACSLinearBuckling : public TACSObject {
     vecs_.assign((size_t)n * nn * 6, 0.0);
     path_.assign((size_t)nn * 6, 0.0);
     TACSBVec *f = dynamic_cast<TACSBVec *>(rhs);
-    return a2ds_report("TACSLinearBuckling::solve",
-                       a2ds_buckling_solve(assembler_->handle(), &opts_,
-                                           f ? f->values().data() : nullptr, eig_.data(),
-                                           err_.data(), vecs_.data(), path_.data()));
+    rc = a2ds_buckling_solve(assembler_->handle(), &opts_, f ? f->values().data() : nullptr,
+                             eig_.data(), err_.data(), vecs_.data(), path_.data());
+    // as the reference leaves them: kmat = K at the zero state, gmat = G
+    // along the load path, aux_mat = K + sigma G (Dirichlet rows applied);
+    // the assembler's variables hold the path
+    a2ds_mesh h = assembler_->handle();
+    if ((!rc || rc == A2DS_ERR_NOCONV) && kmat_)
+      rc = keep_rc(rc, a2ds_assemble_mat(h, A2DS_STIFFNESS_MATRIX, nullptr, kmat_->handle()));
+    if ((!rc || rc == A2DS_ERR_NOCONV) && gmat_)
+      rc = keep_rc(rc, a2ds_assemble_mat(h, A2DS_GEOMETRIC_STIFFNESS_MATRIX, path_.data(),
+                                         gmat_->handle()));
+    if ((!rc || rc == A2DS_ERR_NOCONV) && aux_ && kmat_ && gmat_) {
+      rc = keep_rc(rc, a2ds_bcsr_copy(aux_->handle(), kmat_->handle()));
+      rc = keep_rc(rc, a2ds_bcsr_axpy(aux_->handle(), opts_.sigma, gmat_->handle()));
+      rc = keep_rc(rc, a2ds_bcsr_apply_bcs(aux_->handle()));
+    }
+    TACSBVec path(assembler_->getNumNodes(), 6);
+    path.values() = path_;
+    assembler_->setVariables(&path);
+    return a2ds_report("TACSLinearBuckling::solve", rc);
+  }
+  // checkEigenvector(n) (src/TACSBuckling.cpp:310-349): prints ||K e||,
+  // ||G e|| and ||K e + lambda G e|| with the kmat and gmat of the last
+  // solve (given to the constructor); returns the relative residual
+  // ||K e + lambda G e|| / ||K e|| (the reference returns nothing)
+  double checkEigenvector(int n) {
+    if (!kmat_ || !gmat_ || n < 0 || n >= (int)eig_.size()) {
+      fprintf(stderr, "TACSLinearBuckling::checkEigenvector: needs kmat, gmat and a solve\n");
+      return -1.0;
+    }
+    const int nn = assembler_->getNumNodes();
+    TACSBVec e(nn, 6), t1(nn, 6), t2(nn, 6);
+    TacsScalar err = 0.0;
+    TacsScalar eig = extractEigenvector(n, &e, &err);
+    kmat_->mult(&e, &t1);
+    gmat_->mult(&e, &t2);
+    const double t1n = t1.norm(), t2n = t2.norm();
+    printf("|K*e| = %15.5e  \n|G*e| = %15.5e \n", t1n, t2n);
+    t1.axpy(eig, &t2);
+    const double rn = t1.norm();
+    printf("||K*e + lambda*G*e|| = %15.5e \n", rn);
+    return t1n > 0.0 ? rn / t1n : rn;
   }
   TacsScalar extractEigenvalue(int n, TacsScalar *error) {
     if (n < 0 || n >= (int)eig_.size()) return 0.0;
@@ -613,7 +835,9 @@ class TACSLinearBuckling : public TACSObject {
   }
 
  private:
+  static int keep_rc(int rc, int next) { return rc ? rc : next; }
   TACSAssembler *assembler_;
+  TACSSchurMat *gmat_ = nullptr, *kmat_ = nullptr, *aux_ = nullptr;
   a2ds_buckling_opts opts_;
   std::vector<double> eig_, err_, vecs_, path_;
 };

@@ -104,3 +104,38 @@ def test_preload_buckling_xpt_sensitivity_vs_finite_difference():
         ds = float(np.sum(dX * modes[p]))
         fd = (solve(m.X + eps * modes[p])[2][0] - solve(m.X - eps * modes[p])[2][0]) / (2 * eps)
         assert abs(ds - fd) <= 1e-4 * abs(fd), (p, ds, fd)
+
+
+@pytest.mark.gpu
+def test_preload_c_entries_match_composition():
+    """The C ABI's preload entries (a2ds_preload_buckling and
+    a2ds_preload_xpt_sens, reachable from C++ callers) against the same
+    formula composed from the element-level entries in a2ds.nonlinear."""
+    m = meshgen.cylinder(8, 16)
+    t = m.meta["t"]
+    a = capi.Assembler(m.X, m.conn, nonlinear=True)
+    a.set_material(m.E, m.nu)
+    a.set_thickness([t])
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    load = 0.3 * meshgen.classical_cylinder_load(m.E, m.nu, t, 1.0)
+    u, its, rel = nonlinear.newton_preload(a, m.rhs, load=load, nsteps=4, rtol=1e-11)
+    assert rel <= 1e-11 and len(its) == 4
+    from test_gpu_solve import dense_buckling
+    KT, G = a.create_mat(), a.create_mat()
+    a.assemble_jacobian(KT, u, want_res=False)
+    a.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, u)
+    sigma = 0.95 * dense_buckling(KT.to_dense_nodes(), G.to_dense_nodes(), m.bc_nodes,
+                                  m.bc_mask)[0]
+    lam_p, b_p, KT, G = nonlinear.preload_buckling(a, u, sigma, num_eigvals=2, eig_tol=1e-12,
+                                                   block_size=2)
+    dX_p = nonlinear.preload_xpt_sens(a, u, lam_p[0], b_p.eigvecs[0], KT, G)
+    b = capi.LinearBuckling(a, sigma, max_lanczos=120, num_eigvals=2, eig_tol=1e-12,
+                            block_size=2)
+    lam = b.solve_preloaded(u)
+    assert np.max(np.abs(lam - lam_p) / np.abs(lam_p)) < 1e-10, (lam, lam_p)
+    dX = b.eval_preload_xpt_sens(0)
+    assert np.abs(dX - dX_p).max() <= 1e-6 * np.abs(dX_p).max()
+    # the linear-path sensitivity entries refuse the preloaded state
+    with pytest.raises(capi.A2dsError):
+        b.eig_sens_thickness(0, 1)
