@@ -84,11 +84,53 @@ __global__ void __launch_bounds__(256) k_bcsr_spmv(int nrows, const int *__restr
   }
 }
 
+// FP64 form of the same mapping with 16-byte loads: lane (g, i) reads row
+// i of a block as three double2 (a block row of 48 bytes, 16-byte aligned
+// since blocks are 288 bytes) and the six x entries as three double2; the
+// row's column indices are read once by the warp (lane l holds column
+// start + l) and handed to the groups by shuffles, so no group waits on an
+// index load before its gather.  Two passes cover the usual 6-10 block rows
+// of Quad4 meshes.
+__global__ void __launch_bounds__(256) k_bcsr_spmv_f64(int nrows, const int *__restrict__ rowp,
+                                                       const int *__restrict__ cols,
+                                                       const double *__restrict__ vals,
+                                                       const double *__restrict__ x,
+                                                       double *__restrict__ y) {
+  __shared__ double part[8][32];
+  const int wib = threadIdx.x >> 5;
+  const int row = blockIdx.x * 8 + wib;
+  const int lane = threadIdx.x & 31;
+  if (row >= nrows) return;  // whole warp
+  const int g = lane / 6, i = lane - 6 * g;
+  const int start = rowp[row], end = rowp[row + 1];
+  double acc = 0.0;
+  for (int base = start; base < end; base += 32) {
+    const int myc = base + lane < end ? cols[base + lane] : 0;
+    const int nb = min(32, end - base);
+    for (int k = 0; k < nb; k += 5) {
+      const int slot = k + g;  // this group's block, if any
+      const int c = __shfl_sync(0xffffffffu, myc, slot < 32 ? slot : 0);
+      if (lane < 30 && slot < nb) {
+        const double2 *a = reinterpret_cast<const double2 *>(vals + (size_t)(base + slot) * 36 + 6 * i);
+        const double2 *xv = reinterpret_cast<const double2 *>(x + (size_t)c * 6);
+        const double2 a0 = a[0], a1 = a[1], a2 = a[2];
+        const double2 x0 = __ldg(xv), x1 = __ldg(xv + 1), x2 = __ldg(xv + 2);
+        acc += a0.x * x0.x + a0.y * x0.y + a1.x * x1.x + a1.y * x1.y + a2.x * x2.x + a2.y * x2.y;
+      }
+    }
+  }
+  part[wib][lane] = lane < 30 ? acc : 0.0;
+  __syncwarp();
+  if (lane < 6)
+    y[(size_t)row * 6 + lane] = part[wib][lane] + part[wib][lane + 6] + part[wib][lane + 12] +
+                                part[wib][lane + 18] + part[wib][lane + 24];
+}
+
 int launch_spmv_f64(int nrows, const int *rowp, const int *cols, const double *vals,
                     const double *x, double *y, cudaStream_t s) {
   if (nrows <= 0) return 0;
   int blocks = (nrows * 32 + 255) / 256;
-  k_bcsr_spmv<double, double><<<blocks, 256, 0, s>>>(nrows, rowp, cols, vals, x, y);
+  k_bcsr_spmv_f64<<<blocks, 256, 0, s>>>(nrows, rowp, cols, vals, x, y);
   A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
 }
