@@ -180,6 +180,50 @@ int blk_sub(double *W, const double *Q, int nb, size_t bstride, const double *H,
   return 0;
 }
 
+// Y_o = sum_b Q_b C_{b,o} for the output blocks o < nout (n6 x p each, at
+// Y + o ostride): Y_o[i][c2] = sum_{b, c1} Q_b[i][c1] C[(b p + c1) (nout p)
+// + o p + c2]; C staged in shared memory, one thread per (i, c2).
+__global__ void __launch_bounds__(256) k_blk_mul(const double *__restrict__ Q, int nb,
+                                                 size_t bstride, const double *__restrict__ C,
+                                                 int nout, size_t ostride, size_t n6, int p,
+                                                 double *__restrict__ Y) {
+  extern __shared__ double sC[];
+  const int ld = nout * p, nc = nb * p * ld;
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) sC[k] = C[k];
+  __syncthreads();
+  const size_t total = n6 * p;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = t / p;
+    const int c2 = (int)(t - i * p);
+    for (int o = 0; o < nout; o++) {
+      double acc = 0.0;
+      for (int b = 0; b < nb; b++) {
+        const double *q = Q + (size_t)b * bstride + i * p;
+        const double *c = sC + (size_t)(b * p) * ld + o * p + c2;
+        for (int c1 = 0; c1 < p; c1++) acc += q[c1] * c[(size_t)c1 * ld];
+      }
+      Y[(size_t)o * ostride + t] = acc;
+    }
+  }
+}
+
+int blk_mul(const double *Q, int nb, size_t bstride, const double *C, int nout, size_t ostride,
+            size_t n6, int p, double *Y, cudaStream_t s) {
+  const size_t smem = (size_t)nb * p * nout * p * sizeof(double);
+  if (nb < 1 || nout < 1) return 0;
+  if (smem > 200 * 1024) return fail(A2DS_ERR_ARG, "blk_mul: coefficient table too large");
+  static bool configured = false;
+  if (!configured) {
+    A2DS_CUDA_TRY(cudaFuncSetAttribute(k_blk_mul, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       200 * 1024));
+    configured = true;
+  }
+  k_blk_mul<<<grid_for(n6 * p), 256, smem, s>>>(Q, nb, bstride, C, nout, ostride, n6, p, Y);
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 // X <- X M (M p x p), one thread per row.
 template <int P>
 __global__ void k_blk_rmul(double *__restrict__ X, const double *__restrict__ M, size_t n6) {
@@ -335,14 +379,20 @@ int col_axpy(double *W, const double *Q, int nb, size_t bstride, const double *h
 }
 
 // W[i][c] /= sqrt(nrm2[c]) (columns with nrm2[c] == 0 are left as they are).
+// (The p scale factors are formed once per CTA: FP64 square roots and
+// divisions per element would bound the kernel by the FP64 pipe.)
 __global__ void k_col_unit(double *__restrict__ W, const double *__restrict__ nrm2, size_t n6,
                            int p) {
+  __shared__ double sc[16];
+  if (threadIdx.x < p) {
+    const double q = nrm2[threadIdx.x];
+    sc[threadIdx.x] = q > 0.0 ? 1.0 / sqrt(q) : 1.0;
+  }
+  __syncthreads();
   const size_t total = n6 * p;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const double q = nrm2[e & (size_t)(p - 1)];
-    if (q > 0.0) W[e] /= sqrt(q);
-  }
+       e += (size_t)gridDim.x * blockDim.x)
+    W[e] *= sc[e & (size_t)(p - 1)];
 }
 
 int col_unit(double *W, const double *nrm2, size_t n6, int p, cudaStream_t s) {

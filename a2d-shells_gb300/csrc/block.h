@@ -19,6 +19,10 @@ int blk_dots(const double *Q, int nb, size_t bstride, const double *W, size_t n6
 // W -= sum_b Q_b H[b] (H on the device).
 int blk_sub(double *W, const double *Q, int nb, size_t bstride, const double *H, size_t n6, int p,
             cudaStream_t s);
+// Y_o = sum_b Q_b C_{b,o} for o < nout (each n6 x p, at Y + o ostride):
+// Y_o[i][c2] = sum_{b, c1} Q_b[i][c1] C[(b p + c1) (nout p) + o p + c2].
+int blk_mul(const double *Q, int nb, size_t bstride, const double *C, int nout, size_t ostride,
+            size_t n6, int p, double *Y, cudaStream_t s);
 // X <- X M, M p x p row-major on the device.
 int blk_rmul(double *X, const double *M, size_t n6, int p, cudaStream_t s);
 // out[k] (contiguous, length n6) = sum_{b, c} column c of Q_b times C[(b p + c) nout + k].

@@ -318,10 +318,19 @@ void build_solve_schedule(Factor &f) {
     L.chunks.resize(L.ch_ptr[L.nlevels]);
     std::vector<int> fr(L.row_ptr.begin(), L.row_ptr.end() - 1);
     std::vector<int> fc(L.ch_ptr.begin(), L.ch_ptr.end() - 1);
+    // big chunks (more than APPLY_WARP_ROWS rows) first within each level
+    L.nbig.assign(L.nlevels, 0);
+    for (int c = 0; c < nc; c++)
+      if (cp.c0[c + 1] - cp.c0[c] > APPLY_WARP_ROWS) L.nbig[lev[c]]++;
+    std::vector<int> fb(fc), fs(L.nlevels);
+    for (int l = 0; l < L.nlevels; l++) fs[l] = fc[l] + L.nbig[l];
     for (int c = 0; c < nc; c++) {
       const int ns = cp.c0[c + 1] - cp.c0[c];
       for (int i = cp.c0[c]; i < cp.c0[c + 1]; i++) L.rows[fr[lev[c]]++] = i;
-      if (ns >= 2) L.chunks[fc[lev[c]]++] = c;
+      if (ns > APPLY_WARP_ROWS)
+        L.chunks[fb[lev[c]]++] = c;
+      else if (ns >= 2)
+        L.chunks[fs[lev[c]]++] = c;
     }
     L.max_rows.assign(L.nlevels, 1);
     for (int c = 0; c < nc; c++)
@@ -343,7 +352,7 @@ void build_solve_schedule(Factor &f) {
       // D^{-1} after the full sum)
       const int nr = L.row_ptr[l + 1] - L.row_ptr[l];
       if (L.cta[l] && nr < 4 * 152 && !(upper && single))
-        L.split[l] = std::min(32, std::max(1, maxlen / SOLVE_SPLIT_BLOCKS));
+        L.split[l] = std::min(SOLVE_SPLIT_MAX, std::max(1, maxlen / SOLVE_SPLIT_BLOCKS));
     }
   };
   fill_levels(lv, maxl, false, cp.lo);

@@ -59,7 +59,9 @@ struct PanelSchedule {
 struct ChunkLevels {
   int nlevels = 0;
   std::vector<int> row_ptr, rows;   // rows of each level
-  std::vector<int> ch_ptr, chunks;  // chunks of >= 2 rows of each level
+  std::vector<int> ch_ptr, chunks;  // chunks of >= 2 rows of each level, those of more
+                                    // than APPLY_WARP_ROWS rows first
+  std::vector<int> nbig;            // per level: chunks of more than APPLY_WARP_ROWS rows
   std::vector<char> cta;            // per level: 1 = one CTA per row (long rows)
   std::vector<int> max_rows;        // per level: rows of its largest chunk
   std::vector<int> split;           // per level: CTAs sharing each long row (1 = none)
@@ -103,6 +105,7 @@ struct Factor {
   DBuf<int> d_lo_rows, d_lo_chunks, d_up_rows, d_up_chunks, d_ck_small, d_ck_big;
   DBuf<double> cinv64, cscr64;  // FP64 inverses (all precisions) and gathered blocks
   DBuf<float> cinv32;           // FP32 copy of the inverses for FP32 factors
+  DBuf<unsigned char> tvec;     // solve scratch: the pulled sums of chunk rows
   // algorithmic FP operations of one numeric factorization: 432 per L block
   // (L_ij = A_ij D_j^{-1}), 432 per block update, 432 per diagonal inverse
   double flop_count = 0.0;
@@ -147,8 +150,12 @@ constexpr int PANEL_UC_SMEM = 8192;
 // a pull level uses one CTA per row.
 constexpr int CHUNK_MAX = 128;
 constexpr int SOLVE_LONG_ROW = 24;
-// factor blocks per CTA when a level's long rows are split over CTAs
-constexpr int SOLVE_SPLIT_BLOCKS = 384;
+// factor blocks per CTA when a level's long rows are split over CTAs, and
+// the largest split
+constexpr int SOLVE_SPLIT_BLOCKS = 192;
+constexpr int SOLVE_SPLIT_MAX = 64;
+// chunks of at most this many rows are applied one warp per chunk
+constexpr int APPLY_WARP_ROWS = 16;
 
 // F (f.precision: 64 double, 48 double-float, 32 float values; 8 bytes per
 // value for 64 and 48) <- pattern-embedded copy of A (+ alpha2 * A2 when
@@ -167,7 +174,7 @@ int factor_levels(const Factor &f, void *F, int *status, cudaStream_t s, long lo
 // first call with these (F, x, y, nrhs) and replayed afterwards (s must not
 // be capturing already).
 template <typename T, typename TV>
-int solve_levels(const Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
+int solve_levels(Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
                  long long *launches);
 template <typename T, typename TV>
 int solve_graph(Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,

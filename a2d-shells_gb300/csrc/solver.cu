@@ -405,6 +405,13 @@ struct BucklingState {
   IrWork ir;
   DBuf<float> gw32;
   bool preloaded = false;  // K holds K_T(u) and path the preload state u
+  // deflation of the GMRES-IR shift-invert solves (FP32 factors) by the
+  // Lanczos basis: AQ = (K + sigma G) Q per block, Cq = Q^T A Q; the
+  // deflation space Y (Ritz vectors, defl_k columns in defl_k / p blocks),
+  // AY = A Y and (Y^T A Y)^{-1} on the device
+  DBuf<double> AQ, dT, dHd, Yd, AYd, dCinv, dYc, dSk;
+  std::vector<double> Cq;
+  int defl_k = 0;
   std::vector<double> lam, err, ritz;  // converged data
   int nconv = 0;
   double sigma = 0.0;
@@ -581,7 +588,9 @@ int BucklingState::precond(Mesh &m, Factor &f, const double *V, double *Z, int p
 // than half ends the solve as converged to that floor.
 // Orthogonalisation: two classical Gram-Schmidt passes.  One host
 // synchronisation per Arnoldi step (the p columns' Hessenberg entries).
-// precond(V, Z) applies the preconditioner to one n6 x p block.
+// precond(V, Z, AZ, az) applies the preconditioner to one n6 x p block; a
+// preconditioner that forms A Z on the way stores it in AZ and sets az,
+// otherwise the solver forms it.
 template <class Precond>
 static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const double *Avals,
                               const double *X, double *Y, int p, double rtol, int msub,
@@ -644,8 +653,9 @@ static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const doubl
     for (int j = 0; j < msub; j++) {
       double *Vj = S.V.p + (size_t)j * bs, *Zj = S.Z.p + (size_t)j * bs;
       double *W = S.V.p + (size_t)(j + 1) * bs;
-      if ((rc = precond(Vj, Zj))) return rc;
-      if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Avals, Zj, nullptr, W, p, m.stream)))
+      bool az = false;
+      if ((rc = precond(Vj, Zj, W, az))) return rc;
+      if (!az && (rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Avals, Zj, nullptr, W, p, m.stream)))
         return rc;
       if ((rc = col_dots(S.V.p, j + 1, bs, W, n6, p, dH1, m.stream))) return rc;
       if ((rc = col_axpy(W, S.V.p, j + 1, bs, dH1, n6, p, -1.0, m.stream))) return rc;
@@ -713,7 +723,9 @@ static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const doubl
 static int solve_k(Mesh &m, BucklingState &S, Factor &f, const double *Avals, const double *b,
                    double *x, double rtol, int *inner) {
   if (f.precision == 32) {
-    auto pc = [&](const double *V, double *Z) { return S.precond(m, f, V, Z, 1); };
+    auto pc = [&](const double *V, double *Z, double *, bool &) {
+      return S.precond(m, f, V, Z, 1);
+    };
     return fgmres_block_solve(m, S.ir, pc, Avals, b, x, 1, rtol, GMRES_IR_MSUB, GMRES_IR_CYCLES,
                               inner);
   }
@@ -1001,6 +1013,139 @@ static int prepare_solve(Mesh &m, const a2ds_buckling_opts *opts, BucklingState 
   return 0;
 }
 
+// Deflation of the shift-invert solves by Ritz vectors.  The FP32 factor's
+// relative error is largest along the near-singular directions of
+// A = K + sigma G, the buckling modes next to the shift, which the block
+// Lanczos basis converges to first; so the GMRES-IR preconditioner is
+// M^{-1} followed by the exact correction in span(Y), Y the DEFL_RITZ Ritz
+// vectors of the lowest loads from the basis built so far:
+//   z = M^{-1} v,  z <- z + Y (Y^T A Y)^{-1} Y^T (v - A z),
+// which makes the preconditioned operator exact on span(Y).  AQ = K Q +
+// sigma G Q is formed once per basis block and Cq = Q^T A Q grows by one
+// block row and column per Lanczos step; with Y = Q S (S the Ritz
+// coefficients), A Y = AQ S and Y^T A Y = S^T Cq S need no product with A.
+constexpr int DEFL_RITZ = 16;
+
+static int defl_add_block(Mesh &m, BucklingState &S, Blas &B, int b, int p, int tdim) {
+  const size_t n6 = (size_t)m.nn * 6, bs = n6 * p;
+  int rc;
+  double *AQb = S.AQ.p + (size_t)b * bs;
+  if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.G.p, S.Q.p + (size_t)b * bs, nullptr, AQb, p,
+                     m.stream)))
+    return rc;
+  B.axpby(AQb, 1.0, S.KQ.p + (size_t)b * bs, S.sigma, bs);  // AQ_b = K Q_b + sigma G Q_b
+  if ((rc = blk_dots(S.Q.p, b + 1, bs, AQb, n6, p, S.dHd.p, m.stream))) return rc;
+  m.launches += 2;
+  std::vector<double> h((size_t)(b + 1) * p * p);
+  A2DS_CUDA_TRY(cudaMemcpyAsync(h.data(), S.dHd.p, h.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, m.stream));
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+  for (int bb = 0; bb <= b; bb++)
+    for (int c1 = 0; c1 < p; c1++)
+      for (int c2 = 0; c2 < p; c2++) {
+        const double v = h[((size_t)bb * p + c1) * p + c2];
+        S.Cq[(size_t)(bb * p + c1) * tdim + b * p + c2] = v;
+        S.Cq[(size_t)(b * p + c2) * tdim + bb * p + c1] = v;
+      }
+  return 0;
+}
+
+// Y, AY and (Y^T A Y)^{-1} from the Ritz vectors of the leading mdim x mdim
+// block of T (row-major in Tt with leading dimension tdim): the min(
+// DEFL_RITZ, mdim) lowest loads (lamof ascending in magnitude).
+template <class Lamof>
+static int defl_update_ritz(Mesh &m, BucklingState &S, const std::vector<double> &Tt, int tdim,
+                            int mdim, int p, Lamof &&lamof) {
+  const size_t n6 = (size_t)m.nn * 6, bs = n6 * p;
+  std::vector<double> Tm((size_t)mdim * mdim), w, V;
+  for (int a = 0; a < mdim; a++)
+    for (int b = 0; b < mdim; b++) Tm[(size_t)a * mdim + b] = Tt[(size_t)a * tdim + b];
+  if (sym_eig(mdim, Tm, w, V)) return fail(A2DS_ERR_NUMERIC, "deflation: eigensolver failed");
+  std::vector<int> order(mdim);
+  for (int k = 0; k < mdim; k++) order[k] = k;
+  std::sort(order.begin(), order.end(),
+            [&](int a, int c) { return fabs(lamof(w[a])) < fabs(lamof(w[c])); });
+  const int k = std::min(DEFL_RITZ, mdim);  // a multiple of p (p divides DEFL_RITZ)
+  std::vector<double> Sk((size_t)mdim * k);
+  for (int r = 0; r < mdim; r++)
+    for (int q = 0; q < k; q++) Sk[(size_t)r * k + q] = V[(size_t)r * mdim + order[q]];
+  int rc;
+  if ((rc = S.dSk.upload(Sk.data(), Sk.size(), m.stream))) return rc;
+  if ((rc = blk_mul(S.Q.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.Yd.p, m.stream)) ||
+      (rc = blk_mul(S.AQ.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.AYd.p, m.stream)))
+    return rc;
+  m.launches += 2;
+  // Y^T A Y = Sk^T Cq Sk, inverted on its eigenvectors (|w| below 1e-12
+  // max |w| dropped)
+  std::vector<double> CS((size_t)mdim * k, 0.0), Cy((size_t)k * k, 0.0);
+  for (int a = 0; a < mdim; a++)
+    for (int b = 0; b < mdim; b++) {
+      const double c = S.Cq[(size_t)a * tdim + b];
+      if (c == 0.0) continue;
+      for (int q = 0; q < k; q++) CS[(size_t)a * k + q] += c * Sk[(size_t)b * k + q];
+    }
+  for (int q1 = 0; q1 < k; q1++)
+    for (int q2 = 0; q2 < k; q2++) {
+      double acc = 0.0;
+      for (int a = 0; a < mdim; a++) acc += Sk[(size_t)a * k + q1] * CS[(size_t)a * k + q2];
+      Cy[(size_t)q1 * k + q2] = acc;
+    }
+  std::vector<double> cw, cv;
+  if (sym_eig(k, Cy, cw, cv)) return fail(A2DS_ERR_NUMERIC, "deflation: eigensolver failed");
+  double wmax = 0.0;
+  for (double x : cw) wmax = std::max(wmax, fabs(x));
+  std::vector<double> Ci((size_t)k * k, 0.0);
+  for (int q = 0; q < k; q++) {
+    if (!(fabs(cw[q]) > 1e-12 * wmax)) continue;
+    const double iw = 1.0 / cw[q];
+    for (int i = 0; i < k; i++)
+      for (int j = 0; j < k; j++) Ci[(size_t)i * k + j] += cv[(size_t)i * k + q] * iw * cv[(size_t)j * k + q];
+  }
+  if ((rc = S.dCinv.upload(Ci.data(), Ci.size(), m.stream))) return rc;
+  A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // the host tables go out of scope
+  S.defl_k = k;
+  return 0;
+}
+
+// y = -Cinv h (k x p; h, y laid out [(b p + c1) p + c2] as blk_dots writes
+// and blk_sub reads), one thread per entry.
+__global__ void k_defl_coef(const double *__restrict__ Ci, const double *__restrict__ h,
+                            double *__restrict__ y, int k, int p) {
+  const int t = threadIdx.x;
+  if (t >= k * p) return;
+  const int i = t / p, c = t - i * p;
+  double acc = 0.0;
+  for (int q = 0; q < k; q++) acc += Ci[(size_t)i * k + q] * h[(size_t)q * p + c];
+  y[t] = -acc;
+}
+__global__ void k_diff(double *__restrict__ T, const double *__restrict__ V,
+                       const double *__restrict__ AZ, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    T[i] = V[i] - AZ[i];
+}
+
+// z <- z + Y Cinv Y^T (v - A z) for a block of p columns, and AZ = A z of
+// the corrected z: A z is formed once (the product GMRES needs anyway) and
+// corrected with AY, so the deflation costs no product with A of its own.
+// No host synchronisation.
+static int defl_correct(Mesh &m, BucklingState &S, const double *V, double *Z, double *AZ,
+                        int p) {
+  const int k = S.defl_k, kb = k / p;
+  const size_t n6 = (size_t)m.nn * 6, bs = n6 * p;
+  int rc;
+  if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.Aux.p, Z, nullptr, AZ, p, m.stream)))
+    return rc;
+  k_diff<<<grid_for(bs), 256, 0, m.stream>>>(S.dT.p, V, AZ, bs);  // T = V - A z
+  if ((rc = blk_dots(S.Yd.p, kb, bs, S.dT.p, n6, p, S.dHd.p, m.stream))) return rc;
+  k_defl_coef<<<1, 256, 0, m.stream>>>(S.dCinv.p, S.dHd.p, S.dYc.p, k, p);
+  if ((rc = blk_sub(Z, S.Yd.p, kb, bs, S.dYc.p, n6, p, m.stream))) return rc;
+  if ((rc = blk_sub(AZ, S.AYd.p, kb, bs, S.dYc.p, n6, p, m.stream))) return rc;
+  m.launches += 6;
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 // A = K + sigma G (identity Dirichlet rows), its factor (complete fill) and
 // the block shift-invert Lanczos on A^{-1} K with the K inner product
 // (EPBucklingShiftInvert + SEP::solve, src/bpmat/GSEP.cpp:200-244,485-596);
@@ -1057,6 +1202,21 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
   if ((rc = cholqr2(m, S, S.Q.p, S.KQ.p, p, Bj))) return rc;
 
   const int tdim = (nbmax + 1) * p;
+  // deflation of the GMRES-IR solves (FP32 factors only)
+  const bool deflate = direct && S.fa.precision == 32;
+  S.defl_k = 0;
+  if (deflate) {
+    const int kb = DEFL_RITZ / p;
+    if (DEFL_RITZ % p) return fail(A2DS_ERR_ARG, "deflation: block size must divide 16");
+    if ((rc = S.AQ.alloc((size_t)(nbmax + 1) * bs)) || (rc = S.dT.alloc(bs)) ||
+        (rc = S.dHd.alloc(std::max<size_t>((size_t)(nbmax + 1) * p * p, DEFL_RITZ * p))) ||
+        (rc = S.Yd.alloc((size_t)kb * bs)) ||
+        (rc = S.AYd.alloc((size_t)kb * bs)) || (rc = S.dCinv.alloc(DEFL_RITZ * DEFL_RITZ)) ||
+        (rc = S.dYc.alloc(DEFL_RITZ * p)))
+      return rc;
+    S.Cq.assign((size_t)tdim * tdim, 0.0);
+    if ((rc = defl_add_block(m, S, B, 0, p, tdim))) return rc;
+  }
   std::vector<double> T((size_t)tdim * tdim, 0.0), h1((size_t)p * p), h2((size_t)p * p);
   std::vector<double> Tw, TV, Tm;
   std::vector<int> order;
@@ -1073,7 +1233,12 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
       // unaffected at that tolerance
       const double rtol = std::max(1e-12, std::min(1e-9, 0.1 * opts->eig_tol));
       if (S.fa.precision == 32) {
-        auto pc = [&](const double *V, double *Z) { return S.precond(m, S.fa, V, Z, p); };
+        auto pc = [&](const double *V, double *Z, double *AZ, bool &az) {
+          int r2 = S.precond(m, S.fa, V, Z, p);
+          if (r2 || S.defl_k <= 0) return r2;
+          az = true;
+          return defl_correct(m, S, V, Z, AZ, p);
+        };
         if ((rc = fgmres_block_solve(m, S.ir, pc, S.Aux.p, KQj, W, p, rtol, GMRES_IR_MSUB,
                                      GMRES_IR_CYCLES, &inner)))
           return rc;
@@ -1109,6 +1274,7 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
       return rc;
     m.launches++;
     if ((rc = cholqr2(m, S, W, KW, p, Bj))) return rc;  // synchronises: h1, h2 are ready
+    if (deflate && j + 1 < nbmax && (rc = defl_add_block(m, S, B, j + 1, p, tdim))) return rc;
     // T: diagonal block j (symmetrised), sub/super-diagonal blocks from B_j
     for (int a = 0; a < p; a++)
       for (int b = 0; b < p; b++) {
@@ -1121,6 +1287,8 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
     nsteps = j + 1;
     mdim = nsteps * p;
     lastB = Bj;
+    if (deflate && j + 1 < nbmax && (rc = defl_update_ritz(m, S, T, tdim, mdim, p, lamof)))
+      return rc;
     if (mdim < nev) continue;
     // Ritz values of the leading mdim x mdim block of T
     Tm.assign((size_t)mdim * mdim, 0.0);
@@ -1335,7 +1503,7 @@ int a2ds_fgmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rt
     return rc;
   }
   IrWork w;
-  auto precond = [&](const double *V, double *Z) {
+  auto precond = [&](const double *V, double *Z, double *, bool &) {
     return precondition_block(m, f, V, Z, nrhs, w32.p, xb.p, yb.p);
   };
   int it = 0;
@@ -1721,7 +1889,7 @@ int a2ds_newton_preload(a2ds_mesh mesh, const double *rhs, double load, int nste
   B.launches = &m.launches;
   const double fn = sqrt(B.dot(P->f.p, P->f.p, n6));
   if (!(fn > 0.0)) return fail(A2DS_ERR_ARG, "zero load vector");
-  auto pc = [&](const double *V, double *Z) {
+  auto pc = [&](const double *V, double *Z, double *, bool &) {
     return precondition_block(m, P->ft, V, Z, 1, P->w32.p, P->xb.p, P->yb.p);
   };
   double rel = 0.0;

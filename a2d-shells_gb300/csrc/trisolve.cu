@@ -11,10 +11,12 @@
 // to all R vectors.  The rows are cut into chunks of consecutive rows
 // (ChunkPlan, ilu.h) scheduled by dependency levels; per level one launch
 // pulls, for every row of the level, the sums over its factor blocks outside
-// its chunk (a warp per row, or a CTA per row on levels with long rows), and
-// one launch applies each chunk's precomputed dense inverse (unit-lower for
-// L, D + U for the upper solve) to its rows.  A one-row chunk needs no
-// inverse: the pull finishes it (times D_i^{-1} in the upper solve).
+// its chunk (a warp per row, or a CTA per row on levels with long rows) into
+// a scratch vector t, and one launch applies each chunk's precomputed dense
+// inverse (unit-lower for L, D + U for the upper solve) to t's rows of the
+// chunk, writing y; the apply of one chunk is spread over many CTAs.  A
+// one-row chunk needs no inverse: the pull finishes it in y (times D_i^{-1}
+// in the upper solve).
 // solve_graph() captures the whole launch sequence once per (factor, x, y,
 // R) and replays it.
 #include "a2ds_internal.h"
@@ -22,29 +24,56 @@
 
 namespace a2ds {
 
-// Partial sums of sum_k F_k[ii][:] y[fcols[k]] over k = kb + g, kb + g + step, ...
+// Aligned groups of values: a factor block's row ii (six values at
+// (36 k + 6 ii), 8-byte aligned in FP32, 16 in FP64) and a vector row's R
+// right-hand sides (at a multiple of R values).
+template <typename V, int N, int A>
+struct alignas(A) Vals {
+  V v[N];
+};
+template <typename T>
+using BlockRow = Vals<T, 6, sizeof(T) == 4 ? 8 : 16>;
+template <typename TV, int R>
+using RhsRow = Vals<TV, R, (R * sizeof(TV) >= 16 ? 16 : R * sizeof(TV))>;
+
+template <typename T, typename TV, int R>
+__device__ __forceinline__ void block_row_fma(const BlockRow<T> &a, const TV *yv, TV (&acc)[R]) {
+#pragma unroll
+  for (int c = 0; c < 6; c++) {
+    const RhsRow<TV, R> yr = *reinterpret_cast<const RhsRow<TV, R> *>(yv + c * R);
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] += (TV)a.v[c] * yr.v[r];
+  }
+}
+
+// Partial sums of sum_k F_k[ii][:] y[fcols[k]] over k = kb + g, kb + g + step,
+// ..., two blocks per step so that both blocks' index, factor and vector
+// loads are in flight together.
 template <typename T, typename TV, int R>
 __device__ __forceinline__ void row_partial(int kb, int ke, int g, int step, int ii,
                                             const int *__restrict__ fcols,
                                             const T *__restrict__ F, const TV *y, TV (&acc)[R]) {
-  for (int k = kb + g; k < ke; k += step) {
-    const T *a = F + (size_t)k * 36 + 6 * ii;
-    TV av[6];
-#pragma unroll
-    for (int c = 0; c < 6; c++) av[c] = (TV)a[c];
-    const TV *yv = y + (size_t)fcols[k] * 6 * R;
-#pragma unroll
-    for (int c = 0; c < 6; c++)
-#pragma unroll
-      for (int r = 0; r < R; r++) acc[r] += av[c] * yv[c * R + r];
+  int k = kb + g;
+  for (; k + step < ke; k += 2 * step) {
+    const int j0 = fcols[k], j1 = fcols[k + step];
+    const BlockRow<T> a0 = *reinterpret_cast<const BlockRow<T> *>(F + (size_t)k * 36 + 6 * ii);
+    const BlockRow<T> a1 =
+        *reinterpret_cast<const BlockRow<T> *>(F + (size_t)(k + step) * 36 + 6 * ii);
+    block_row_fma<T, TV, R>(a0, y + (size_t)j0 * 6 * R, acc);
+    block_row_fma<T, TV, R>(a1, y + (size_t)j1 * 6 * R, acc);
+  }
+  if (k < ke) {
+    const BlockRow<T> a0 = *reinterpret_cast<const BlockRow<T> *>(F + (size_t)k * 36 + 6 * ii);
+    block_row_fma<T, TV, R>(a0, y + (size_t)fcols[k] * 6 * R, acc);
   }
 }
 
-// y_i = src_i - sum_{k in [beg_i, end_i)} F_k y_{fcols[k]} for every row of
-// a level, one warp per row (five groups of six lanes over the blocks).  In
-// the upper solve (UPPER) a row that is its own chunk is finished here:
-// y_i = D_i^{-1} (src_i - sum).  Lower: beg = frowp, end = row_lend, src = x;
-// upper: beg = row_ustart, end = frowp + 1, src = y.
+// r_i = src_i - sum_{k in [beg_i, end_i)} F_k y_{fcols[k]} for every row of
+// a level, one warp per row (five groups of six lanes over the blocks),
+// stored in t_i for rows of multi-row chunks and in y_i for rows that are
+// their own chunk; in the upper solve (UPPER) such a row is finished here:
+// y_i = D_i^{-1} r_i.  Lower: beg = frowp, end = row_lend; upper: beg =
+// row_ustart, end = frowp + 1; src = y (holding x, then the lower result).
 template <typename T, typename TV, int R, bool UPPER>
 __global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows, int nrows,
                                                    const int *__restrict__ frowp,
@@ -52,7 +81,8 @@ __global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows,
                                                    const int *__restrict__ single,
                                                    const int *__restrict__ fcols,
                                                    const int *__restrict__ fdiag,
-                                                   const T *__restrict__ F, const TV *src, TV *y) {
+                                                   const T *__restrict__ F, const TV *src, TV *y,
+                                                   TV *t) {
   __shared__ TV part[8][30][R];
   __shared__ TV z[8][6][R];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -70,7 +100,8 @@ __global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows,
 #pragma unroll
     for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
   __syncwarp();
-  const bool fin = UPPER && single[i];
+  const bool one = single[i], fin = UPPER && one;
+  TV *dst = one ? y : t;
   for (int o = lane; o < 6 * R; o += 32) {
     const int d = o / R, r = o - R * d;
     const TV v = part[wib][d][r] + part[wib][d + 6][r] + part[wib][d + 12][r] +
@@ -79,7 +110,7 @@ __global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows,
     if (fin)
       z[wib][d][r] = src[idx] - v;
     else
-      y[idx] = src[idx] - v;
+      dst[idx] = src[idx] - v;
   }
   if (!fin) return;
   __syncwarp();
@@ -95,8 +126,9 @@ __global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows,
 
 // The same for levels with long rows: one 256-thread CTA per row, 42 groups
 // of six threads over the row's blocks.  With split > 1 a row's blocks are
-// shared by gridDim.y CTAs that subtract their partial sums from y_i with
-// atomic adds (y_i already holds src_i; not for rows finished with D_i^{-1}).
+// shared by gridDim.y CTAs that subtract their partial sums from its t_i or
+// y_i with atomic adds (which already hold src_i; not for rows finished with
+// D_i^{-1}).
 template <typename T, typename TV, int R, bool UPPER>
 __global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, int nrows,
                                                   const int *__restrict__ frowp,
@@ -104,14 +136,15 @@ __global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, 
                                                   const int *__restrict__ single,
                                                   const int *__restrict__ fcols,
                                                   const int *__restrict__ fdiag,
-                                                  const T *__restrict__ F, const TV *src, TV *y) {
+                                                  const T *__restrict__ F, const TV *src, TV *y,
+                                                  TV *t) {
   __shared__ TV part[252][R];
   __shared__ TV z[6][R];
   const int rr = blockIdx.x;
   if (rr >= nrows) return;
   const int i = rows[rr];
-  const int t = threadIdx.x;
-  const int g = t / 6, ii = t - 6 * g;
+  const int tid = threadIdx.x;
+  const int g = tid / 6, ii = tid - 6 * g;
   int kb = UPPER ? bound[i] : frowp[i];
   int ke = UPPER ? frowp[i + 1] : bound[i];
   const int split = gridDim.y;
@@ -120,32 +153,33 @@ __global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, 
     kb += per * blockIdx.y;
     ke = min(ke, kb + per);
   }
-  if (t < 252) {
+  if (tid < 252) {
     TV acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
     row_partial<T, TV, R>(kb, ke, g, 42, ii, fcols, F, y, acc);
 #pragma unroll
-    for (int r = 0; r < R; r++) part[t][r] = acc[r];
+    for (int r = 0; r < R; r++) part[tid][r] = acc[r];
   }
   __syncthreads();
-  const bool fin = UPPER && single[i];
-  for (int o = t; o < 6 * R; o += blockDim.x) {
+  const bool one = single[i], fin = UPPER && one;
+  TV *dst = one ? y : t;
+  for (int o = tid; o < 6 * R; o += blockDim.x) {
     const int d = o / R, r = o - R * d;
     TV v = 0;
     for (int gg = 0; gg < 42; gg++) v += part[6 * gg + d][r];
     const size_t idx = ((size_t)i * 6 + d) * R + r;
     if (split > 1)
-      atomicAdd(&y[idx], -v);
+      atomicAdd(&dst[idx], -v);
     else if (fin)
       z[d][r] = src[idx] - v;
     else
-      y[idx] = src[idx] - v;
+      dst[idx] = src[idx] - v;
   }
   if (!fin || split > 1) return;
   __syncthreads();
   const T *Dinv = F + (size_t)fdiag[i] * 36;
-  for (int o = t; o < 6 * R; o += blockDim.x) {
+  for (int o = tid; o < 6 * R; o += blockDim.x) {
     const int d = o / R, r = o - R * d;
     TV v = 0;
 #pragma unroll
@@ -182,41 +216,112 @@ __device__ __forceinline__ TV warp_reduce_scatter(TV (&v)[R], int lane, int &rhs
   return sum;
 }
 
-// y_c <- Inv_c y_c for every chunk c of a level (one CTA per chunk): the
-// chunk's rows (6 ns x R values, the pulled sums) are staged in shared
-// memory, then each warp takes rows of the inverse (row-major, 6 ns wide;
-// lower: only columns up to the row's block, upper: from it on), lanes over
-// the columns, and a reduce-scatter over the R right-hand sides.
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+  using type = float2;
+};
+template <>
+struct Pair<double> {
+  using type = double2;
+};
+// The 2 R values of two consecutive vector rows, loaded as one aligned unit.
+template <typename TV, int N>
+struct alignas(N * sizeof(TV) >= 16 ? 16 : N * sizeof(TV)) Pack {
+  TV v[N];
+};
+
+// Rows of the inverse formed together by one warp: all six rows of a block
+// row share its column range, so the vector values loaded for a column are
+// used ROWS times (fewer for wide R to bound the accumulators).
+template <int R>
+struct ApplyRows {
+  static constexpr int value = R <= 4 ? 6 : (R == 8 ? 3 : 1);
+};
+
+// One warp's share of y_c = Inv_c t_c: rows 6 blk + q0 .. + ROWS - 1 of the
+// inverse (row-major, w = 6 ns wide; lower: columns up to the block's end,
+// upper: from its start on), lanes over column pairs (one 8/16-byte load of
+// the inverse per row, one load of the two columns' R values from the
+// staged vector sv), then a reduce-scatter over the R right-hand sides per
+// row.  Every column range starts at an even column and the inverse's
+// offsets are even, so the paired loads are aligned.  The inverse is read
+// with the streaming hint: it is used once per solve and must not evict
+// the staged vectors' lines.
 template <typename T, typename TV, int R, bool UPPER>
-__global__ void __launch_bounds__(1024) k_chunk_apply(const int *__restrict__ chunks,
-                                                     const int *__restrict__ c0,
-                                                     const long long *__restrict__ off,
-                                                     const T *__restrict__ inv, TV *y) {
-  extern __shared__ unsigned char smem_raw[];
-  TV *sv = reinterpret_cast<TV *>(smem_raw);  // [r][col], 6 ns x R
-  const int c = chunks[blockIdx.x];
+__device__ __forceinline__ void apply_rows(const T *__restrict__ Inv, int w, int blk, int q0,
+                                           const TV *sv, TV *yc, int lane) {
+  using T2 = typename Pair<T>::type;
+  constexpr int ROWS = ApplyRows<R>::value;
+  const int cb = UPPER ? 6 * blk : 0, ce = UPPER ? w : 6 * blk + 6;
+  const T *I0 = Inv + (size_t)(6 * blk + q0) * w;
+  TV acc[ROWS][R];
+#pragma unroll
+  for (int q = 0; q < ROWS; q++)
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[q][r] = 0;
+#pragma unroll 1
+  for (int col = cb + 2 * lane; col < ce; col += 64) {
+    const Pack<TV, 2 * R> tv = *reinterpret_cast<const Pack<TV, 2 * R> *>(sv + (size_t)col * R);
+#pragma unroll
+    for (int q = 0; q < ROWS; q++) {
+      const T2 m = __ldcs(reinterpret_cast<const T2 *>(I0 + (size_t)q * w + col));
+#pragma unroll
+      for (int r = 0; r < R; r++) acc[q][r] += (TV)m.x * tv.v[r] + (TV)m.y * tv.v[R + r];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < ROWS; q++) {
+    int rhs;
+    const TV sum = warp_reduce_scatter<TV, R>(acc[q], lane, rhs);
+    if ((lane & (32 / R - 1)) == 0) yc[(size_t)(6 * blk + q0 + q) * R + rhs] = sum;
+  }
+}
+
+// y_c = Inv_c t_c for every chunk c of a level, in one launch of 256-thread
+// CTAs.  The level's nbig chunks of more than APPLY_WARP_ROWS rows come
+// first, each spread over S CTAs (blocks [0, nbig S)): the CTA stages t_c
+// (6 ns x R values, layout as in t) in shared memory, then its warps take
+// units of ROWS rows of one block row, unit u = split + S (warp + 8 k)
+// (interleaved, so the short and long block rows of the triangular inverse
+// spread evenly).  The small chunks follow, one warp per chunk and eight
+// per CTA, each warp staging its own chunk.
+template <typename T, typename TV, int R, bool UPPER>
+__global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2)
+    k_chunk_apply(const int *__restrict__ chunks, int nch, int nbig, int S,
+                  const int *__restrict__ c0, const long long *__restrict__ off,
+                  const T *__restrict__ inv, const TV *__restrict__ t, TV *__restrict__ y) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int PER = 6 / ApplyRows<R>::value;  // units per block row
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = blockIdx.x;
+  if (b < nbig * S) {
+    TV *sv = reinterpret_cast<TV *>(smem_raw);
+    const int c = chunks[b / S], split = b % S;
+    const int a = c0[c], ns = c0[c + 1] - a, w = 6 * ns;
+    const T *Inv = inv + off[c] + (UPPER ? (long long)w * w : 0);
+    const TV *tc = t + (size_t)a * 6 * R;
+    for (int k = threadIdx.x; k < w * R; k += blockDim.x) sv[k] = tc[k];
+    __syncthreads();
+    TV *yc = y + (size_t)a * 6 * R;
+    for (int u = split + S * warp; u < ns * PER; u += S * 8)
+      apply_rows<T, TV, R, UPPER>(Inv, w, u / PER, (u % PER) * ApplyRows<R>::value, sv, yc,
+                                  lane);
+    return;
+  }
+  const int ci = nbig + (b - nbig * S) * 8 + warp;
+  if (ci >= nch) return;  // whole warp leaves together
+  TV *sv = reinterpret_cast<TV *>(smem_raw) + (size_t)warp * 6 * APPLY_WARP_ROWS * R;
+  const int c = chunks[ci];
   const int a = c0[c], ns = c0[c + 1] - a, w = 6 * ns;
   const T *Inv = inv + off[c] + (UPPER ? (long long)w * w : 0);
+  const TV *tc = t + (size_t)a * 6 * R;
+  for (int k = lane; k < w * R; k += 32) sv[k] = tc[k];
+  __syncwarp();
   TV *yc = y + (size_t)a * 6 * R;
-  for (int k = threadIdx.x; k < w * R; k += blockDim.x) sv[(k % R) * w + k / R] = yc[k];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int row = warp; row < w; row += nw) {
-    const int blk = row / 6;
-    const int cb = UPPER ? 6 * blk : 0, ce = UPPER ? w : 6 * blk + 6;
-    const T *Ir = Inv + (size_t)row * w;
-    TV acc[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) acc[r] = 0;
-    for (int col = cb + lane; col < ce; col += 32) {
-      const TV m = (TV)Ir[col];
-#pragma unroll
-      for (int r = 0; r < R; r++) acc[r] += m * sv[r * w + col];
-    }
-    int rhs;
-    const TV sum = warp_reduce_scatter<TV, R>(acc, lane, rhs);
-    if ((lane & (32 / R - 1)) == 0) yc[(size_t)row * R + rhs] = sum;
-  }
+  for (int u = 0; u < ns * PER; u++)
+    apply_rows<T, TV, R, UPPER>(Inv, w, u / PER, (u % PER) * ApplyRows<R>::value, sv, yc, lane);
 }
 
 // Dense FP64 copy of every multi-row chunk's diagonal block out of the factor
@@ -304,11 +409,12 @@ __global__ void k_chunk_inverse(const int *__restrict__ chunks, const int *__res
 }
 
 // ------------------------------------------------------------ launchers
-// Shared memory of k_chunk_apply for the largest chunk: 6 CHUNK_MAX x R
-// values, above the default 48 KB for wide blocks of FP64 vectors.
+// Dynamic shared memory of the apply kernel at its largest (one chunk of
+// CHUNK_MAX rows, or eight of APPLY_WARP_ROWS rows), above the default 48 KB
+// for wide blocks of FP64 vectors.  Set outside any stream capture.
 template <typename T, typename TV, int R>
 static int chunk_apply_config() {
-  const int smem = 6 * CHUNK_MAX * R * (int)sizeof(TV);
+  const int smem = std::max(CHUNK_MAX, 8 * APPLY_WARP_ROWS) * 6 * R * (int)sizeof(TV);
   A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, false>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, true>,
@@ -331,7 +437,6 @@ static int chunk_apply_config_all() {
 int chunk_alloc(Factor &f) {
   const ChunkPlan &cp = f.cp;
   int rc;
-  // (function attributes are set here, outside any stream capture)
   if ((rc = f.precision == 32 ? chunk_apply_config_all<float, float>()
                               : chunk_apply_config_all<double, double>()))
     return rc;
@@ -391,8 +496,15 @@ const double *chunk_inverses<double>(const Factor &f) { return f.cinv64.p; }
 template <>
 const float *chunk_inverses<float>(const Factor &f) { return f.cinv32.p; }
 
+// CTAs per big chunk of a level with nbig big chunks of at most mr rows
+// (units = block rows x 6 / ROWS): about 4 x 152 CTAs for the big chunks,
+// at least one unit per warp.
+static int chunk_apply_split(int nbig, int mr, int per) {
+  return std::max(1, std::min((4 * 152 + nbig - 1) / nbig, mr * per / 8));
+}
+
 template <typename T, typename TV, int R, bool UPPER>
-static void solve_level(const Factor &f, const T *F, const TV *src, TV *y, int l, cudaStream_t s,
+static void solve_level(const Factor &f, const T *F, TV *y, TV *t, int l, cudaStream_t s,
                         long long &nl) {
   const ChunkLevels &L = UPPER ? f.cp.up : f.cp.lo;
   const int *rows = (UPPER ? f.d_up_rows.p : f.d_lo_rows.p) + L.row_ptr[l];
@@ -400,40 +512,60 @@ static void solve_level(const Factor &f, const T *F, const TV *src, TV *y, int l
   const int *bound = UPPER ? f.d_row_ustart.p : f.d_row_lend.p;
   if (L.cta[l])
     k_pull_cta<T, TV, R, UPPER><<<dim3(nrows, L.split[l]), 256, 0, s>>>(
-        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, src, y);
+        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, y, y, t);
   else
     k_pull_warp<T, TV, R, UPPER><<<(nrows + 7) / 8, 256, 0, s>>>(
-        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, src, y);
+        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, y, y, t);
   nl++;
   const int nch = L.ch_ptr[l + 1] - L.ch_ptr[l];
   if (nch > 0) {
-    // staging for this level's largest chunk; small chunks take 64 threads
-    const int mr = L.max_rows[l];
-    const size_t smem = (size_t)6 * mr * R * sizeof(TV);
-    k_chunk_apply<T, TV, R, UPPER><<<nch, mr <= 16 ? 64 : (mr <= 48 ? 256 : 1024), smem, s>>>(
-        (UPPER ? f.d_up_chunks.p : f.d_lo_chunks.p) + L.ch_ptr[l], f.d_ck_c0.p, f.d_ck_off.p,
-        chunk_inverses<T>(f), y);
+    const int *chunks = (UPPER ? f.d_up_chunks.p : f.d_lo_chunks.p) + L.ch_ptr[l];
+    const int nbig = L.nbig[l], mr = L.max_rows[l];
+    const int S = nbig ? chunk_apply_split(nbig, mr, 6 / ApplyRows<R>::value) : 1;
+    const int blocks = nbig * S + (nch - nbig + 7) / 8;
+    const size_t smem =
+        (size_t)(nbig ? std::max(mr, 8 * APPLY_WARP_ROWS) : 8 * APPLY_WARP_ROWS) * 6 * R *
+        sizeof(TV);
+    k_chunk_apply<T, TV, R, UPPER><<<blocks, 256, smem, s>>>(
+        chunks, nch, nbig, S, f.d_ck_c0.p, f.d_ck_off.p, chunk_inverses<T>(f), t, y);
     nl++;
   }
 }
 
+// The scratch vector t of the solves (n x 6 x R values of TV), grown on
+// demand; growing it drops the captured solve graphs that refer to the old
+// buffer (never called while s is capturing).
+static int solve_scratch(Factor &f, size_t bytes) {
+  if (f.tvec.n >= bytes) return 0;
+  for (SolveGraph &g : f.graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  f.graphs.clear();
+  return f.tvec.alloc(bytes);
+}
+
 template <typename T, typename TV, int R>
-static int solve_levels_r(const Factor &f, const T *F, const TV *x, TV *y, cudaStream_t s,
+static int solve_levels_r(Factor &f, const T *F, const TV *x, TV *y, cudaStream_t s,
                           long long *launches) {
   long long nl = 0;
-  // the lower pulls subtract from y in place (split rows add atomically)
+  const size_t vb = (size_t)f.n * 6 * R * sizeof(TV);
+  int rc;
+  if ((rc = solve_scratch(f, vb))) return rc;
+  TV *t = reinterpret_cast<TV *>(f.tvec.p);
+  // the pulls subtract from y_i (one-row chunks) or t_i in place (split rows
+  // add atomically), so both start from x, then t from the lower result
   if ((const void *)x != (const void *)y)
-    A2DS_CUDA_TRY(cudaMemcpyAsync(y, x, (size_t)f.n * 6 * R * sizeof(TV),
-                                  cudaMemcpyDeviceToDevice, s));
-  for (int l = 0; l < f.cp.lo.nlevels; l++) solve_level<T, TV, R, false>(f, F, y, y, l, s, nl);
-  for (int l = 0; l < f.cp.up.nlevels; l++) solve_level<T, TV, R, true>(f, F, y, y, l, s, nl);
+    A2DS_CUDA_TRY(cudaMemcpyAsync(y, x, vb, cudaMemcpyDeviceToDevice, s));
+  A2DS_CUDA_TRY(cudaMemcpyAsync(t, y, vb, cudaMemcpyDeviceToDevice, s));
+  for (int l = 0; l < f.cp.lo.nlevels; l++) solve_level<T, TV, R, false>(f, F, y, t, l, s, nl);
+  A2DS_CUDA_TRY(cudaMemcpyAsync(t, y, vb, cudaMemcpyDeviceToDevice, s));
+  for (int l = 0; l < f.cp.up.nlevels; l++) solve_level<T, TV, R, true>(f, F, y, t, l, s, nl);
   if (launches) *launches += nl;
   A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
 template <typename T, typename TV>
-int solve_levels(const Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
+int solve_levels(Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_t s,
                  long long *launches) {
   switch (nrhs) {
     case 1: return solve_levels_r<T, TV, 1>(f, F, x, y, s, launches);
@@ -457,6 +589,8 @@ int solve_graph(Factor &f, const T *F, const TV *x, TV *y, int nrhs, cudaStream_
     }
   long long nl = 0;
   cudaGraph_t graph = nullptr;
+  int rc0;
+  if ((rc0 = solve_scratch(f, (size_t)f.n * 6 * nrhs * sizeof(TV)))) return rc0;
   A2DS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = solve_levels<T, TV>(f, F, x, y, nrhs, s, &nl);
   cudaError_t e = cudaStreamEndCapture(s, &graph);
@@ -486,9 +620,9 @@ Factor::~Factor() {
     if (g.exec) cudaGraphExecDestroy(g.exec);
 }
 
-template int solve_levels<double, double>(const Factor &, const double *, const double *, double *,
+template int solve_levels<double, double>(Factor &, const double *, const double *, double *,
                                           int, cudaStream_t, long long *);
-template int solve_levels<float, float>(const Factor &, const float *, const float *, float *, int,
+template int solve_levels<float, float>(Factor &, const float *, const float *, float *, int,
                                         cudaStream_t, long long *);
 template int solve_graph<double, double>(Factor &, const double *, const double *, double *, int,
                                          cudaStream_t, long long *);
