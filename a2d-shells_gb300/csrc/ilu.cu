@@ -335,24 +335,31 @@ void build_solve_schedule(Factor &f) {
     L.max_rows.assign(L.nlevels, 1);
     for (int c = 0; c < nc; c++)
       L.max_rows[lev[c]] = std::max(L.max_rows[lev[c]], cp.c0[c + 1] - cp.c0[c]);
-    L.cta.assign(L.nlevels, 0);
-    L.split.assign(L.nlevels, 1);
+    // pull segments, level by level in row order
+    L.seg_ptr.assign(1, 0);
+    L.seg_row.clear();
+    L.seg_kb.clear();
+    L.seg_ke.clear();
+    L.seg_flag.clear();
+    L.fin_ptr.assign(1, 0);
+    L.fin_rows.clear();
     for (int l = 0; l < L.nlevels; l++) {
-      int maxlen = 0;
-      bool single = false;
       for (int k = L.row_ptr[l]; k < L.row_ptr[l + 1]; k++) {
         const int i = L.rows[k];
-        const int len = upper ? f.frowp[i + 1] - cp.row_ustart[i] : cp.row_lend[i] - f.frowp[i];
-        maxlen = std::max(maxlen, len);
-        single = single || cp.row_single[i];
+        const int kb = upper ? cp.row_ustart[i] : f.frowp[i];
+        const int ke = upper ? f.frowp[i + 1] : cp.row_lend[i];
+        const int len = ke - kb;
+        const int nseg = std::max(1, (len + SOLVE_SEG - 1) / SOLVE_SEG);
+        for (int q = 0; q < nseg; q++) {
+          L.seg_row.push_back(i);
+          L.seg_kb.push_back(kb + q * SOLVE_SEG);
+          L.seg_ke.push_back(std::min(ke, kb + (q + 1) * SOLVE_SEG));
+          L.seg_flag.push_back(nseg > 1 ? 1 : 0);
+        }
+        if (upper && nseg > 1 && cp.row_single[i]) L.fin_rows.push_back(i);
       }
-      L.cta[l] = maxlen > SOLVE_LONG_ROW;
-      // long rows of levels with few rows: split over CTAs (atomic partial
-      // sums), except upper rows that are their own chunk (finished by
-      // D^{-1} after the full sum)
-      const int nr = L.row_ptr[l + 1] - L.row_ptr[l];
-      if (L.cta[l] && nr < 4 * 152 && !(upper && single))
-        L.split[l] = std::min(SOLVE_SPLIT_MAX, std::max(1, maxlen / SOLVE_SPLIT_BLOCKS));
+      L.seg_ptr.push_back((int)L.seg_row.size());
+      L.fin_ptr.push_back((int)L.fin_rows.size());
     }
   };
   fill_levels(lv, maxl, false, cp.lo);
@@ -375,10 +382,18 @@ int upload_schedules(Factor &f, cudaStream_t s) {
   if ((rc = f.d_row_lend.upload(cp.row_lend.data(), cp.row_lend.size(), s))) return rc;
   if ((rc = f.d_row_ustart.upload(cp.row_ustart.data(), cp.row_ustart.size(), s))) return rc;
   if ((rc = f.d_row_single.upload(cp.row_single.data(), cp.row_single.size(), s))) return rc;
-  if ((rc = f.d_lo_rows.upload(cp.lo.rows.data(), cp.lo.rows.size(), s))) return rc;
   if ((rc = f.d_lo_chunks.upload(cp.lo.chunks.data(), cp.lo.chunks.size(), s))) return rc;
-  if ((rc = f.d_up_rows.upload(cp.up.rows.data(), cp.up.rows.size(), s))) return rc;
   if ((rc = f.d_up_chunks.upload(cp.up.chunks.data(), cp.up.chunks.size(), s))) return rc;
+  if ((rc = f.d_lo_seg_row.upload(cp.lo.seg_row.data(), cp.lo.seg_row.size(), s)) ||
+      (rc = f.d_lo_seg_kb.upload(cp.lo.seg_kb.data(), cp.lo.seg_kb.size(), s)) ||
+      (rc = f.d_lo_seg_ke.upload(cp.lo.seg_ke.data(), cp.lo.seg_ke.size(), s)) ||
+      (rc = f.d_lo_seg_flag.upload(cp.lo.seg_flag.data(), cp.lo.seg_flag.size(), s)) ||
+      (rc = f.d_up_seg_row.upload(cp.up.seg_row.data(), cp.up.seg_row.size(), s)) ||
+      (rc = f.d_up_seg_kb.upload(cp.up.seg_kb.data(), cp.up.seg_kb.size(), s)) ||
+      (rc = f.d_up_seg_ke.upload(cp.up.seg_ke.data(), cp.up.seg_ke.size(), s)) ||
+      (rc = f.d_up_seg_flag.upload(cp.up.seg_flag.data(), cp.up.seg_flag.size(), s)) ||
+      (rc = f.d_up_fin.upload(cp.up.fin_rows.data(), cp.up.fin_rows.size(), s)))
+    return rc;
   if ((rc = f.d_ck_small.upload(cp.small.data(), cp.small.size(), s))) return rc;
   if ((rc = f.d_ck_big.upload(cp.big.data(), cp.big.size(), s))) return rc;
   const PanelSchedule &pn = f.pn;

@@ -53,18 +53,24 @@ struct PanelSchedule {
 // the numeric factorization); the chunk's other factor blocks point to
 // earlier chunks (lower) or later ones (upper).  Chunks are scheduled by
 // dependency levels over those external columns: one launch pulls the
-// external sums of every row of the level, one applies the chunk inverses.
+// external sums of every row of the level (each row's external blocks cut
+// into segments of at most SOLVE_SEG blocks, one warp per segment, the
+// segments of one row adding atomically), one applies the chunk inverses.
 // On the AMD-ordered cylinders this gives 16 levels at 256x512 and 43 at
 // 512x1024 (CHUNK_MAX 128), against 1,893 and 3,810 row levels.
 struct ChunkLevels {
   int nlevels = 0;
   std::vector<int> row_ptr, rows;   // rows of each level
+  // pull segments of each level: row, block range [kb, ke), flags (bit 0:
+  // the row has more than one segment, so they add atomically)
+  std::vector<int> seg_ptr, seg_row, seg_kb, seg_ke, seg_flag;
+  // upper levels: one-row chunks whose pull is segmented, finished by the
+  // apply launch (y_i = D_i^{-1} t_i)
+  std::vector<int> fin_ptr, fin_rows;
   std::vector<int> ch_ptr, chunks;  // chunks of >= 2 rows of each level, those of more
                                     // than APPLY_WARP_ROWS rows first
   std::vector<int> nbig;            // per level: chunks of more than APPLY_WARP_ROWS rows
-  std::vector<char> cta;            // per level: 1 = one CTA per row (long rows)
   std::vector<int> max_rows;        // per level: rows of its largest chunk
-  std::vector<int> split;           // per level: CTAs sharing each long row (1 = none)
 };
 struct ChunkPlan {
   std::vector<int> c0;          // chunk starts (nchunks + 1 entries, last = n)
@@ -102,7 +108,9 @@ struct Factor {
   ChunkPlan cp;
   DBuf<int> d_ck_c0, d_row_lend, d_row_ustart, d_row_single;
   DBuf<long long> d_ck_off;
-  DBuf<int> d_lo_rows, d_lo_chunks, d_up_rows, d_up_chunks, d_ck_small, d_ck_big;
+  DBuf<int> d_lo_chunks, d_up_chunks, d_ck_small, d_ck_big;
+  DBuf<int> d_lo_seg_row, d_lo_seg_kb, d_lo_seg_ke, d_lo_seg_flag;
+  DBuf<int> d_up_seg_row, d_up_seg_kb, d_up_seg_ke, d_up_seg_flag, d_up_fin;
   DBuf<double> cinv64, cscr64;  // FP64 inverses (all precisions) and gathered blocks
   DBuf<float> cinv32;           // FP32 copy of the inverses for FP32 factors
   DBuf<unsigned char> tvec;     // solve scratch: the pulled sums of chunk rows
@@ -146,14 +154,10 @@ constexpr long long PANEL_TABLE_MAX = 1LL << 28;
 // union U columns of a panel staged in shared memory by its phase-2 kernel
 constexpr int PANEL_UC_SMEM = 8192;
 
-// Largest chunk of the solves (block rows), and the row length above which
-// a pull level uses one CTA per row.
+// Largest chunk of the solves (block rows), and the factor blocks of one
+// pull segment (one warp: five groups of six lanes, two blocks per step).
 constexpr int CHUNK_MAX = 128;
-constexpr int SOLVE_LONG_ROW = 24;
-// factor blocks per CTA when a level's long rows are split over CTAs, and
-// the largest split
-constexpr int SOLVE_SPLIT_BLOCKS = 192;
-constexpr int SOLVE_SPLIT_MAX = 64;
+constexpr int SOLVE_SEG = 40;
 // chunks of at most this many rows are applied one warp per chunk
 constexpr int APPLY_WARP_ROWS = 16;
 

@@ -68,46 +68,54 @@ __device__ __forceinline__ void row_partial(int kb, int ke, int g, int step, int
   }
 }
 
-// r_i = src_i - sum_{k in [beg_i, end_i)} F_k y_{fcols[k]} for every row of
-// a level, one warp per row (five groups of six lanes over the blocks),
-// stored in t_i for rows of multi-row chunks and in y_i for rows that are
-// their own chunk; in the upper solve (UPPER) such a row is finished here:
-// y_i = D_i^{-1} r_i.  Lower: beg = frowp, end = row_lend; upper: beg =
-// row_ustart, end = frowp + 1; src = y (holding x, then the lower result).
+// The pull of one level, one warp per segment (a row's external blocks
+// [kb, ke), at most SOLVE_SEG of them; five groups of six lanes over the
+// blocks): v = sum_k F_k y_{fcols[k]} over the segment, then for the
+// segment's row i
+//   one segment:  r_i = src_i - v, stored in t_i (rows of multi-row chunks)
+//                 or y_i (one-row chunks; upper: y_i = D_i^{-1} r_i);
+//   several:      each segment subtracts v atomically from t_i, or from y_i
+//                 for a lower one-row chunk; both start as copies of src
+//                 (an upper one-row chunk is then finished by the apply
+//                 launch: y_i = D_i^{-1} t_i).
+// Lower: blocks [frowp, row_lend); upper: [row_ustart, frowp + 1); src = y
+// (holding x, then the lower result).
 template <typename T, typename TV, int R, bool UPPER>
-__global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows, int nrows,
-                                                   const int *__restrict__ frowp,
-                                                   const int *__restrict__ bound,
-                                                   const int *__restrict__ single,
-                                                   const int *__restrict__ fcols,
-                                                   const int *__restrict__ fdiag,
-                                                   const T *__restrict__ F, const TV *src, TV *y,
-                                                   TV *t) {
+__global__ void __launch_bounds__(256) k_pull_seg(const int *__restrict__ seg_row,
+                                                  const int *__restrict__ seg_kb,
+                                                  const int *__restrict__ seg_ke,
+                                                  const int *__restrict__ seg_flag, int nseg,
+                                                  const int *__restrict__ single,
+                                                  const int *__restrict__ fcols,
+                                                  const int *__restrict__ fdiag,
+                                                  const T *__restrict__ F, const TV *src, TV *y,
+                                                  TV *t) {
   __shared__ TV part[8][30][R];
   __shared__ TV z[8][6][R];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wr = blockIdx.x * 8 + wib;
-  if (wr >= nrows) return;  // whole warp leaves together
-  const int i = rows[wr];
+  const int sg = blockIdx.x * 8 + wib;
+  if (sg >= nseg) return;  // whole warp leaves together
+  const int i = seg_row[sg];
   const int g = lane / 6, ii = lane - 6 * g;
-  const int kb = UPPER ? bound[i] : frowp[i];
-  const int ke = UPPER ? frowp[i + 1] : bound[i];
   TV acc[R];
 #pragma unroll
   for (int r = 0; r < R; r++) acc[r] = 0;
-  if (lane < 30) row_partial<T, TV, R>(kb, ke, g, 5, ii, fcols, F, y, acc);
+  if (lane < 30) row_partial<T, TV, R>(seg_kb[sg], seg_ke[sg], g, 5, ii, fcols, F, y, acc);
   if (lane < 30)
 #pragma unroll
     for (int r = 0; r < R; r++) part[wib][lane][r] = acc[r];
   __syncwarp();
-  const bool one = single[i], fin = UPPER && one;
-  TV *dst = one ? y : t;
+  const bool one = single[i], multi = seg_flag[sg] & 1;
+  const bool fin = UPPER && one && !multi;
+  TV *dst = (one && !(UPPER && multi)) ? y : t;
   for (int o = lane; o < 6 * R; o += 32) {
     const int d = o / R, r = o - R * d;
     const TV v = part[wib][d][r] + part[wib][d + 6][r] + part[wib][d + 12][r] +
                  part[wib][d + 18][r] + part[wib][d + 24][r];
     const size_t idx = ((size_t)i * 6 + d) * R + r;
-    if (fin)
+    if (multi)
+      atomicAdd(&dst[idx], -v);
+    else if (fin)
       z[wib][d][r] = src[idx] - v;
     else
       dst[idx] = src[idx] - v;
@@ -120,70 +128,6 @@ __global__ void __launch_bounds__(256) k_pull_warp(const int *__restrict__ rows,
     TV v = 0;
 #pragma unroll
     for (int c = 0; c < 6; c++) v += (TV)Dinv[6 * d + c] * z[wib][c][r];
-    y[((size_t)i * 6 + d) * R + r] = v;
-  }
-}
-
-// The same for levels with long rows: one 256-thread CTA per row, 42 groups
-// of six threads over the row's blocks.  With split > 1 a row's blocks are
-// shared by gridDim.y CTAs that subtract their partial sums from its t_i or
-// y_i with atomic adds (which already hold src_i; not for rows finished with
-// D_i^{-1}).
-template <typename T, typename TV, int R, bool UPPER>
-__global__ void __launch_bounds__(256) k_pull_cta(const int *__restrict__ rows, int nrows,
-                                                  const int *__restrict__ frowp,
-                                                  const int *__restrict__ bound,
-                                                  const int *__restrict__ single,
-                                                  const int *__restrict__ fcols,
-                                                  const int *__restrict__ fdiag,
-                                                  const T *__restrict__ F, const TV *src, TV *y,
-                                                  TV *t) {
-  __shared__ TV part[252][R];
-  __shared__ TV z[6][R];
-  const int rr = blockIdx.x;
-  if (rr >= nrows) return;
-  const int i = rows[rr];
-  const int tid = threadIdx.x;
-  const int g = tid / 6, ii = tid - 6 * g;
-  int kb = UPPER ? bound[i] : frowp[i];
-  int ke = UPPER ? frowp[i + 1] : bound[i];
-  const int split = gridDim.y;
-  if (split > 1) {
-    const int per = (ke - kb + split - 1) / split;
-    kb += per * blockIdx.y;
-    ke = min(ke, kb + per);
-  }
-  if (tid < 252) {
-    TV acc[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) acc[r] = 0;
-    row_partial<T, TV, R>(kb, ke, g, 42, ii, fcols, F, y, acc);
-#pragma unroll
-    for (int r = 0; r < R; r++) part[tid][r] = acc[r];
-  }
-  __syncthreads();
-  const bool one = single[i], fin = UPPER && one;
-  TV *dst = one ? y : t;
-  for (int o = tid; o < 6 * R; o += blockDim.x) {
-    const int d = o / R, r = o - R * d;
-    TV v = 0;
-    for (int gg = 0; gg < 42; gg++) v += part[6 * gg + d][r];
-    const size_t idx = ((size_t)i * 6 + d) * R + r;
-    if (split > 1)
-      atomicAdd(&dst[idx], -v);
-    else if (fin)
-      z[d][r] = src[idx] - v;
-    else
-      dst[idx] = src[idx] - v;
-  }
-  if (!fin || split > 1) return;
-  __syncthreads();
-  const T *Dinv = F + (size_t)fdiag[i] * 36;
-  for (int o = tid; o < 6 * R; o += blockDim.x) {
-    const int d = o / R, r = o - R * d;
-    TV v = 0;
-#pragma unroll
-    for (int c = 0; c < 6; c++) v += (TV)Dinv[6 * d + c] * z[c][r];
     y[((size_t)i * 6 + d) * R + r] = v;
   }
 }
@@ -286,16 +230,35 @@ __device__ __forceinline__ void apply_rows(const T *__restrict__ Inv, int w, int
 // units of ROWS rows of one block row, unit u = split + S (warp + 8 k)
 // (interleaved, so the short and long block rows of the triangular inverse
 // spread evenly).  The small chunks follow, one warp per chunk and eight
-// per CTA, each warp staging its own chunk.
+// per CTA, each warp staging its own chunk; then the upper solve's one-row
+// chunks whose pulls were segmented (fin), one warp each.
 template <typename T, typename TV, int R, bool UPPER>
 __global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2)
     k_chunk_apply(const int *__restrict__ chunks, int nch, int nbig, int S,
                   const int *__restrict__ c0, const long long *__restrict__ off,
-                  const T *__restrict__ inv, const TV *__restrict__ t, TV *__restrict__ y) {
+                  const T *__restrict__ inv, const TV *__restrict__ t, TV *__restrict__ y,
+                  const int *__restrict__ fin, int nfin, const int *__restrict__ fdiag,
+                  const T *__restrict__ F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int PER = 6 / ApplyRows<R>::value;  // units per block row
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nsmall = (nch - nbig + 7) / 8;
   const int b = blockIdx.x;
+  if (b >= nbig * S + nsmall) {
+    // one-row chunks of the upper solve with segmented pulls: y_i = D_i^{-1} t_i
+    const int fi = (b - nbig * S - nsmall) * 8 + warp;
+    if (fi >= nfin) return;
+    const int i = fin[fi];
+    const T *Dinv = F + (size_t)fdiag[i] * 36;
+    for (int o = lane; o < 6 * R; o += 32) {
+      const int d = o / R, r = o - R * d;
+      TV v = 0;
+#pragma unroll
+      for (int c = 0; c < 6; c++) v += (TV)Dinv[6 * d + c] * t[((size_t)i * 6 + c) * R + r];
+      y[((size_t)i * 6 + d) * R + r] = v;
+    }
+    return;
+  }
   if (b < nbig * S) {
     TV *sv = reinterpret_cast<TV *>(smem_raw);
     const int c = chunks[b / S], split = b % S;
@@ -507,27 +470,29 @@ template <typename T, typename TV, int R, bool UPPER>
 static void solve_level(const Factor &f, const T *F, TV *y, TV *t, int l, cudaStream_t s,
                         long long &nl) {
   const ChunkLevels &L = UPPER ? f.cp.up : f.cp.lo;
-  const int *rows = (UPPER ? f.d_up_rows.p : f.d_lo_rows.p) + L.row_ptr[l];
-  const int nrows = L.row_ptr[l + 1] - L.row_ptr[l];
-  const int *bound = UPPER ? f.d_row_ustart.p : f.d_row_lend.p;
-  if (L.cta[l])
-    k_pull_cta<T, TV, R, UPPER><<<dim3(nrows, L.split[l]), 256, 0, s>>>(
-        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, y, y, t);
-  else
-    k_pull_warp<T, TV, R, UPPER><<<(nrows + 7) / 8, 256, 0, s>>>(
-        rows, nrows, f.d_frowp.p, bound, f.d_row_single.p, f.d_fcols.p, f.d_fdiag.p, F, y, y, t);
-  nl++;
+  const int s0 = L.seg_ptr[l], nseg = L.seg_ptr[l + 1] - s0;
+  if (nseg > 0) {
+    k_pull_seg<T, TV, R, UPPER><<<(nseg + 7) / 8, 256, 0, s>>>(
+        (UPPER ? f.d_up_seg_row.p : f.d_lo_seg_row.p) + s0,
+        (UPPER ? f.d_up_seg_kb.p : f.d_lo_seg_kb.p) + s0,
+        (UPPER ? f.d_up_seg_ke.p : f.d_lo_seg_ke.p) + s0,
+        (UPPER ? f.d_up_seg_flag.p : f.d_lo_seg_flag.p) + s0, nseg, f.d_row_single.p,
+        f.d_fcols.p, f.d_fdiag.p, F, y, y, t);
+    nl++;
+  }
   const int nch = L.ch_ptr[l + 1] - L.ch_ptr[l];
-  if (nch > 0) {
+  const int f0 = UPPER ? L.fin_ptr[l] : 0, nfin = UPPER ? L.fin_ptr[l + 1] - f0 : 0;
+  if (nch > 0 || nfin > 0) {
     const int *chunks = (UPPER ? f.d_up_chunks.p : f.d_lo_chunks.p) + L.ch_ptr[l];
     const int nbig = L.nbig[l], mr = L.max_rows[l];
     const int S = nbig ? chunk_apply_split(nbig, mr, 6 / ApplyRows<R>::value) : 1;
-    const int blocks = nbig * S + (nch - nbig + 7) / 8;
+    const int blocks = nbig * S + (nch - nbig + 7) / 8 + (nfin + 7) / 8;
     const size_t smem =
         (size_t)(nbig ? std::max(mr, 8 * APPLY_WARP_ROWS) : 8 * APPLY_WARP_ROWS) * 6 * R *
         sizeof(TV);
     k_chunk_apply<T, TV, R, UPPER><<<blocks, 256, smem, s>>>(
-        chunks, nch, nbig, S, f.d_ck_c0.p, f.d_ck_off.p, chunk_inverses<T>(f), t, y);
+        chunks, nch, nbig, S, f.d_ck_c0.p, f.d_ck_off.p, chunk_inverses<T>(f), t, y,
+        UPPER ? f.d_up_fin.p + f0 : nullptr, nfin, f.d_fdiag.p, F);
     nl++;
   }
 }
