@@ -137,8 +137,19 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
         long long e = p;
         while (e < cnt[l + 1] && bucket_row[e] == bucket_row[p]) e++;
         const int i = bucket_row[p];
+        // a long target row takes a CTA only when its task has enough block
+        // updates to fill one; small tasks on long rows (the leaf levels'
+        // updates of the top separators' rows) go to the warp-group kernel,
+        // which searches the row's columns in global memory
+        long long work = 0;
+        if (pk < 0 && f.frowp[i + 1] - f.frowp[i] > FACTOR_WARP_COLS)
+          for (long long q = p; q < e; q++) {
+            const int j = f.fcols[bucket_jp[q]];
+            work += f.frowp[j + 1] - f.fdiag[j] - 1;
+          }
         const bool first = pk >= 0 ? in_panel_rows[i] != 0
-                                   : f.frowp[i + 1] - f.frowp[i] > FACTOR_WARP_COLS;
+                                   : (f.frowp[i + 1] - f.frowp[i] > FACTOR_WARP_COLS &&
+                                      work >= FACTOR_LONG_WORK);
         if (first == (pass == 0)) {
           f.task_row.push_back(i);
           for (long long q = p; q < e; q++) f.task_jp.push_back(bucket_jp[q]);

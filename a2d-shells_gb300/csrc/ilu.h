@@ -137,10 +137,14 @@ int chunk_alloc(Factor &f);
 // invert its unit-lower and D + U parts (after the numeric factorization).
 int chunk_build(Factor &f, const void *F, cudaStream_t s, long long *launches);
 
-// Update kernels: target rows with at most FACTOR_WARP_COLS blocks are
-// updated by a group of 6, 12 or 30 lanes, longer ones by one CTA (column
-// indices staged in shared memory up to FACTOR_CTA_COLS).
+// Update kernels: tasks on target rows with at most FACTOR_WARP_COLS
+// blocks, or with fewer than FACTOR_LONG_WORK block updates, go to a group
+// of 6, 12 or 30 lanes; the rest to one CTA each (column indices staged in
+// shared memory up to FACTOR_CTA_COLS).
 constexpr int FACTOR_WARP_COLS = 512;
+// block updates below which a task on a long target row still goes to the
+// warp-group kernel (a 384-thread CTA applies 64 block updates at a time)
+constexpr long long FACTOR_LONG_WORK = 256;
 constexpr int FACTOR_CTA_COLS = 10240;
 // at most this many CTAs share one single-pivot long update task
 constexpr int FACTOR_MAX_SPLIT = 8;

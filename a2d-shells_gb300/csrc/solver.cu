@@ -31,6 +31,7 @@
 
 #include "a2ds_internal.h"
 #include "block.h"
+#include "df64.h"
 #include "host_graph.h"
 #include "ilu.h"
 #include "kernels.h"
@@ -387,6 +388,10 @@ constexpr int GMRES_IR_CYCLES = 8;
 // preconditioned blocks Z (msub), small device coefficients H.
 struct IrWork {
   DBuf<double> V, Z, H;
+  // double-float inner GMRES (fgmres_df_solve): Arnoldi blocks, FP32
+  // preconditioned blocks, the FP64 residual block, coefficient scratch
+  DBuf<df64> Vd, Zd, hs;
+  DBuf<double> R;
   int iters = 0, cycles = 0;  // Arnoldi steps and cycles, accumulated
 };
 
@@ -412,6 +417,11 @@ struct BucklingState {
   DBuf<double> AQ, dT, dHd, Yd, AYd, dCinv, dYc, dSk;
   std::vector<double> Cq;
   int defl_k = 0;
+  // the double-float inner solves: K + sigma G as df64, the deflation
+  // vectors as FP32 with A Y as df64, the deflation residual
+  DBuf<df64> AuxDF, AYdf, Tdf;
+  DBuf<float> Yf;
+  bool use_df = false;
   std::vector<double> lam, err, ritz;  // converged data
   int nconv = 0;
   double sigma = 0.0;
@@ -730,6 +740,174 @@ static int solve_k(Mesh &m, BucklingState &S, Factor &f, const double *Avals, co
                               inner);
   }
   return refined_block_solve(m, S, f, Avals, b, x, 1, rtol, 4, inner);
+}
+
+// y = -Cinv h (k x p; h, y laid out [(b p + c1) p + c2] as blk_dots writes
+// and blk_sub reads), one thread per entry.
+__global__ void k_defl_coef(const double *__restrict__ Ci, const double *__restrict__ h,
+                            double *__restrict__ y, int k, int p) {
+  const int t = threadIdx.x;
+  if (t >= k * p) return;
+  const int i = t / p, c = t - i * p;
+  double acc = 0.0;
+  for (int q = 0; q < k; q++) acc += Ci[(size_t)i * k + q] * h[(size_t)q * p + c];
+  y[t] = -acc;
+}
+
+// GMRES-IR with a double-float inner loop: the FP32 factor f inside p
+// flexible GMRES(msub) solves in lockstep, as fgmres_block_solve, but with
+// the Arnoldi vectors, the preconditioned vectors and the shifted operator
+// S.AuxDF in df64 (krylov_df.cu; the product A z reads the FP32 factor's
+// output itself), so the per-step products and Gram-Schmidt passes run on
+// the FP32 pipe.  The solution Y and the
+// residual X - A Y that starts every cycle and decides convergence are FP64
+// (S.Aux).  With S.defl_k > 0 each preconditioned block is deflated by the
+// Ritz vectors (S.Yf, S.AYdf) as in defl_correct.
+static int fgmres_df_solve(Mesh &m, BucklingState &S, Factor &f, const double *X, double *Y,
+                           int p, double rtol, int msub, int max_cycles, int *iters) {
+  const size_t n6 = (size_t)m.nn * 6, bs = n6 * p;
+  const int ld = msub + 1;
+  IrWork &W = S.ir;
+  int rc;
+  if (msub < 1 || msub > 63) return fail(A2DS_ERR_ARG, "GMRES-IR subspace must be 1..63");
+  if ((W.Vd.n < (size_t)(msub + 1) * bs && (rc = W.Vd.alloc((size_t)(msub + 1) * bs))) ||
+      (W.Zd.n < (size_t)msub * bs && (rc = W.Zd.alloc((size_t)msub * bs))) ||
+      (W.R.n < bs && (rc = W.R.alloc(bs))) || (W.hs.n < 64 * 16 && (rc = W.hs.alloc(64 * 16))) ||
+      (W.H.n < (size_t)(2 * ld + 1) * p && (rc = W.H.alloc((size_t)(2 * ld + 1) * p))) ||
+      (S.gw32.n < bs && (rc = S.gw32.alloc(bs))))
+    return rc;
+  double *dH1 = W.H.p, *dH2 = W.H.p + (size_t)ld * p, *dN = W.H.p + (size_t)2 * ld * p;
+  std::vector<double> xn(p, 0.0), nrm2(p), h1((size_t)ld * p), h2((size_t)ld * p);
+  std::vector<double> H((size_t)p * ld * msub), g((size_t)p * ld), qc((size_t)p * msub),
+      qs((size_t)p * msub), yv((size_t)msub * p);
+  auto Hc = [&](int c, int row, int col) -> double & {
+    return H[((size_t)c * msub + col) * ld + row];
+  };
+  A2DS_CUDA_TRY(cudaMemsetAsync(Y, 0, bs * sizeof(double), m.stream));
+  A2DS_CUDA_TRY(cudaMemcpyAsync(W.R.p, X, bs * sizeof(double), cudaMemcpyDeviceToDevice,
+                                m.stream));
+  double prev_worst = 0.0;
+  bool estimates_met = false;
+  for (int cyc = 0;; cyc++) {
+    if ((rc = col_dots(W.R.p, 1, bs, W.R.p, n6, p, dN, m.stream))) return rc;
+    A2DS_CUDA_TRY(cudaMemcpyAsync(nrm2.data(), dN, p * sizeof(double), cudaMemcpyDeviceToHost,
+                                  m.stream));
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+    m.launches++;
+    if (cyc == 0)
+      for (int c = 0; c < p; c++) xn[c] = sqrt(nrm2[c]);
+    bool done = true;
+    double worst = 0.0;
+    for (int c = 0; c < p; c++) {
+      if (!(sqrt(nrm2[c]) <= rtol * xn[c])) done = false;
+      if (xn[c] > 0.0) worst = std::max(worst, sqrt(nrm2[c]) / xn[c]);
+    }
+    if (!std::isfinite(worst)) return fail(A2DS_ERR_NUMERIC, "GMRES-IR residual is not finite");
+    if (done) return 0;
+    if (cyc > 0 && estimates_met && !(worst < 0.5 * prev_worst)) return 0;  // attainable floor
+    prev_worst = worst;
+    if (cyc == max_cycles) {
+      char msg[200];
+      snprintf(msg, sizeof msg,
+               "GMRES-IR did not reach the tolerance in %d cycles of %d steps (relative "
+               "residual %.3e, target %.3e, %d right-hand sides)",
+               max_cycles, msub, worst, rtol, p);
+      return fail(A2DS_ERR_NOCONV, msg);
+    }
+    S.ir.cycles++;
+    if ((rc = df_from_f64(W.Vd.p, W.R.p, bs, m.stream)) ||
+        (rc = df_col_unit(W.Vd.p, dN, n6, p, m.stream)))
+      return rc;
+    m.launches += 2;
+    std::fill(H.begin(), H.end(), 0.0);
+    std::fill(g.begin(), g.end(), 0.0);
+    for (int c = 0; c < p; c++) g[(size_t)c * ld] = sqrt(nrm2[c]);
+    int nit = 0;
+    for (int j = 0; j < msub; j++) {
+      df64 *Vj = W.Vd.p + (size_t)j * bs, *Wd = W.Vd.p + (size_t)(j + 1) * bs;
+      df64 *Zj = W.Zd.p + (size_t)j * bs;
+      // preconditioner: the FP32 rounding of V_j through the FP32 factor
+      A2DS_CUDA_TRY(cudaEventRecord(S.next_event(), m.stream));
+      if ((rc = df_hi(S.gw32.p, Vj, bs, m.stream))) return rc;
+      if ((rc = solve_graph<float, float>(f, f.F32.p, S.gw32.p, S.gw32.p, p, m.stream,
+                                          &m.launches)))
+        return rc;
+      A2DS_CUDA_TRY(cudaEventRecord(S.next_event(), m.stream));
+      if ((rc = df_from_f32(Zj, S.gw32.p, bs, m.stream)) ||
+          (rc = df_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.AuxDF.p, S.gw32.p, Wd, p, m.stream)))
+        return rc;
+      m.launches += 2;
+      if (S.defl_k > 0) {
+        // z += Y Cinv Y^T (v - A z), A z corrected with A Y
+        const int k = S.defl_k, kb = k / p;
+        if ((rc = df_diff(S.Tdf.p, Vj, Wd, bs, m.stream)) ||
+            (rc = df_blk_dots(S.Yf.p, kb, bs, S.Tdf.p, n6, p, S.dHd.p, m.stream)))
+          return rc;
+        k_defl_coef<<<1, 256, 0, m.stream>>>(S.dCinv.p, S.dHd.p, S.dYc.p, k, p);
+        if ((rc = df_defl_sub(Zj, S.Yf.p, Wd, S.AYdf.p, kb, bs, S.dYc.p, n6, p, m.stream)))
+          return rc;
+        m.launches += 4;
+      }
+      if ((rc = df_col_dots(W.Vd.p, j + 1, bs, Wd, n6, p, dH1, m.stream)) ||
+          (rc = df_col_axpy(Wd, W.Vd.p, j + 1, bs, dH1, n6, p, -1.0, W.hs.p, m.stream)) ||
+          (rc = df_col_dots(W.Vd.p, j + 1, bs, Wd, n6, p, dH2, m.stream)) ||
+          (rc = df_col_axpy(Wd, W.Vd.p, j + 1, bs, dH2, n6, p, -1.0, W.hs.p, m.stream)) ||
+          (rc = df_col_dots(Wd, 1, bs, Wd, n6, p, dN, m.stream)))
+        return rc;
+      A2DS_CUDA_TRY(cudaMemcpyAsync(h1.data(), dH1, (size_t)(j + 1) * p * sizeof(double),
+                                    cudaMemcpyDeviceToHost, m.stream));
+      A2DS_CUDA_TRY(cudaMemcpyAsync(h2.data(), dH2, (size_t)(j + 1) * p * sizeof(double),
+                                    cudaMemcpyDeviceToHost, m.stream));
+      A2DS_CUDA_TRY(cudaMemcpyAsync(nrm2.data(), dN, p * sizeof(double), cudaMemcpyDeviceToHost,
+                                    m.stream));
+      if ((rc = df_col_unit(Wd, dN, n6, p, m.stream))) return rc;
+      m.launches += 10;
+      A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));
+      nit = j + 1;
+      S.ir.iters++;
+      if (iters) (*iters)++;
+      bool conv = true;
+      for (int c = 0; c < p; c++) {
+        for (int k = 0; k <= j; k++) Hc(c, k, j) = h1[(size_t)k * p + c] + h2[(size_t)k * p + c];
+        Hc(c, j + 1, j) = sqrt(nrm2[c]);
+        double *qcc = qc.data() + (size_t)c * msub, *qsc = qs.data() + (size_t)c * msub;
+        for (int k = 0; k < j; k++) {
+          const double a = Hc(c, k, j), b = Hc(c, k + 1, j);
+          Hc(c, k, j) = a * qcc[k] + b * qsc[k];
+          Hc(c, k + 1, j) = -a * qsc[k] + b * qcc[k];
+        }
+        const double a = Hc(c, j, j), b = Hc(c, j + 1, j);
+        const double sq = sqrt(a * a + b * b);
+        qcc[j] = sq > 0.0 ? a / sq : 1.0;
+        qsc[j] = sq > 0.0 ? b / sq : 0.0;
+        Hc(c, j, j) = a * qcc[j] + b * qsc[j];
+        Hc(c, j + 1, j) = 0.0;
+        double *gc = g.data() + (size_t)c * ld;
+        const double r = gc[j];
+        gc[j] = r * qcc[j];
+        gc[j + 1] = -r * qsc[j];
+        if (!(fabs(gc[j + 1]) <= rtol * xn[c])) conv = false;
+      }
+      estimates_met = conv;
+      if (conv) break;
+    }
+    for (int c = 0; c < p; c++) {
+      const double *gc = g.data() + (size_t)c * ld;
+      for (int i = nit - 1; i >= 0; i--) {
+        double sum = gc[i];
+        for (int k = i + 1; k < nit; k++) sum -= Hc(c, i, k) * yv[(size_t)k * p + c];
+        const double d = Hc(c, i, i);
+        yv[(size_t)i * p + c] = d != 0.0 ? sum / d : 0.0;
+      }
+    }
+    A2DS_CUDA_TRY(cudaMemcpyAsync(dH1, yv.data(), (size_t)nit * p * sizeof(double),
+                                  cudaMemcpyHostToDevice, m.stream));
+    if ((rc = df_col_axpy_f64(Y, W.Zd.p, nit, bs, dH1, n6, p, m.stream))) return rc;
+    if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.Aux.p, Y, X, W.R.p, p, m.stream)))
+      return rc;
+    m.launches += 2;
+    A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // yv is pageable host memory
+  }
 }
 
 // K-orthonormalise the block W (with KW = K W): one Cholesky-QR pass,
@@ -1071,10 +1249,22 @@ static int defl_update_ritz(Mesh &m, BucklingState &S, const std::vector<double>
     for (int q = 0; q < k; q++) Sk[(size_t)r * k + q] = V[(size_t)r * mdim + order[q]];
   int rc;
   if ((rc = S.dSk.upload(Sk.data(), Sk.size(), m.stream))) return rc;
-  if ((rc = blk_mul(S.Q.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.Yd.p, m.stream)) ||
-      (rc = blk_mul(S.AQ.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.AYd.p, m.stream)))
-    return rc;
-  m.launches += 2;
+  if ((rc = blk_mul(S.Q.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.Yd.p, m.stream))) return rc;
+  m.launches++;
+  if (S.use_df) {
+    // the double-float inner solves deflate with the FP32 rounding of Y and
+    // A times exactly that
+    if ((rc = f64_to_f32(S.Yf.p, S.Yd.p, (size_t)(k / p) * bs, m.stream))) return rc;
+    for (int b = 0; b < k / p; b++)
+      if ((rc = df_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.AuxDF.p, S.Yf.p + (size_t)b * bs,
+                        S.AYdf.p + (size_t)b * bs, p, m.stream)))
+        return rc;
+    m.launches += 1 + k / p;
+  } else {
+    if ((rc = blk_mul(S.AQ.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.AYd.p, m.stream)))
+      return rc;
+    m.launches++;
+  }
   // Y^T A Y = Sk^T Cq Sk, inverted on its eigenvectors (|w| below 1e-12
   // max |w| dropped)
   std::vector<double> CS((size_t)mdim * k, 0.0), Cy((size_t)k * k, 0.0);
@@ -1107,17 +1297,6 @@ static int defl_update_ritz(Mesh &m, BucklingState &S, const std::vector<double>
   return 0;
 }
 
-// y = -Cinv h (k x p; h, y laid out [(b p + c1) p + c2] as blk_dots writes
-// and blk_sub reads), one thread per entry.
-__global__ void k_defl_coef(const double *__restrict__ Ci, const double *__restrict__ h,
-                            double *__restrict__ y, int k, int p) {
-  const int t = threadIdx.x;
-  if (t >= k * p) return;
-  const int i = t / p, c = t - i * p;
-  double acc = 0.0;
-  for (int q = 0; q < k; q++) acc += Ci[(size_t)i * k + q] * h[(size_t)q * p + c];
-  y[t] = -acc;
-}
 __global__ void k_diff(double *__restrict__ T, const double *__restrict__ V,
                        const double *__restrict__ AZ, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -1205,6 +1384,7 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
   // deflation of the GMRES-IR solves (FP32 factors only)
   const bool deflate = direct && S.fa.precision == 32;
   S.defl_k = 0;
+  S.use_df = deflate;
   if (deflate) {
     const int kb = DEFL_RITZ / p;
     if (DEFL_RITZ % p) return fail(A2DS_ERR_ARG, "deflation: block size must divide 16");
@@ -1214,6 +1394,13 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
         (rc = S.AYd.alloc((size_t)kb * bs)) || (rc = S.dCinv.alloc(DEFL_RITZ * DEFL_RITZ)) ||
         (rc = S.dYc.alloc(DEFL_RITZ * p)))
       return rc;
+    if (S.use_df) {
+      if ((rc = S.AuxDF.alloc(nv)) || (rc = S.Yf.alloc((size_t)kb * bs)) ||
+          (rc = S.AYdf.alloc((size_t)kb * bs)) || (rc = S.Tdf.alloc(bs)))
+        return rc;
+      if ((rc = df_from_f64(S.AuxDF.p, S.Aux.p, nv, m.stream))) return rc;
+      m.launches++;
+    }
     S.Cq.assign((size_t)tdim * tdim, 0.0);
     if ((rc = defl_add_block(m, S, B, 0, p, tdim))) return rc;
   }
@@ -1239,9 +1426,14 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
           az = true;
           return defl_correct(m, S, V, Z, AZ, p);
         };
-        if ((rc = fgmres_block_solve(m, S.ir, pc, S.Aux.p, KQj, W, p, rtol, GMRES_IR_MSUB,
-                                     GMRES_IR_CYCLES, &inner)))
+        if (S.use_df) {
+          if ((rc = fgmres_df_solve(m, S, S.fa, KQj, W, p, rtol, GMRES_IR_MSUB, GMRES_IR_CYCLES,
+                                    &inner)))
+            return rc;
+        } else if ((rc = fgmres_block_solve(m, S.ir, pc, S.Aux.p, KQj, W, p, rtol, GMRES_IR_MSUB,
+                                            GMRES_IR_CYCLES, &inner))) {
           return rc;
+        }
       } else if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, rtol, 2, &inner))) {
         return rc;
       }

@@ -178,7 +178,8 @@ struct alignas(N * sizeof(TV) >= 16 ? 16 : N * sizeof(TV)) Pack {
 
 // Rows of the inverse formed together by one warp: all six rows of a block
 // row share its column range, so the vector values loaded for a column are
-// used ROWS times (fewer for wide R to bound the accumulators).
+// used ROWS times (fewer for wide R to bound the accumulators).  Levels with
+// only a few large chunks use one row per warp instead, for more warps.
 template <int R>
 struct ApplyRows {
   static constexpr int value = R <= 4 ? 6 : (R == 8 ? 3 : 1);
@@ -193,11 +194,10 @@ struct ApplyRows {
 // offsets are even, so the paired loads are aligned.  The inverse is read
 // with the streaming hint: it is used once per solve and must not evict
 // the staged vectors' lines.
-template <typename T, typename TV, int R, bool UPPER>
+template <typename T, typename TV, int R, bool UPPER, int ROWS>
 __device__ __forceinline__ void apply_rows(const T *__restrict__ Inv, int w, int blk, int q0,
                                            const TV *sv, TV *yc, int lane) {
   using T2 = typename Pair<T>::type;
-  constexpr int ROWS = ApplyRows<R>::value;
   const int cb = UPPER ? 6 * blk : 0, ce = UPPER ? w : 6 * blk + 6;
   const T *I0 = Inv + (size_t)(6 * blk + q0) * w;
   TV acc[ROWS][R];
@@ -205,7 +205,8 @@ __device__ __forceinline__ void apply_rows(const T *__restrict__ Inv, int w, int
   for (int q = 0; q < ROWS; q++)
 #pragma unroll
     for (int r = 0; r < R; r++) acc[q][r] = 0;
-#pragma unroll 1
+  constexpr int UNR = ROWS == 1 ? 4 : 1;  // loads in flight per lane
+#pragma unroll UNR
   for (int col = cb + 2 * lane; col < ce; col += 64) {
     const Pack<TV, 2 * R> tv = *reinterpret_cast<const Pack<TV, 2 * R> *>(sv + (size_t)col * R);
 #pragma unroll
@@ -232,7 +233,7 @@ __device__ __forceinline__ void apply_rows(const T *__restrict__ Inv, int w, int
 // spread evenly).  The small chunks follow, one warp per chunk and eight
 // per CTA, each warp staging its own chunk; then the upper solve's one-row
 // chunks whose pulls were segmented (fin), one warp each.
-template <typename T, typename TV, int R, bool UPPER>
+template <typename T, typename TV, int R, bool UPPER, int ROWS>
 __global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2)
     k_chunk_apply(const int *__restrict__ chunks, int nch, int nbig, int S,
                   const int *__restrict__ c0, const long long *__restrict__ off,
@@ -240,7 +241,7 @@ __global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2)
                   const int *__restrict__ fin, int nfin, const int *__restrict__ fdiag,
                   const T *__restrict__ F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int PER = 6 / ApplyRows<R>::value;  // units per block row
+  constexpr int PER = 6 / ROWS;  // units per block row
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nsmall = (nch - nbig + 7) / 8;
   const int b = blockIdx.x;
@@ -269,8 +270,7 @@ __global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2)
     __syncthreads();
     TV *yc = y + (size_t)a * 6 * R;
     for (int u = split + S * warp; u < ns * PER; u += S * 8)
-      apply_rows<T, TV, R, UPPER>(Inv, w, u / PER, (u % PER) * ApplyRows<R>::value, sv, yc,
-                                  lane);
+      apply_rows<T, TV, R, UPPER, ROWS>(Inv, w, u / PER, (u % PER) * ROWS, sv, yc, lane);
     return;
   }
   const int ci = nbig + (b - nbig * S) * 8 + warp;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2)
   __syncwarp();
   TV *yc = y + (size_t)a * 6 * R;
   for (int u = 0; u < ns * PER; u++)
-    apply_rows<T, TV, R, UPPER>(Inv, w, u / PER, (u % PER) * ApplyRows<R>::value, sv, yc, lane);
+    apply_rows<T, TV, R, UPPER, ROWS>(Inv, w, u / PER, (u % PER) * ROWS, sv, yc, lane);
 }
 
 // Dense FP64 copy of every multi-row chunk's diagonal block out of the factor
@@ -378,9 +378,14 @@ __global__ void k_chunk_inverse(const int *__restrict__ chunks, const int *__res
 template <typename T, typename TV, int R>
 static int chunk_apply_config() {
   const int smem = std::max(CHUNK_MAX, 8 * APPLY_WARP_ROWS) * 6 * R * (int)sizeof(TV);
-  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, false>,
+  constexpr int RW = ApplyRows<R>::value;
+  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, false, RW>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, true>,
+  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, true, RW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, false, 1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  A2DS_CUDA_TRY(cudaFuncSetAttribute(k_chunk_apply<T, TV, R, true, 1>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   return 0;
 }
@@ -485,14 +490,22 @@ static void solve_level(const Factor &f, const T *F, TV *y, TV *t, int l, cudaSt
   if (nch > 0 || nfin > 0) {
     const int *chunks = (UPPER ? f.d_up_chunks.p : f.d_lo_chunks.p) + L.ch_ptr[l];
     const int nbig = L.nbig[l], mr = L.max_rows[l];
-    const int S = nbig ? chunk_apply_split(nbig, mr, 6 / ApplyRows<R>::value) : 1;
+    constexpr int RW = ApplyRows<R>::value;
+    // few large chunks: one row per warp (six times the warps)
+    const bool few = (long long)nbig * mr * (6 / RW) < 8LL * 4 * 152;
+    const int S = nbig ? chunk_apply_split(nbig, mr, few ? 6 : 6 / RW) : 1;
     const int blocks = nbig * S + (nch - nbig + 7) / 8 + (nfin + 7) / 8;
     const size_t smem =
         (size_t)(nbig ? std::max(mr, 8 * APPLY_WARP_ROWS) : 8 * APPLY_WARP_ROWS) * 6 * R *
         sizeof(TV);
-    k_chunk_apply<T, TV, R, UPPER><<<blocks, 256, smem, s>>>(
-        chunks, nch, nbig, S, f.d_ck_c0.p, f.d_ck_off.p, chunk_inverses<T>(f), t, y,
-        UPPER ? f.d_up_fin.p + f0 : nullptr, nfin, f.d_fdiag.p, F);
+    if (few)
+      k_chunk_apply<T, TV, R, UPPER, 1><<<blocks, 256, smem, s>>>(
+          chunks, nch, nbig, S, f.d_ck_c0.p, f.d_ck_off.p, chunk_inverses<T>(f), t, y,
+          UPPER ? f.d_up_fin.p + f0 : nullptr, nfin, f.d_fdiag.p, F);
+    else
+      k_chunk_apply<T, TV, R, UPPER, RW><<<blocks, 256, smem, s>>>(
+          chunks, nch, nbig, S, f.d_ck_c0.p, f.d_ck_off.p, chunk_inverses<T>(f), t, y,
+          UPPER ? f.d_up_fin.p + f0 : nullptr, nfin, f.d_fdiag.p, F);
     nl++;
   }
 }

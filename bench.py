@@ -138,6 +138,15 @@ PREC_NAME = {64: "FP64 factors", 48: "double-float (2 x FP32) factors with FP64 
              32: "FP32 factors and triangular solves inside FP64 GMRES-IR"}
 DTYPE = {64: "f64", 48: "df64 factor (2 x f32) + f64", 32: "f32 factor + f64"}
 
+# FP64 operations per element of the two assembly kernels (Quad4 linear
+# shell, K: shell_kernel<2, 0, 0>, G: shell_kernel<2, 1, 0>), counted by ncu
+# as DADD + DMUL + 2 DFMA thread instructions over a whole launch on the
+# 128x256 cylinder (32,768 elements) and divided by the elements; the same
+# capture shows the FP64 pipe active ~90 % of the cycles in both kernels
+# (profiles/shell_kernel_fp64_cylinder128x256.md).
+ASM_FP64_FLOPS_PER_ELEM = {"K": 42916, "G": 119624}
+ASM_FP64_PIPE_ACTIVE_PCT = {"K": 90.5, "G": 89.7}
+
 # DRAM traffic of one numeric factorization of the bench workload, summed
 # over all its launches from an ncu capture (profiles/factor_cylinder256x512_traffic.md)
 FACTOR_TRAFFIC = {(256, 512, 48): 279.65e9}
@@ -236,6 +245,26 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def assembly_roofline(m, stats, fp64_peak):
+    """The assembly kernels are bound by the FP64 pipe (GB300's FP64 rate is
+    ~1/60 of its FP32 rate): achieved FP64 rate = elements/s x the counted
+    FP64 operations per element, against the measured DGEMM rate (an upper
+    bound for FMA-only code; the element kernels also issue DADD/DMUL)."""
+    out = {"bound": "fp64 pipe", "peak_tflops": fp64_peak,
+           "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}
+    for key, t in (("K", stats["assemble_k_s"]), ("G", stats["assemble_g_s"])):
+        eps = m.num_elements / t
+        tf = eps * ASM_FP64_FLOPS_PER_ELEM[key] / 1e12
+        out[key] = {"elements_per_s": eps, "fp64_flops_per_element": ASM_FP64_FLOPS_PER_ELEM[key],
+                    "achieved_tflops": tf, "frac": (tf / fp64_peak) if fp64_peak else None,
+                    "fp64_pipe_active_pct_ncu": ASM_FP64_PIPE_ACTIVE_PCT[key]}
+    out["note"] = ("assemble_k_s / assemble_g_s include the launch and the host synchronisation "
+                   "around it; G costs ~2.8x K because its element work is 2.8x the FP64 "
+                   "operations (stresses at the load path plus the second derivatives of the "
+                   "nonlinear strain terms)")
+    return out
 
 
 def workload_sigma(m):
@@ -460,6 +489,7 @@ def main():
                     "trisolve_ms_total": stats["trisolve_ms"], "trisolve_calls": stats["trisolve_calls"]},
         "assembly_elems_per_s": {"K": m.num_elements / stats["assemble_k_s"],
                                  "G": m.num_elements / stats["assemble_g_s"]},
+        "assembly_roofline": assembly_roofline(m, stats, fp64),
         "eigvals": b.eigvals.tolist(), "eig_rel_drift_between_runs": lam_err,
         "eig_residual_max": float(np.max(b.errors)), "sigma": sigma,
         "eig_rel_err_vs_fp64": vs_fp64, "fp64_variant": fp64_variant,
