@@ -742,6 +742,29 @@ int factor_scatter(const Factor &f, int n, const int *rowp, const int *cols, con
   }
 }
 
+__global__ void k_df64_to_f32(float *__restrict__ out, const df64 *__restrict__ F, size_t n) {
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    const df64 v = F[k];
+    out[k] = __fadd_rn(v.hi, v.lo);  // the nearest FP32 value of hi + lo
+  }
+}
+
+int factor_df_to_f32(const Factor &f, int n, const int *rowp, const int *cols, const double *A,
+                     const double *A2, double alpha2, void *work, float *F32, int *status,
+                     cudaStream_t s, long long *launches) {
+  df64 *Fd = (df64 *)work;
+  int rc;
+  if ((rc = scatter_t<df64>(n, rowp, cols, A, A2, alpha2, f.d_frowp.p, f.d_fcols.p, Fd, s)) ||
+      (rc = levels_t<df64>(f, Fd, status, s, launches)))
+    return rc;
+  const size_t nv = (size_t)f.nnzb() * 36;
+  k_df64_to_f32<<<(int)std::min<size_t>((nv + 255) / 256, 152 * 32), 256, 0, s>>>(F32, Fd, nv);
+  if (launches) *launches += 2;
+  A2DS_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 int factor_levels(const Factor &f, void *F, int *status, cudaStream_t s, long long *launches) {
   switch (f.precision) {
     case 64:

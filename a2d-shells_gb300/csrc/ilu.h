@@ -89,6 +89,7 @@ struct ChunkPlan {
 // A factorization handle (the TACSSchurPc role on one GPU).
 struct Factor {
   int n = 0, lev_fill = 0, precision = 64;
+  bool df_compute = false;  // FP32 factor computed in double-float (factor_df_to_f32)
   std::vector<int> frowp, fcols, fdiag;
   DBuf<int> d_frowp, d_fcols, d_fdiag, d_status;
   DBuf<double> F64;
@@ -159,7 +160,7 @@ constexpr long long PANEL_TABLE_MAX = 1LL << 28;
 constexpr int PANEL_UC_SMEM = 8192;
 
 // Largest chunk of the solves (block rows), and the factor blocks of one
-// pull segment (one warp: five groups of six lanes, two blocks per step).
+// pull segment (one warp: five groups of six lanes, four blocks per step).
 constexpr int CHUNK_MAX = 128;
 constexpr int SOLVE_SEG = 40;
 // chunks of at most this many rows are applied one warp per chunk
@@ -175,6 +176,14 @@ int factor_scatter(const Factor &f, int n, const int *rowp, const int *cols, con
 // singular diagonal block (0 = none).  A double-float factor is converted to
 // FP64 in place at the end.
 int factor_levels(const Factor &f, void *F, int *status, cudaStream_t s, long long *launches);
+// An FP32 factor (f.F32) computed in double-float arithmetic: the scatter
+// and the level-scheduled factorization run on df64 values in work (8 bytes
+// per value, nnzb_f x 36), then every value is rounded to FP32 once, so the
+// FP32 factor carries one rounding instead of the FP32 factorization's
+// accumulated errors.
+int factor_df_to_f32(const Factor &f, int n, const int *rowp, const int *cols, const double *A,
+                     const double *A2, double alpha2, void *work, float *F32, int *status,
+                     cudaStream_t s, long long *launches);
 
 // y = (LU)^{-1} x for nrhs in {1, 2, 4, 8, 16} right-hand sides, layout
 // (row, dof, rhs); y may alias x.  solve_levels launches the level kernels

@@ -216,6 +216,13 @@ int factor_numeric(Mesh &m, Factor &f, const double *A, const double *A2, double
   int rc;
   A2DS_CUDA_TRY(cudaMemsetAsync(f.d_status.p, 0, sizeof(int), m.stream));
   void *F = f.precision == 32 ? (void *)f.F32.p : (void *)f.F64.p;
+  if (f.precision == 32 && f.df_compute) {
+    if (f.F64.n < (size_t)f.nnzb() * 36 && (rc = f.F64.alloc((size_t)f.nnzb() * 36))) return rc;
+    if ((rc = factor_df_to_f32(f, m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, f.F64.p, f.F32.p,
+                               f.d_status.p, m.stream, &m.launches)))
+      return rc;
+    return chunk_build(f, F, m.stream, &m.launches);
+  }
   if ((rc = factor_scatter(f, m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, F, m.stream))) return rc;
   m.launches++;
   if ((rc = factor_levels(f, F, f.d_status.p, m.stream, &m.launches))) return rc;
@@ -1172,6 +1179,10 @@ static int prepare_solve(Mesh &m, const a2ds_buckling_opts *opts, BucklingState 
     if ((rc = factor_setup(m, opts->lev_fill, opts->precision, Sp->fk))) return rc;
     if (opts->lev_fill >= m.nn && (rc = factor_clone(m, Sp->fk, opts->precision, Sp->fa)))
       return rc;
+    // the shifted factor's FP32 values are computed in double-float and
+    // rounded once: its inner solves dominate the step, and the GMRES-IR
+    // steps they need grow with the factor's error
+    Sp->fa.df_compute = opts->precision == 32;
   }
   BucklingState &S = *Sp;
   S.sigma = opts->sigma;

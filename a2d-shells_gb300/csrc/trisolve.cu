@@ -47,22 +47,25 @@ __device__ __forceinline__ void block_row_fma(const BlockRow<T> &a, const TV *yv
 }
 
 // Partial sums of sum_k F_k[ii][:] y[fcols[k]] over k = kb + g, kb + g + step,
-// ..., two blocks per step so that both blocks' index, factor and vector
-// loads are in flight together.
+// ..., four blocks per step so that their index, factor and vector loads are
+// in flight together.
 template <typename T, typename TV, int R>
 __device__ __forceinline__ void row_partial(int kb, int ke, int g, int step, int ii,
                                             const int *__restrict__ fcols,
                                             const T *__restrict__ F, const TV *y, TV (&acc)[R]) {
   int k = kb + g;
-  for (; k + step < ke; k += 2 * step) {
-    const int j0 = fcols[k], j1 = fcols[k + step];
-    const BlockRow<T> a0 = *reinterpret_cast<const BlockRow<T> *>(F + (size_t)k * 36 + 6 * ii);
-    const BlockRow<T> a1 =
-        *reinterpret_cast<const BlockRow<T> *>(F + (size_t)(k + step) * 36 + 6 * ii);
-    block_row_fma<T, TV, R>(a0, y + (size_t)j0 * 6 * R, acc);
-    block_row_fma<T, TV, R>(a1, y + (size_t)j1 * 6 * R, acc);
+  for (; k + 3 * step < ke; k += 4 * step) {
+    int j[4];
+    BlockRow<T> a[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) j[u] = fcols[k + u * step];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      a[u] = *reinterpret_cast<const BlockRow<T> *>(F + (size_t)(k + u * step) * 36 + 6 * ii);
+#pragma unroll
+    for (int u = 0; u < 4; u++) block_row_fma<T, TV, R>(a[u], y + (size_t)j[u] * 6 * R, acc);
   }
-  if (k < ke) {
+  for (; k < ke; k += step) {
     const BlockRow<T> a0 = *reinterpret_cast<const BlockRow<T> *>(F + (size_t)k * 36 + 6 * ii);
     block_row_fma<T, TV, R>(a0, y + (size_t)fcols[k] * 6 * R, acc);
   }

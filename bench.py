@@ -147,6 +147,14 @@ DTYPE = {64: "f64", 48: "df64 factor (2 x f32) + f64", 32: "f32 factor + f64"}
 ASM_FP64_FLOPS_PER_ELEM = {"K": 42916, "G": 119624}
 ASM_FP64_PIPE_ACTIVE_PCT = {"K": 90.5, "G": 89.7}
 
+# DRAM bytes (read + write) of one 4-vector triangular-solve pass with FP32
+# factors per algorithmic byte of that pass (the formula below): an ncu
+# capture of all 64 launches of one solve on the 256x512 cylinder read
+# 1.6238 GB against 1.8663 GB algorithmic (profiles/trisolve_fp32_cylinder256x512_dram.md);
+# the pass reads each factor block once at every size, so the 512x1024
+# traffic is this ratio times its algorithmic bytes.
+TRISOLVE_TRAFFIC_RATIO = {32: 1.6238 / 1.8663}
+
 # DRAM traffic of one numeric factorization of the bench workload, summed
 # over all its launches from an ncu capture (profiles/factor_cylinder256x512_traffic.md)
 FACTOR_TRAFFIC = {(256, 512, 48): 279.65e9}
@@ -430,6 +438,10 @@ def main():
         rl_bytes = nnzf * (36 * vbytes + 4) + 2 * 2 * 6 * m.num_nodes * args.block * vbytes
         rl_ms = tri_ms
         rl_unit = "bytes per solve pass (factor values and column indices read once)"
+        ratio = TRISOLVE_TRAFFIC_RATIO.get(args.precision) if args.block == 4 else None
+        rl_traffic = ratio * rl_bytes if ratio else None
+        rl_traffic_note = ("ncu DRAM bytes of one 4-vector FP32 solve at 256x512 scaled by the "
+                           "algorithmic bytes" if ratio else None)
     else:
         rl_kernel = ("numeric complete-LU factorization of K + sigma G (panel-blocked trailing "
                      "updates k_update_panel, per-level k_update_long / k_update_group, "
@@ -437,6 +449,8 @@ def main():
         rl_bytes = nnzf * 36 * vbytes * 2
         rl_ms = fa_ms
         rl_unit = "bytes per factorization (factor values read and written once)"
+        rl_traffic = FACTOR_TRAFFIC.get((args.nx, args.ny, args.precision))
+        rl_traffic_note = "ncu DRAM bytes of one factorization" if rl_traffic else None
     achieved_gbs = rl_bytes / (rl_ms * 1e-3) / 1e9
     achieved_tf = stats["factor_flops"] / (fa_ms * 1e-3) / 1e12
     lam_err = (float(np.max(np.abs(b.eigvals - ref_lam) / np.abs(ref_lam)))
@@ -468,7 +482,7 @@ def main():
             "kernel": rl_kernel, "bound": "hbm", "achieved": achieved_gbs, "peak": hbm,
             "unit": "GB/s", "frac": (achieved_gbs / hbm) if hbm else None,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": FACTOR_TRAFFIC.get((args.nx, args.ny, args.precision)),
+            "traffic": rl_traffic, "traffic_source": rl_traffic_note,
             "algorithmic_bytes": rl_bytes, "algorithmic_bytes_unit": rl_unit,
             "ms_per_launch_sequence": rl_ms,
             "factorization": {"ms": fa_ms, "flops": stats["factor_flops"],
