@@ -422,7 +422,7 @@ template <typename T>
 __global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ task_row,
                                                         const int *__restrict__ task_ptr,
                                                         const int *__restrict__ task_jp,
-                                                        int ntasks, int nsplit,
+                                                        int ntasks, int nsplit, int cap,
                                                         const int *__restrict__ frowp,
                                                         const int *__restrict__ fcols,
                                                         const int *__restrict__ fdiag,
@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ 
   const int nslots = blockDim.x / 6;
   const int i = task_row[t];
   const int rs = frowp[i], len = frowp[i + 1] - rs;
-  const bool staged = len <= FACTOR_CTA_COLS;
+  const bool staged = len <= cap;
   if (staged)
     for (int k = tid; k < len; k += blockDim.x) s_cols[k] = fcols[rs + k];
   const int *cols = staged ? s_cols : fcols + rs;
@@ -688,9 +688,15 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
                                                       f.d_fdiag.p, F);
         nl++;
       }
-      k_update_long<T><<<nlong * nsplit, 384, smem, s>>>(
-          f.d_task_row.p + t0, f.d_task_ptr.p + t0, f.d_task_jp.p, nlong, nsplit, f.d_frowp.p,
-          f.d_fcols.p, f.d_fdiag.p, F);
+      // single CTAs per task: 192 threads (32 block updates at a time; the
+      // leaf levels' long tasks apply few short U rows per pivot) and the
+      // column staging sized to the level's longest row, so more tasks are
+      // in flight per SM; split tasks (long U rows) keep 384 threads
+      const int cap = pk >= 0 ? FACTOR_CTA_COLS
+                              : std::min(FACTOR_CTA_COLS, std::max(1, f.task_long_cols[lv]));
+      k_update_long<T><<<nlong * nsplit, nsplit > 1 ? 384 : 192, cap * (int)sizeof(int), s>>>(
+          f.d_task_row.p + t0, f.d_task_ptr.p + t0, f.d_task_jp.p, nlong, nsplit, cap,
+          f.d_frowp.p, f.d_fcols.p, f.d_fdiag.p, F);
       nl++;
     }
     if (ns > 0) {

@@ -74,6 +74,7 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
     }
   f.task_level_ptr.assign(nl + 1, 0);
   f.task_nlong.assign(nl, 0);
+  f.task_long_cols.assign(nl, 0);
   f.task_group.clear();
   f.task_row.clear();
   f.task_ptr.assign(1, 0);
@@ -155,10 +156,12 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
           for (long long q = p; q < e; q++) f.task_jp.push_back(bucket_jp[q]);
           f.task_ptr.push_back((int)f.task_jp.size());
           if (pass == 0) {
-            if (pk >= 0)
+            if (pk >= 0) {
               pn.task_np[l]++;
-            else
+            } else {
               f.task_nlong[l]++;
+              f.task_long_cols[l] = std::max(f.task_long_cols[l], f.frowp[i + 1] - f.frowp[i]);
+            }
           }
         }
         p = e;

@@ -98,6 +98,7 @@ struct Factor {
   // right-looking update tasks, grouped by level; within a level the tasks
   // of long target rows (> FACTOR_WARP_COLS blocks) come first
   std::vector<int> task_level_ptr, task_nlong, task_row, task_ptr, task_jp;
+  std::vector<int> task_long_cols;  // per level: longest target row of its long tasks
   std::vector<int> task_group;  // block updates in flight per short task, per level (1, 2, 5)
   // panels of narrow levels (blocked trailing updates, see build_update_tasks)
   PanelSchedule pn;

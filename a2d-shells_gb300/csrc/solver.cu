@@ -190,6 +190,7 @@ static int factor_clone(Mesh &m, const Factor &src, int precision, Factor &f) {
   f.flv.rows = src.flv.rows;
   f.task_level_ptr = src.task_level_ptr;
   f.task_nlong = src.task_nlong;
+  f.task_long_cols = src.task_long_cols;
   f.task_group = src.task_group;
   f.pn = src.pn;
   f.task_row = src.task_row;
