@@ -108,12 +108,15 @@ def run_preload(args):
     mag = np.abs(ds)
     significant = np.where(mag >= 1e-3 * mag.max())[0]
     out["fd_candidates"] = significant.tolist()
+    gap = abs(base["lam"][1] - base["lam"][0])
     for p in rng.choice(significant, min(args.fd_params, significant.size), replace=False):
-        eps = args.fd_step
+        # the step moves lambda_1 by 1 % of its gap to lambda_2 at most, so
+        # the difference quotient does not cross into the next eigenvalue
+        eps = min(args.fd_step, 0.01 * gap / max(abs(ds[p]), 1e-300))
         lp = preload_solve(m.X + eps * modes[p])["lam"][0]
         lm = preload_solve(m.X - eps * modes[p])["lam"][0]
         d = (lp - lm) / (2 * eps)
-        fd.append({"param": int(p), "adjoint": ds[p], "central_difference": d,
+        fd.append({"param": int(p), "step": eps, "adjoint": ds[p], "central_difference": d,
                    "rel_diff": abs(ds[p] - d) / max(abs(d), 1e-300),
                    "diff_vs_gradient_max": abs(ds[p] - d) / mag.max()})
     out["fd_check"] = fd
@@ -133,8 +136,11 @@ def run_panel(args):
 
     # shift: 0.9 x the lowest load of a cheap first solve about a small shift
     # (the loads of smallest magnitude converge first either way)
+    # complete LU: a level of fill at least the node count (the panel has
+    # more than the reference's customary lev = 1e6 nodes)
+    lev = max(1000000, m.num_nodes)
     b0 = capi.LinearBuckling(a, args.sigma, max_lanczos=200, num_eigvals=1, eig_tol=1e-6,
-                             precision=args.precision, block_size=4)
+                             lev_fill=lev, precision=args.precision, block_size=4)
     try:
         b0.solve(m.rhs, want_vectors=False)
     except capi.A2dsError:
@@ -146,7 +152,8 @@ def run_panel(args):
 
     def solve(aa):
         bb = capi.LinearBuckling(aa, sigma, max_lanczos=200, num_eigvals=args.neig,
-                                 eig_tol=1e-10, precision=args.precision, block_size=4)
+                                 eig_tol=1e-10, lev_fill=lev, precision=args.precision,
+                                 block_size=4)
         lam = bb.solve(m.rhs, want_vectors=False).copy()
         return bb, lam
 

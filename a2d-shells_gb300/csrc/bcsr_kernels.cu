@@ -49,42 +49,12 @@ int launch_axpy(double *y, double alpha, const double *x, size_t n, cudaStream_t
   return 0;
 }
 
-// y = A x: one warp per block row.  Lanes 0..29 form five groups of six;
+// y = A x, one warp per block row: lanes 0..29 form five groups of six;
 // lane (g, i) takes blocks g, g+5, ... of the row and forms the dot product
 // of row i of each block (six contiguous values) with the matching six
 // entries of x, so every FMA issued is useful and no accumulator is indexed
-// dynamically.  The five group partial sums are combined through shared
-// memory.
-template <typename TV, typename TX>
-__global__ void __launch_bounds__(256) k_bcsr_spmv(int nrows, const int *__restrict__ rowp,
-                                                   const int *__restrict__ cols,
-                                                   const TV *__restrict__ vals,
-                                                   const TX *__restrict__ x, TX *__restrict__ y) {
-  __shared__ TX part[8][32];
-  const int wib = threadIdx.x >> 5;
-  const int warp = blockIdx.x * 8 + wib;
-  const int lane = threadIdx.x & 31;
-  TX acc = 0;
-  if (warp < nrows && lane < 30) {
-    const int g = lane / 6, i = lane - 6 * g;
-    const int start = rowp[warp], end = rowp[warp + 1];
-    for (int jp = start + g; jp < end; jp += 5) {
-      const TV *a = vals + (size_t)jp * 36 + 6 * i;
-      const TX *xv = x + (size_t)cols[jp] * 6;
-#pragma unroll
-      for (int j = 0; j < 6; j++) acc += (TX)a[j] * xv[j];
-    }
-  }
-  part[wib][lane] = acc;
-  __syncwarp();
-  if (warp < nrows && lane < 6) {
-    TX v = part[wib][lane] + part[wib][lane + 6] + part[wib][lane + 12] +
-           part[wib][lane + 18] + part[wib][lane + 24];
-    y[(size_t)warp * 6 + lane] = v;
-  }
-}
-
-// FP64 form of the same mapping with 16-byte loads: lane (g, i) reads row
+// dynamically; the five group partial sums are combined through shared
+// memory.  FP64 values are read with 16-byte loads: lane (g, i) reads row
 // i of a block as three double2 (a block row of 48 bytes, 16-byte aligned
 // since blocks are 288 bytes) and the six x entries as three double2; the
 // row's column indices are read once by the warp (lane l holds column
@@ -131,15 +101,6 @@ int launch_spmv_f64(int nrows, const int *rowp, const int *cols, const double *v
   if (nrows <= 0) return 0;
   int blocks = (nrows * 32 + 255) / 256;
   k_bcsr_spmv_f64<<<blocks, 256, 0, s>>>(nrows, rowp, cols, vals, x, y);
-  A2DS_CUDA_TRY(cudaGetLastError());
-  return 0;
-}
-
-int launch_spmv_f32(int nrows, const int *rowp, const int *cols, const float *vals,
-                    const float *x, float *y, cudaStream_t s) {
-  if (nrows <= 0) return 0;
-  int blocks = (nrows * 32 + 255) / 256;
-  k_bcsr_spmv<float, float><<<blocks, 256, 0, s>>>(nrows, rowp, cols, vals, x, y);
   A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -536,9 +536,10 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
 // (FACTOR_CTA_COLS ints) and uc (PANEL_UC_SMEM ints), each read from global
 // memory instead when longer.
 template <typename T>
-__global__ void __launch_bounds__(384, 2) k_update_panel(
+__global__ void __launch_bounds__(384, 3) k_update_panel(
     const int *__restrict__ task_row, const int *__restrict__ task_jpk, int ntasks,
-    const int *__restrict__ prow, int np, const int *__restrict__ uc, int nuc,
+    const int *__restrict__ prow, int np, const int *__restrict__ uc, int nuc, int cols_cap,
+    int uc_cap,
     const int *__restrict__ tab, const int *__restrict__ tp, const int *__restrict__ frowp,
     const int *__restrict__ fcols, const int *__restrict__ fdiag, T *__restrict__ F) {
   constexpr int PM = PANEL_MAX_ROWS;
@@ -552,8 +553,8 @@ __global__ void __launch_bounds__(384, 2) k_update_panel(
   const int nslots = blockDim.x / 6;
   const int i = task_row[t];
   const int rs = frowp[i], len = frowp[i + 1] - rs;
-  int *s_cols = s_dyn, *s_uc = s_dyn + FACTOR_CTA_COLS;
-  const bool staged = len <= FACTOR_CTA_COLS, uc_staged = nuc <= PANEL_UC_SMEM;
+  int *s_cols = s_dyn, *s_uc = s_dyn + cols_cap;
+  const bool staged = len <= cols_cap, uc_staged = nuc <= uc_cap;
   if (staged)
     for (int k = tid; k < len; k += blockDim.x) s_cols[k] = fcols[rs + k];
   if (uc_staged)
@@ -718,9 +719,13 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
       const int a = pn.task_ptr[pk], ntk = pn.task_ptr[pk + 1] - a;
       const int u0 = pn.uc_ptr[pk], nuc = pn.uc_ptr[pk + 1] - u0;
       if (ntk > 0) {
-        k_update_panel<T><<<ntk, 384, psmem, s>>>(
+        // shared staging sized to this panel (longest target row, union of
+        // U columns), so more CTAs fit on an SM
+        const int cols_cap = std::min(FACTOR_CTA_COLS, std::max(1, pn.task_maxlen[pk]));
+        const int uc_cap = std::min(PANEL_UC_SMEM, std::max(1, nuc));
+        k_update_panel<T><<<ntk, 384, (cols_cap + uc_cap) * (int)sizeof(int), s>>>(
             f.d_pn_task_row.p + a, f.d_pn_task_jpk.p + (size_t)a * PM, ntk,
-            f.d_pn_prow.p + (size_t)pk * PM, pn.np[pk], f.d_pn_uc.p + u0, nuc,
+            f.d_pn_prow.p + (size_t)pk * PM, pn.np[pk], f.d_pn_uc.p + u0, nuc, cols_cap, uc_cap,
             f.d_pn_tab.p + pn.tab_off[pk], f.d_pn_tp.p + (size_t)pk * PM * PM, f.d_frowp.p,
             f.d_fcols.p, f.d_fdiag.p, F);
         nl++;

@@ -233,7 +233,9 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
         rows.push_back(f.task_row[t]);
     std::sort(rows.begin(), rows.end());
     rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+    int maxlen = 0;
     for (int i : rows) {
+      maxlen = std::max(maxlen, f.frowp[i + 1] - f.frowp[i]);
       pn.task_row.push_back(i);
       const size_t b0 = pn.task_jpk.size();
       pn.task_jpk.resize(b0 + PM, -1);
@@ -241,6 +243,7 @@ void build_update_tasks(Factor &f, const std::vector<int> &lev) {
         if (kof[f.fcols[q]] >= 0) pn.task_jpk[b0 + kof[f.fcols[q]]] = q;
     }
     pn.task_ptr.push_back((int)pn.task_row.size());
+    pn.task_maxlen.push_back(maxlen);
     for (int k = 0; k < np; k++) kof[prow[k]] = -1;
   }
 }

@@ -43,6 +43,7 @@ struct PanelSchedule {
   // phase-2 tasks: per panel a range of target rows; PANEL_MAX_ROWS L
   // positions per task (L block of the row in column prow[k], -1: none)
   std::vector<int> task_ptr, task_row, task_jpk;
+  std::vector<int> task_maxlen;  // per panel: longest target row of its phase-2 tasks
 };
 
 // Chunked triangular solves.  Rows are cut into chunks of consecutive rows:

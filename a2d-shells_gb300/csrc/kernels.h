@@ -9,6 +9,4 @@ namespace a2ds {
 int launch_axpy(double *y, double alpha, const double *x, size_t n, cudaStream_t s);
 int launch_spmv_f64(int nrows, const int *rowp, const int *cols, const double *vals,
                     const double *x, double *y, cudaStream_t s);
-int launch_spmv_f32(int nrows, const int *rowp, const int *cols, const float *vals,
-                    const float *x, float *y, cudaStream_t s);
 }  // namespace a2ds

@@ -218,8 +218,11 @@ int factor_numeric(Mesh &m, Factor &f, const double *A, const double *A2, double
   A2DS_CUDA_TRY(cudaMemsetAsync(f.d_status.p, 0, sizeof(int), m.stream));
   void *F = f.precision == 32 ? (void *)f.F32.p : (void *)f.F64.p;
   if (f.precision == 32 && f.df_compute) {
-    if (f.F64.n < (size_t)f.nnzb() * 36 && (rc = f.F64.alloc((size_t)f.nnzb() * 36))) return rc;
-    if ((rc = factor_df_to_f32(f, m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, f.F64.p, f.F32.p,
+    // the double-float work array (the size of an FP64 factor) lives only
+    // for the factorization (freeing it waits for the device)
+    DBuf<double> work;
+    if ((rc = work.alloc((size_t)f.nnzb() * 36))) return rc;
+    if ((rc = factor_df_to_f32(f, m.nn, m.d_rowp.p, m.d_cols.p, A, A2, alpha2, work.p, f.F32.p,
                                f.d_status.p, m.stream, &m.launches)))
       return rc;
     return chunk_build(f, F, m.stream, &m.launches);

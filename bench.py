@@ -299,7 +299,7 @@ def spmv_roofline(capi, a, m, hbm, iters=50):
             ms = K.time_mult(p, iters)
             nbytes = nnzb * (36 * 8 + 4) + (m.num_nodes + 1) * 4 + 2 * 6 * m.num_nodes * 8 * p
             gbs = nbytes / (ms * 1e-3) / 1e9
-            out[f"p{p}"] = {"kernel": "k_bcsr_spmv" if p == 1 else f"k_blk_spmm<{p}>",
+            out[f"p{p}"] = {"kernel": "k_bcsr_spmv_f64" if p == 1 else f"k_blk_spmm<{p}>",
                             "ms": ms, "bytes": nbytes, "achieved_gbs": gbs,
                             "frac_of_measured_hbm": (gbs / hbm) if hbm else None,
                             "fp64_tflops": 72.0 * nnzb * p / (ms * 1e-3) / 1e12}
@@ -445,13 +445,28 @@ def main():
     else:
         rl_kernel = ("numeric complete-LU factorization of K + sigma G (panel-blocked trailing "
                      "updates k_update_panel, per-level k_update_long / k_update_group, "
-                     "pivot inverses)")
-        rl_bytes = nnzf * 36 * vbytes * 2
+                     "pivot inverses)" + ("; computed in double-float, rounded to FP32"
+                                          if args.precision == 32 else ""))
+        if args.precision == 32:
+            # double-float work values read and written once, the FP32 factor written once
+            rl_bytes = nnzf * 36 * 8 * 2 + nnzf * 36 * 4
+        else:
+            rl_bytes = nnzf * 36 * vbytes * 2
         rl_ms = fa_ms
         rl_unit = "bytes per factorization (factor values read and written once)"
         rl_traffic = FACTOR_TRAFFIC.get((args.nx, args.ny, args.precision))
         rl_traffic_note = "ncu DRAM bytes of one factorization" if rl_traffic else None
     achieved_gbs = rl_bytes / (rl_ms * 1e-3) / 1e9
+    # the step's HBM-bound kernel sequence, reported beside the dominant one
+    tri_bytes = nnzf * (36 * vbytes + 4) + 2 * 2 * 6 * m.num_nodes * args.block * vbytes
+    tri_ratio = TRISOLVE_TRAFFIC_RATIO.get(args.precision) if args.block == 4 else None
+    tri_gbs = tri_bytes / (tri_ms * 1e-3) / 1e9
+    trisolve_roofline = {
+        "kernel": (f"one triangular-solve pass on a block of {args.block} vectors "
+                   "(k_pull_seg, k_chunk_apply)"),
+        "bound": "hbm", "achieved": tri_gbs, "peak": hbm, "unit": "GB/s",
+        "frac": (tri_gbs / hbm) if hbm else None, "ms": tri_ms, "algorithmic_bytes": tri_bytes,
+        "traffic": tri_ratio * tri_bytes if tri_ratio else None}
     achieved_tf = stats["factor_flops"] / (fa_ms * 1e-3) / 1e12
     lam_err = (float(np.max(np.abs(b.eigvals - ref_lam) / np.abs(ref_lam)))
                if ref_lam is not None else None)
@@ -485,14 +500,18 @@ def main():
             "traffic": rl_traffic, "traffic_source": rl_traffic_note,
             "algorithmic_bytes": rl_bytes, "algorithmic_bytes_unit": rl_unit,
             "ms_per_launch_sequence": rl_ms,
+            "triangular_solve": trisolve_roofline,
             "factorization": {"ms": fa_ms, "flops": stats["factor_flops"],
                               "achieved_tflops_fp64_equivalent_count": achieved_tf,
                               "fp64_peak_tflops_measured_dgemm": fp64,
                               "pipe": {32: "fp32", 48: "fp32 (double-float)", 64: "fp64"}[args.precision]},
-            "note": ("sparse 6x6-block LU and triangular solves: neither pipe is saturated; the "
+            "note": ("sparse 6x6-block LU and triangular solves: neither is HBM-bound; the "
                      "triangular solves are bound by the latency of their dependent level "
-                     "launches, the factorization by launch/memory latency and the issue rate "
-                     "of its block updates; the HBM fraction is reported for the contract"),
+                     "launches and loads, the factorization by dependent-load chains at its lower "
+                     "levels and by FP32 issue of the double-float updates in its panels "
+                     "(~12 FP32 instructions per multiply-subtract), so its HBM fraction is "
+                     "small by construction; the FP64-equivalent rate beside the DGEMM ceiling is "
+                     "the meaningful figure; the HBM fraction is reported for the contract"),
         },
         "phases_s": {k: stats[k] for k in ["assemble_k_s", "assemble_g_s", "factor_s", "path_s",
                                             "lanczos_s"]},

@@ -15,7 +15,9 @@ import pytest
 from conftest import REPO
 from a2ds import capi
 
-REFERENCE_TREE = os.environ.get("A2DS_REFERENCE_TREE", "/root/reference")
+# the reference tree: A2DS_REFERENCE, else a checkout beside this repository
+REFERENCE_TREE = (os.environ.get("A2DS_REFERENCE")
+                  or os.path.join(os.path.dirname(REPO), "reference"))
 DECKS = os.path.join(REFERENCE_TREE, "examples", "cylinder-buckling")
 GOLDEN_GEN = os.path.join(REPO, "oracle", "_ref", "golden_gen")
 
