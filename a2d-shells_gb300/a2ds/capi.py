@@ -52,7 +52,7 @@ EXPORTS = [
     "a2ds_preload_xpt_sens",
     "a2ds_eval_mat_sv_sens_inner_product", "a2ds_eig_sens_xpts",
     "a2ds_bcsr_mult", "a2ds_bcsr_mult_rows", "a2ds_bcsr_mult_rows_noalloc", "a2ds_bcsr_copy", "a2ds_bcsr_axpy",
-    "a2ds_bcsr_time_mult",
+    "a2ds_bcsr_time_mult", "a2ds_bcsr_time_mult_df",
     "a2ds_bcsr_apply_bcs", "a2ds_pc_create", "a2ds_pc_destroy", "a2ds_pc_factor",
     "a2ds_pc_apply", "a2ds_pc_apply_multi", "a2ds_pc_get", "a2ds_gmres_solve",
     "a2ds_fgmres_solve", "a2ds_buckling_default_opts", "a2ds_buckling_solve",
@@ -150,6 +150,7 @@ def load(build: bool = False):
     lib.a2ds_preload_buckling.argtypes = [VP, ctypes.POINTER(BucklingOpts), P_D, P_D, P_D, P_D]
     lib.a2ds_preload_xpt_sens.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
     lib.a2ds_bcsr_time_mult.argtypes = [VP, ctypes.c_int, ctypes.c_int, P_D]
+    lib.a2ds_bcsr_time_mult_df.argtypes = [VP, ctypes.c_int, ctypes.c_int, P_D]
     lib.a2ds_eig_sens_xpts.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D]
     lib.a2ds_add_mat_xpt_sens_inner_product.argtypes = [VP, ctypes.c_int, ctypes.c_double, P_D,
                                                         P_D, P_D, ctypes.c_double, P_D]
@@ -392,6 +393,14 @@ class BCSRMat:
         """Device milliseconds per product with nvec device-resident vectors."""
         ms = ctypes.c_double(0.0)
         _check(self.lib.a2ds_bcsr_time_mult(self.h, int(nvec), int(iters), ctypes.byref(ms)))
+        return ms.value
+
+    def time_mult_df(self, nvec=4, iters=20):
+        """Device milliseconds per double-float product (the matrix as
+        double-float pairs) with nvec device-resident FP32 vectors: the
+        product of the mixed-precision GMRES-IR inner loop."""
+        ms = ctypes.c_double(0.0)
+        _check(self.lib.a2ds_bcsr_time_mult_df(self.h, int(nvec), int(iters), ctypes.byref(ms)))
         return ms.value
 
     def mult_rows(self, x, noalloc=False):

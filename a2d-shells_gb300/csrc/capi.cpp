@@ -487,6 +487,46 @@ int a2ds_bcsr_mult_rows(a2ds_bcsr A, const double *x, double *y) {
   A2DS_GUARD_END
 }
 
+int a2ds_bcsr_time_mult_df(a2ds_bcsr A, int nvec, int iters, double *ms_per_mult) {
+  A2DS_GUARD_BEGIN
+  if (!A || !ms_per_mult) return fail(A2DS_ERR_ARG, "null argument");
+  if (iters < 1 || iters > 100000) return fail(A2DS_ERR_ARG, "iters must be in [1, 100000]");
+  if (nvec != 1 && nvec != 2 && nvec != 4 && nvec != 8 && nvec != 16)
+    return fail(A2DS_ERR_ARG, "nvec must be 1, 2, 4, 8 or 16");
+  Mesh &m = A->mesh->m;
+  const size_t n = (size_t)m.nn * 6 * nvec, nv = (size_t)m.nnzb * 36;
+  // double-float arrays held as float pairs
+  DBuf<float> ad, dx, dy;
+  int rc;
+  if ((rc = ad.alloc(2 * nv)) || (rc = dx.alloc(n)) || (rc = dy.alloc(2 * n))) return rc;
+  df64 *Ad = reinterpret_cast<df64 *>(ad.p), *Y = reinterpret_cast<df64 *>(dy.p);
+  if ((rc = df_from_f64(Ad, A->vals.p, nv, m.stream))) return rc;
+  A2DS_CUDA_TRY(cudaMemsetAsync(dx.p, 0, n * sizeof(float), m.stream));
+  auto mult = [&]() { return df_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Ad, dx.p, Y, nvec, m.stream); };
+  for (int w = 0; w < 3; w++)
+    if ((rc = mult())) return rc;
+  cudaEvent_t e0, e1;
+  A2DS_CUDA_TRY(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(A2DS_ERR_CUDA, "cudaEventCreate failed");
+  }
+  float ms = 0.0f;
+  cudaEventRecord(e0, m.stream);
+  for (int it = 0; it < iters && !rc; it++) rc = mult();
+  cudaEventRecord(e1, m.stream);
+  cudaError_t e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(A2DS_ERR_CUDA, cudaGetErrorString(e));
+  m.launches += iters + 4;
+  *ms_per_mult = (double)ms / iters;
+  return 0;
+  A2DS_GUARD_END
+}
+
 int a2ds_bcsr_time_mult(a2ds_bcsr A, int nvec, int iters, double *ms_per_mult) {
   A2DS_GUARD_BEGIN
   if (!A || !ms_per_mult) return fail(A2DS_ERR_ARG, "null argument");

@@ -337,6 +337,21 @@ __device__ __forceinline__ int find_col(const int *cols, int lo, int hi, int c) 
   return (lo < hi && cols[lo] == c) ? lo : -1;
 }
 
+// Galloping search for c in the sorted cols[lo, hi): probes lo, lo + 2,
+// lo + 5, ... until a column >= c, then a binary search in the last gap.
+// A slot's successive U columns land at increasing target positions close
+// to the previous one, so starting from there costs a few probes of nearby
+// (cached) addresses instead of a search of the whole remaining row.
+__device__ __forceinline__ int find_col_from(const int *cols, int lo, int hi, int c) {
+  int step = 1, b = lo;
+  while (b < hi && cols[b] < c) {
+    lo = b + 1;
+    b = lo + step;
+    step <<= 1;
+  }
+  return find_col(cols, lo, min(b + 1, hi), c);
+}
+
 // L_ij = A_ij D_j^{-1} for every L entry of one level, in place; a CTA of
 // 288 threads handles 8 entries, thread (entry q, element e).  D_j^{-1} is
 // final (the level's pivot kernel ran), A_ij is final (every pivot that
@@ -511,11 +526,15 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
         F[(size_t)jp * 36 + gl + d * G] = v[d];
       }
     __syncwarp(gmask);
-    const int ue = frowp[j + 1], lo0 = jp + 1 - rs;
+    const int ue = frowp[j + 1];
+    int hint = jp + 1 - rs;  // the U columns of pivot j lie after column j in row i
 #pragma unroll 1
     for (int pu = fdiag[j] + 1 + slot; pu < ue; pu += S) {
-      const int pos = find_col(cols, lo0, len, fcols[pu]);
-      if (pos >= 0) blk_col_update(F + (size_t)(rs + pos) * 36, L, F + (size_t)pu * 36, b);
+      const int pos = find_col_from(cols, hint, len, fcols[pu]);
+      if (pos >= 0) {
+        blk_col_update(F + (size_t)(rs + pos) * 36, L, F + (size_t)pu * 36, b);
+        hint = pos + 1;
+      }
     }
     __syncwarp(gmask);
   }

@@ -288,7 +288,9 @@ def workload_sigma(m):
 def spmv_roofline(capi, a, m, hbm, iters=50):
     """K times 1 and 4 device-resident vectors (the path's and the block
     Lanczos' product), timed with CUDA events after the timed region;
-    algorithmic bytes nnzb (36 x 8 + 4) + (nn + 1) 4 + 2 (6 nn 8) p."""
+    algorithmic bytes nnzb (36 x 8 + 4) + (nn + 1) 4 + 2 (6 nn 8) p; and the
+    double-float product of the GMRES-IR inner loop (FP32 vectors in,
+    double-float out: 6 nn p (4 + 8) vector bytes)."""
     try:
         K = a.create_mat()
         a.assemble_mat_type(capi.A2DS_STIFFNESS_MATRIX, K)
@@ -303,6 +305,16 @@ def spmv_roofline(capi, a, m, hbm, iters=50):
                             "ms": ms, "bytes": nbytes, "achieved_gbs": gbs,
                             "frac_of_measured_hbm": (gbs / hbm) if hbm else None,
                             "fp64_tflops": 72.0 * nnzb * p / (ms * 1e-3) / 1e12}
+        # the double-float product of the GMRES-IR inner loop (FP32 pipe):
+        # the matrix as double-float pairs, FP32 vectors in, double-float out
+        for p in (1, 4):
+            ms = K.time_mult_df(p, iters)
+            nbytes = (nnzb * (36 * 8 + 4) + (m.num_nodes + 1) * 4 +
+                      6 * m.num_nodes * p * 4 + 6 * m.num_nodes * p * 8)
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            out[f"p{p}_df64"] = {"kernel": f"k_df_spmm<{p}>", "ms": ms, "bytes": nbytes,
+                                 "achieved_gbs": gbs,
+                                 "frac_of_measured_hbm": (gbs / hbm) if hbm else None}
         return out
     except Exception as ex:  # reported beside the headline, never in place of it
         return {"error": str(ex)[:200]}

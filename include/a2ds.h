@@ -243,6 +243,10 @@ int a2ds_bcsr_mult_rows_noalloc(a2ds_bcsr A, const double *x, double *y);
    over iters launches after 3 warm-up launches, CUDA events on the mesh's
    stream.  No counterpart in the reference (a measurement entry). */
 int a2ds_bcsr_time_mult(a2ds_bcsr A, int nvec, int iters, double *ms_per_mult);
+/* The same for the double-float product of the mixed-precision GMRES-IR
+   inner loop: A converted once to double-float pairs (8 bytes per value),
+   times nvec (1, 2, 4, 8, 16) stacked FP32 vectors, double-float result. */
+int a2ds_bcsr_time_mult_df(a2ds_bcsr A, int nvec, int iters, double *ms_per_mult);
 
 int a2ds_bcsr_copy(a2ds_bcsr Y, a2ds_bcsr X);
 int a2ds_bcsr_axpy(a2ds_bcsr Y, double alpha, a2ds_bcsr X);

@@ -201,7 +201,8 @@ def test_mesh_assembly_matches_oracle_elementwise():
 
 @pytest.mark.gpu
 def test_bcsr_time_mult():
-    """The measurement entry behind bench.py's SpMV figures: positive device
+    """The measurement entries behind bench.py's SpMV figures (FP64 product
+    and the double-float product of the GMRES-IR inner loop): positive device
     times for 1 and 4 vectors, argument checks."""
     f = np.load(os.path.join(GOLDEN, "cyl_q4_8x16_ilu1.npz"))
     a = capi.Assembler(f["X"], f["conn"])
@@ -215,7 +216,11 @@ def test_bcsr_time_mult():
     for p in (1, 4):
         ms = K.time_mult(p, 5)
         assert np.isfinite(ms) and ms > 0.0
+        ms = K.time_mult_df(p, 5)
+        assert np.isfinite(ms) and ms > 0.0
     with pytest.raises(capi.A2dsError):
         K.time_mult(3, 5)
     with pytest.raises(capi.A2dsError):
         K.time_mult(1, 0)
+    with pytest.raises(capi.A2dsError):
+        K.time_mult_df(3, 5)
