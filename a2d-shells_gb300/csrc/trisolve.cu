@@ -20,6 +20,7 @@
 // solve_graph() captures the whole launch sequence once per (factor, x, y,
 // R) and replays it.
 #include "a2ds_internal.h"
+#include "df64.h"
 #include "ilu.h"
 
 namespace a2ds {
@@ -290,11 +291,12 @@ __global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2)
     apply_rows<T, TV, R, UPPER, ROWS>(Inv, w, u / PER, (u % PER) * ROWS, sv, yc, lane);
 }
 
-// Dense FP64 copy of every multi-row chunk's diagonal block out of the factor
-// (scratch zeroed beforehand; chunk c's (6 ns)^2 block at off[c] / 2, since
+// Dense copy (FP64; FP32 for FP32 factors) of every multi-row chunk's
+// diagonal block out of the factor (scratch zeroed beforehand; chunk c's
+// (6 ns)^2 block at off[c] / 2, since
 // the inverse storage holds two blocks per chunk), one CTA per chunk, one
 // warp per row: the row's blocks inside its chunk are [row_lend, row_ustart).
-template <typename TF>
+template <typename TF, typename TS>
 __global__ void __launch_bounds__(256) k_chunk_gather(const int *__restrict__ chunks,
                                                       const int *__restrict__ c0,
                                                       const long long *__restrict__ off,
@@ -302,17 +304,17 @@ __global__ void __launch_bounds__(256) k_chunk_gather(const int *__restrict__ ch
                                                       const int *__restrict__ row_lend,
                                                       const int *__restrict__ row_ustart,
                                                       const TF *__restrict__ F,
-                                                      double *__restrict__ Mall) {
+                                                      TS *__restrict__ Mall) {
   const int ch = chunks[blockIdx.x];
   const int a = c0[ch], ns = c0[ch + 1] - a, w = 6 * ns;
-  double *M = Mall + off[ch] / 2;
+  TS *M = Mall + off[ch] / 2;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int r = warp; r < ns; r += nw) {
     const int i = a + r, k0 = row_lend[i], k1 = row_ustart[i];
     for (int idx = lane; idx < (k1 - k0) * 36; idx += 32) {
       const int k = k0 + idx / 36, e = idx % 36;
       const int ea = e / 6, eb = e % 6;
-      M[(size_t)(6 * r + ea) * w + 6 * (fcols[k] - a) + eb] = (double)F[(size_t)k * 36 + e];
+      M[(size_t)(6 * r + ea) * w + 6 * (fcols[k] - a) + eb] = (TS)F[(size_t)k * 36 + e];
     }
   }
 }
@@ -374,6 +376,90 @@ __global__ void k_chunk_inverse(const int *__restrict__ chunks, const int *__res
   }
 }
 
+// The same inverses for FP32 factors on the FP32 pipe: the gathered FP32
+// blocks are exact in double-float, the substitution accumulates in
+// double-float (~48-bit significand, so the FP32 rounding of the result is
+// that of an FP64 computation up to ties) and X (double-float, in the FP64
+// inverse storage) is rounded to FP32 afterwards.  ~9 FP32 operations per
+// multiply-subtract instead of one FP64 FMA at 1/60 of the FP32 rate.
+__device__ __forceinline__ void df_sub_prod_f(float &hi, float &lo, float m, df64 x) {
+  const float ph = __fmul_rn(m, x.hi);
+  float pe = fmaf(m, x.hi, -ph);
+  pe = fmaf(m, x.lo, pe);
+  const float s = __fsub_rn(hi, ph);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(-ph, bb));
+  hi = s;
+  lo = __fadd_rn(lo, __fsub_rn(err, pe));
+}
+
+template <bool UPPER>
+__global__ void k_chunk_inverse_df(const int *__restrict__ chunks, const int *__restrict__ c0,
+                                   const long long *__restrict__ off,
+                                   const float *__restrict__ Mall, df64 *__restrict__ inv) {
+  const int ch = chunks[blockIdx.x];
+  const int ns = c0[ch + 1] - c0[ch], w = 6 * ns;
+  const float *M = Mall + off[ch] / 2;
+  df64 *X = inv + off[ch] + (UPPER ? (long long)w * w : 0);
+  for (int c = threadIdx.x; c < w; c += blockDim.x) {
+    const int bc = c / 6;
+    if (!UPPER) {
+      for (int i = 0; i < ns; i++) {
+        float vh[6], vl[6];
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+          vh[a] = (6 * i + a == c) ? 1.0f : 0.0f;
+          vl[a] = 0.0f;
+        }
+        if (i > bc) {
+          for (int q = 6 * bc; q < 6 * i; q++) {
+            const df64 xq = X[(size_t)q * w + c];
+#pragma unroll
+            for (int a = 0; a < 6; a++)
+              df_sub_prod_f(vh[a], vl[a], M[(size_t)(6 * i + a) * w + q], xq);
+          }
+        }
+#pragma unroll
+        for (int a = 0; a < 6; a++) X[(size_t)(6 * i + a) * w + c] = df_norm(vh[a], vl[a]);
+      }
+    } else {
+      for (int i = ns - 1; i >= 0; i--) {
+        float zh[6], zl[6];
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+          zh[a] = (6 * i + a == c) ? 1.0f : 0.0f;
+          zl[a] = 0.0f;
+        }
+        if (i <= bc) {
+          for (int q = 6 * (i + 1); q < 6 * bc + 6; q++) {
+            const df64 xq = X[(size_t)q * w + c];
+#pragma unroll
+            for (int a = 0; a < 6; a++)
+              df_sub_prod_f(zh[a], zl[a], M[(size_t)(6 * i + a) * w + q], xq);
+          }
+        }
+        df64 z[6];
+#pragma unroll
+        for (int a = 0; a < 6; a++) z[a] = df_norm(zh[a], zl[a]);
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+          const float *Dr = M + (size_t)(6 * i + a) * w + 6 * i;
+          float h = 0.0f, l = 0.0f;
+#pragma unroll
+          for (int b = 0; b < 6; b++) df_sub_prod_f(h, l, -Dr[b], z[b]);
+          X[(size_t)(6 * i + a) * w + c] = i <= bc ? df_norm(h, l) : df64{0.0f, 0.0f};
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_narrow_df(float *__restrict__ y, const df64 *__restrict__ x, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] = __fadd_rn(x[i].hi, x[i].lo);
+}
+
 // ------------------------------------------------------------ launchers
 // Dynamic shared memory of the apply kernel at its largest (one chunk of
 // CHUNK_MAX rows, or eight of APPLY_WARP_ROWS rows), above the default 48 KB
@@ -417,22 +503,46 @@ int chunk_alloc(Factor &f) {
   return 0;
 }
 
-__global__ void k_narrow(float *__restrict__ y, const double *__restrict__ x, size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
-    y[i] = (float)x[i];
-}
 
 template <typename TF>
 static int chunk_build_t(Factor &f, const TF *F, cudaStream_t s, long long *launches) {
   const int nch = (int)f.cp.lo.chunks.size();
   if (nch == 0) return 0;
+  const int ns_ = (int)f.cp.small.size(), nb_ = (int)f.cp.big.size();
+  if (f.precision == 32) {
+    // FP32 factor: gathered blocks as FP32 (in the scratch), inverses in
+    // double-float (in the FP64 inverse storage), then rounded to FP32
+    float *scr = reinterpret_cast<float *>(f.cscr64.p);
+    df64 *inv = reinterpret_cast<df64 *>(f.cinv64.p);
+    A2DS_CUDA_TRY(cudaMemsetAsync(scr, 0, (size_t)f.cp.scr_size * sizeof(float), s));
+    k_chunk_gather<TF, float><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                                  f.d_fcols.p, f.d_row_lend.p, f.d_row_ustart.p,
+                                                  F, scr);
+    if (ns_) {
+      k_chunk_inverse_df<false><<<ns_, 64, 0, s>>>(f.d_ck_small.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                                   scr, inv);
+      k_chunk_inverse_df<true><<<ns_, 64, 0, s>>>(f.d_ck_small.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                                  scr, inv);
+    }
+    if (nb_) {
+      k_chunk_inverse_df<false><<<nb_, 6 * CHUNK_MAX, 0, s>>>(f.d_ck_big.p, f.d_ck_c0.p,
+                                                              f.d_ck_off.p, scr, inv);
+      k_chunk_inverse_df<true><<<nb_, 6 * CHUNK_MAX, 0, s>>>(f.d_ck_big.p, f.d_ck_c0.p,
+                                                             f.d_ck_off.p, scr, inv);
+    }
+    const size_t n = (size_t)f.cp.inv_size;
+    k_narrow_df<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(f.cinv32.p,
+                                                                              inv, n);
+    if (launches) *launches += 2 + 2 * (ns_ > 0) + 2 * (nb_ > 0);
+    A2DS_CUDA_TRY(cudaGetLastError());
+    return 0;
+  }
   double *scr = f.cscr64.p, *inv = f.cinv64.p;
   A2DS_CUDA_TRY(cudaMemsetAsync(scr, 0, (size_t)f.cp.scr_size * sizeof(double), s));
-  k_chunk_gather<TF><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
-                                         f.d_fcols.p, f.d_row_lend.p, f.d_row_ustart.p, F, scr);
+  k_chunk_gather<TF, double><<<nch, 256, 0, s>>>(f.d_lo_chunks.p, f.d_ck_c0.p, f.d_ck_off.p,
+                                                 f.d_fcols.p, f.d_row_lend.p, f.d_row_ustart.p,
+                                                 F, scr);
   // small chunks: 64 threads; large ones: a thread per column (6 CHUNK_MAX)
-  const int ns_ = (int)f.cp.small.size(), nb_ = (int)f.cp.big.size();
   if (ns_) {
     k_chunk_inverse<double, false><<<ns_, 64, 0, s>>>(f.d_ck_small.p, f.d_ck_c0.p, f.d_ck_off.p,
                                                        scr, inv);
@@ -446,11 +556,6 @@ static int chunk_build_t(Factor &f, const TF *F, cudaStream_t s, long long *laun
                                                                 f.d_ck_off.p, scr, inv);
   }
   if (launches) *launches += 1 + 2 * (ns_ > 0) + 2 * (nb_ > 0);
-  if (f.precision == 32) {
-    const size_t n = (size_t)f.cp.inv_size;
-    k_narrow<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(f.cinv32.p, inv, n);
-    if (launches) *launches += 1;
-  }
   A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
 }
