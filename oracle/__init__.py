@@ -9,7 +9,8 @@ The C sources in oracle/c/ restate the reference (sean-engelstad/a2d-shells)
 function by function; they are pinned against fixtures generated by the
 reference itself (tests/golden/, see tests/golden/make_golden.py and
 oracle/ref/).  `load()` compiles them with gcc into oracle/_build/ on first
-use (also on the GPU machine, where no prebuilt x86 binary survives).
+use (on every machine, since a binary built on another architecture does
+not run).
 """
 from __future__ import annotations
 

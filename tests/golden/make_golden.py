@@ -17,7 +17,7 @@ builds) and packs inputs and outputs into small .npz files:
   f5.npz                .f5 files of the reference's TACSToFH5 (raw bytes)
                         for two seeded meshes and nine output-class flags
 
-Only this container has the reference sources; the fixtures are committed so
+Only a machine with the reference sources can run it; the fixtures are committed so
 the tests never need them.  Run:  python tests/golden/make_golden.py [part ...]
 (parts: the make_* names without the prefix, e.g. config1; default all).
 """

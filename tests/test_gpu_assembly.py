@@ -152,6 +152,26 @@ def test_cylinder_assembly_vs_reference(case, scatter):
     a.assemble_mat_type(capi.A2DS_GEOMETRIC_STIFFNESS_MATRIX, G, f["path"], scatter)
     _, _, gv = G.get_arrays()
     assert rel(gv, f["G"]) < 5e-11
+    # BCSRMat::copyValues / axpy / applyBCs (the shifted operator of
+    # TACSLinearBuckling::solve: aux <- K, aux += sigma G, aux.applyBCs)
+    # against the same operations on the reference's arrays and on this
+    # library's own K and G
+    A = a.create_mat()
+    A.copy_values(K)
+    assert np.array_equal(A.get_arrays()[2], vals)
+    sigma = 0.37
+    A.axpy(sigma, G)
+    av = A.get_arrays()[2]
+    assert rel(av, f["K_after"] + sigma * f["G"]) < 5e-11
+    # one rounding per entry (FMA or multiply-add) of |K| + |sigma G|
+    scale = np.abs(vals) + np.abs(sigma * gv)
+    close = np.abs(av - (vals + sigma * gv)) <= 4e-16 * scale
+    assert np.all(close)
+    A.apply_bcs()
+    av = A.get_arrays()[2]
+    # applyBCs only rewrites constrained rows, into K's (identity) rows
+    close = np.abs(av - (vals + sigma * gv)) <= 4e-16 * scale
+    assert np.all(close | (av == vals))
     # y = K x through the GPU SpMV against the reference's BCSRMat::mult
     xr = np.sin(1.0 + np.arange(6 * (rowp.size - 1)))
     y = np.zeros_like(xr)
