@@ -425,14 +425,13 @@ struct BucklingState {
   // Lanczos basis: AQ = (K + sigma G) Q per block, Cq = Q^T A Q; the
   // deflation space Y (Ritz vectors, defl_k columns in defl_k / p blocks),
   // AY = A Y and (Y^T A Y)^{-1} on the device
-  DBuf<double> AQ, dT, dHd, Yd, AYd, dCinv, dYc, dSk;
+  DBuf<double> AQ, dHd, Yd, dCinv, dYc, dSk;
   std::vector<double> Cq;
   int defl_k = 0;
   // the double-float inner solves: K + sigma G as df64, the deflation
   // vectors as FP32 with A Y as df64, the deflation residual
   DBuf<df64> AuxDF, AYdf, Tdf;
   DBuf<float> Yf;
-  bool use_df = false;
   std::vector<double> lam, err, ritz;  // converged data
   int nconv = 0;
   double sigma = 0.0;
@@ -609,9 +608,7 @@ int BucklingState::precond(Mesh &m, Factor &f, const double *V, double *Z, int p
 // than half ends the solve as converged to that floor.
 // Orthogonalisation: two classical Gram-Schmidt passes.  One host
 // synchronisation per Arnoldi step (the p columns' Hessenberg entries).
-// precond(V, Z, AZ, az) applies the preconditioner to one n6 x p block; a
-// preconditioner that forms A Z on the way stores it in AZ and sets az,
-// otherwise the solver forms it.
+// precond(V, Z) applies the preconditioner to one n6 x p block.
 template <class Precond>
 static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const double *Avals,
                               const double *X, double *Y, int p, double rtol, int msub,
@@ -674,9 +671,8 @@ static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const doubl
     for (int j = 0; j < msub; j++) {
       double *Vj = S.V.p + (size_t)j * bs, *Zj = S.Z.p + (size_t)j * bs;
       double *W = S.V.p + (size_t)(j + 1) * bs;
-      bool az = false;
-      if ((rc = precond(Vj, Zj, W, az))) return rc;
-      if (!az && (rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Avals, Zj, nullptr, W, p, m.stream)))
+      if ((rc = precond(Vj, Zj))) return rc;
+      if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, Avals, Zj, nullptr, W, p, m.stream)))
         return rc;
       if ((rc = col_dots(S.V.p, j + 1, bs, W, n6, p, dH1, m.stream))) return rc;
       if ((rc = col_axpy(W, S.V.p, j + 1, bs, dH1, n6, p, -1.0, m.stream))) return rc;
@@ -744,9 +740,7 @@ static int fgmres_block_solve(Mesh &m, IrWork &S, Precond &&precond, const doubl
 static int solve_k(Mesh &m, BucklingState &S, Factor &f, const double *Avals, const double *b,
                    double *x, double rtol, int *inner) {
   if (f.precision == 32) {
-    auto pc = [&](const double *V, double *Z, double *, bool &) {
-      return S.precond(m, f, V, Z, 1);
-    };
+    auto pc = [&](const double *V, double *Z) { return S.precond(m, f, V, Z, 1); };
     return fgmres_block_solve(m, S.ir, pc, Avals, b, x, 1, rtol, GMRES_IR_MSUB, GMRES_IR_CYCLES,
                               inner);
   }
@@ -773,7 +767,8 @@ __global__ void k_defl_coef(const double *__restrict__ Ci, const double *__restr
 // the FP32 pipe.  The solution Y and the
 // residual X - A Y that starts every cycle and decides convergence are FP64
 // (S.Aux).  With S.defl_k > 0 each preconditioned block is deflated by the
-// Ritz vectors (S.Yf, S.AYdf) as in defl_correct.
+// Ritz vectors (S.Yf, S.AYdf): z += Y (Y^T A Y)^{-1} Y^T (v - A z), with
+// A z corrected by A Y.
 static int fgmres_df_solve(Mesh &m, BucklingState &S, Factor &f, const double *X, double *Y,
                            int p, double rtol, int msub, int max_cycles, int *iters) {
   const size_t n6 = (size_t)m.nn * 6, bs = n6 * p;
@@ -1265,21 +1260,14 @@ static int defl_update_ritz(Mesh &m, BucklingState &S, const std::vector<double>
   int rc;
   if ((rc = S.dSk.upload(Sk.data(), Sk.size(), m.stream))) return rc;
   if ((rc = blk_mul(S.Q.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.Yd.p, m.stream))) return rc;
-  m.launches++;
-  if (S.use_df) {
-    // the double-float inner solves deflate with the FP32 rounding of Y and
-    // A times exactly that
-    if ((rc = f64_to_f32(S.Yf.p, S.Yd.p, (size_t)(k / p) * bs, m.stream))) return rc;
-    for (int b = 0; b < k / p; b++)
-      if ((rc = df_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.AuxDF.p, S.Yf.p + (size_t)b * bs,
-                        S.AYdf.p + (size_t)b * bs, p, m.stream)))
-        return rc;
-    m.launches += 1 + k / p;
-  } else {
-    if ((rc = blk_mul(S.AQ.p, mdim / p, bs, S.dSk.p, k / p, bs, n6, p, S.AYd.p, m.stream)))
+  // the double-float inner solves deflate with the FP32 rounding of Y and
+  // A times exactly that
+  if ((rc = f64_to_f32(S.Yf.p, S.Yd.p, (size_t)(k / p) * bs, m.stream))) return rc;
+  for (int b = 0; b < k / p; b++)
+    if ((rc = df_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.AuxDF.p, S.Yf.p + (size_t)b * bs,
+                      S.AYdf.p + (size_t)b * bs, p, m.stream)))
       return rc;
-    m.launches++;
-  }
+  m.launches += 2 + k / p;
   // Y^T A Y = Sk^T Cq Sk, inverted on its eigenvectors (|w| below 1e-12
   // max |w| dropped)
   std::vector<double> CS((size_t)mdim * k, 0.0), Cy((size_t)k * k, 0.0);
@@ -1309,34 +1297,6 @@ static int defl_update_ritz(Mesh &m, BucklingState &S, const std::vector<double>
   if ((rc = S.dCinv.upload(Ci.data(), Ci.size(), m.stream))) return rc;
   A2DS_CUDA_TRY(cudaStreamSynchronize(m.stream));  // the host tables go out of scope
   S.defl_k = k;
-  return 0;
-}
-
-__global__ void k_diff(double *__restrict__ T, const double *__restrict__ V,
-                       const double *__restrict__ AZ, size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
-    T[i] = V[i] - AZ[i];
-}
-
-// z <- z + Y Cinv Y^T (v - A z) for a block of p columns, and AZ = A z of
-// the corrected z: A z is formed once (the product GMRES needs anyway) and
-// corrected with AY, so the deflation costs no product with A of its own.
-// No host synchronisation.
-static int defl_correct(Mesh &m, BucklingState &S, const double *V, double *Z, double *AZ,
-                        int p) {
-  const int k = S.defl_k, kb = k / p;
-  const size_t n6 = (size_t)m.nn * 6, bs = n6 * p;
-  int rc;
-  if ((rc = blk_spmm(m.nn, m.d_rowp.p, m.d_cols.p, S.Aux.p, Z, nullptr, AZ, p, m.stream)))
-    return rc;
-  k_diff<<<grid_for(bs), 256, 0, m.stream>>>(S.dT.p, V, AZ, bs);  // T = V - A z
-  if ((rc = blk_dots(S.Yd.p, kb, bs, S.dT.p, n6, p, S.dHd.p, m.stream))) return rc;
-  k_defl_coef<<<1, 256, 0, m.stream>>>(S.dCinv.p, S.dHd.p, S.dYc.p, k, p);
-  if ((rc = blk_sub(Z, S.Yd.p, kb, bs, S.dYc.p, n6, p, m.stream))) return rc;
-  if ((rc = blk_sub(AZ, S.AYd.p, kb, bs, S.dYc.p, n6, p, m.stream))) return rc;
-  m.launches += 6;
-  A2DS_CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
@@ -1399,23 +1359,18 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
   // deflation of the GMRES-IR solves (FP32 factors only)
   const bool deflate = direct && S.fa.precision == 32;
   S.defl_k = 0;
-  S.use_df = deflate;
   if (deflate) {
     const int kb = DEFL_RITZ / p;
     if (DEFL_RITZ % p) return fail(A2DS_ERR_ARG, "deflation: block size must divide 16");
-    if ((rc = S.AQ.alloc((size_t)(nbmax + 1) * bs)) || (rc = S.dT.alloc(bs)) ||
+    if ((rc = S.AQ.alloc((size_t)(nbmax + 1) * bs)) ||
         (rc = S.dHd.alloc(std::max<size_t>((size_t)(nbmax + 1) * p * p, DEFL_RITZ * p))) ||
-        (rc = S.Yd.alloc((size_t)kb * bs)) ||
-        (rc = S.AYd.alloc((size_t)kb * bs)) || (rc = S.dCinv.alloc(DEFL_RITZ * DEFL_RITZ)) ||
-        (rc = S.dYc.alloc(DEFL_RITZ * p)))
+        (rc = S.Yd.alloc((size_t)kb * bs)) || (rc = S.dCinv.alloc(DEFL_RITZ * DEFL_RITZ)) ||
+        (rc = S.dYc.alloc(DEFL_RITZ * p)) || (rc = S.AuxDF.alloc(nv)) ||
+        (rc = S.Yf.alloc((size_t)kb * bs)) || (rc = S.AYdf.alloc((size_t)kb * bs)) ||
+        (rc = S.Tdf.alloc(bs)))
       return rc;
-    if (S.use_df) {
-      if ((rc = S.AuxDF.alloc(nv)) || (rc = S.Yf.alloc((size_t)kb * bs)) ||
-          (rc = S.AYdf.alloc((size_t)kb * bs)) || (rc = S.Tdf.alloc(bs)))
-        return rc;
-      if ((rc = df_from_f64(S.AuxDF.p, S.Aux.p, nv, m.stream))) return rc;
-      m.launches++;
-    }
+    if ((rc = df_from_f64(S.AuxDF.p, S.Aux.p, nv, m.stream))) return rc;
+    m.launches++;
     S.Cq.assign((size_t)tdim * tdim, 0.0);
     if ((rc = defl_add_block(m, S, B, 0, p, tdim))) return rc;
   }
@@ -1435,20 +1390,10 @@ static int shift_invert_phase(Mesh &m, BucklingState &S, const a2ds_buckling_opt
       // unaffected at that tolerance
       const double rtol = std::max(1e-12, std::min(1e-9, 0.1 * opts->eig_tol));
       if (S.fa.precision == 32) {
-        auto pc = [&](const double *V, double *Z, double *AZ, bool &az) {
-          int r2 = S.precond(m, S.fa, V, Z, p);
-          if (r2 || S.defl_k <= 0) return r2;
-          az = true;
-          return defl_correct(m, S, V, Z, AZ, p);
-        };
-        if (S.use_df) {
-          if ((rc = fgmres_df_solve(m, S, S.fa, KQj, W, p, rtol, GMRES_IR_MSUB, GMRES_IR_CYCLES,
-                                    &inner)))
-            return rc;
-        } else if ((rc = fgmres_block_solve(m, S.ir, pc, S.Aux.p, KQj, W, p, rtol, GMRES_IR_MSUB,
-                                            GMRES_IR_CYCLES, &inner))) {
+        // GMRES-IR with the double-float inner loop, deflated by Ritz vectors
+        if ((rc = fgmres_df_solve(m, S, S.fa, KQj, W, p, rtol, GMRES_IR_MSUB, GMRES_IR_CYCLES,
+                                  &inner)))
           return rc;
-        }
       } else if ((rc = refined_block_solve(m, S, S.fa, S.Aux.p, KQj, W, p, rtol, 2, &inner))) {
         return rc;
       }
@@ -1710,7 +1655,7 @@ int a2ds_fgmres_solve(a2ds_bcsr A, a2ds_pc pc, int msub, int nrestart, double rt
     return rc;
   }
   IrWork w;
-  auto precond = [&](const double *V, double *Z, double *, bool &) {
+  auto precond = [&](const double *V, double *Z) {
     return precondition_block(m, f, V, Z, nrhs, w32.p, xb.p, yb.p);
   };
   int it = 0;
@@ -2096,7 +2041,7 @@ int a2ds_newton_preload(a2ds_mesh mesh, const double *rhs, double load, int nste
   B.launches = &m.launches;
   const double fn = sqrt(B.dot(P->f.p, P->f.p, n6));
   if (!(fn > 0.0)) return fail(A2DS_ERR_ARG, "zero load vector");
-  auto pc = [&](const double *V, double *Z, double *, bool &) {
+  auto pc = [&](const double *V, double *Z) {
     return precondition_block(m, P->ft, V, Z, 1, P->w32.p, P->xb.p, P->yb.p);
   };
   double rel = 0.0;
