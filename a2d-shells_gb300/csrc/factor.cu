@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
 }
 
 // Phase 2 of a panel (runs of narrow levels whose pivot rows P are
-// factored together): one 384-thread CTA per target row i outside P.
+// factored together): one CTA per target row i outside P.
 // (a) Row i's L blocks in P's columns, in pivot order: L_ik = A_ik D_k^{-1}
 // (A_ik is final once the earlier pivots of P have been applied to it), kept
 // in shared memory, written back, and applied to row i's later P columns.
@@ -549,13 +549,26 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
 // uc, the union of P's U columns outside P) is held in registers while all
 // of row i's pivots in P are applied to it in pivot order, so the trailing
 // blocks are read and written once per panel instead of once per level.
+// FP32: one thread per target block (its 36 values in registers, the U
+// block read as nine 16-byte vectors, 216 multiply-adds per U block read);
+// FP64 and double-float: six threads per target block, one column each.
 // tab[k nuc + u] / tp[k PM + k2] are the U positions of pivot k at column
 // uc[u] / at P's column k2 (-1: none); task_jpk holds row i's L positions in
 // P's columns (-1: none).  Dynamic shared memory: row i's columns
 // (FACTOR_CTA_COLS ints) and uc (PANEL_UC_SMEM ints), each read from global
-// memory instead when longer.
+// memory instead when longer.  FP32 factor values must be 16-byte aligned
+// (checked by the launcher).
 template <typename T>
-__global__ void __launch_bounds__(384, 3) k_update_panel(
+struct PanelLaunch {
+  static constexpr int threads = 384, min_blocks = 3;
+};
+template <>
+struct PanelLaunch<float> {
+  static constexpr int threads = 256, min_blocks = 2;
+};
+template <typename T>
+__global__ void __launch_bounds__(PanelLaunch<T>::threads, PanelLaunch<T>::min_blocks)
+    k_update_panel(
     const int *__restrict__ task_row, const int *__restrict__ task_jpk, int ntasks,
     const int *__restrict__ prow, int np, const int *__restrict__ uc, int nuc, int cols_cap,
     int uc_cap,
@@ -563,7 +576,7 @@ __global__ void __launch_bounds__(384, 3) k_update_panel(
     const int *__restrict__ fcols, const int *__restrict__ fdiag, T *__restrict__ F) {
   constexpr int PM = PANEL_MAX_ROWS;
   extern __shared__ int s_dyn[];
-  __shared__ T s_L[PM][36];
+  __shared__ __align__(16) T s_L[PM][36];
   __shared__ int s_jp[PM], s_kk[PM], s_nk;
   const int t = blockIdx.x;
   if (t >= ntasks) return;
@@ -601,17 +614,72 @@ __global__ void __launch_bounds__(384, 3) k_update_panel(
       F[(size_t)jp * 36 + tid] = v;
     }
     __syncthreads();
-    if (kk + 1 + slot < nk) {
-      const int k2 = s_kk[kk + 1 + slot];
-      const int pu = tp[k * PM + k2];
-      if (pu >= 0) blk_col_update(F + (size_t)s_jp[k2] * 36, &s_L[k][0], F + (size_t)pu * 36, b);
-    }
+    if (slot < nslots)
+      for (int q = kk + 1 + slot; q < nk; q += nslots) {
+        const int k2 = s_kk[q];
+        const int pu = tp[k * PM + k2];
+        if (pu >= 0)
+          blk_col_update(F + (size_t)s_jp[k2] * 36, &s_L[k][0], F + (size_t)pu * 36, b);
+      }
     __syncthreads();  // before the next pivot reads its (updated) A_ik
   }
   // (b) the other blocks: positions after row i's first L block in P (the
   // pivot order of P is its level order, not its column order)
   int lo0 = len;
   for (int kk = 0; kk < nk; kk++) lo0 = min(lo0, s_jp[s_kk[kk]] - rs + 1);
+  if constexpr (std::is_same<T, float>::value) {
+    // one thread per target block; the U position of the next pivot is
+    // loaded while the current one is applied (nk >= 1 whenever lo0 < len)
+#pragma unroll 1
+    for (int pos = lo0 + tid; pos < len; pos += blockDim.x) {
+      const int u = find_col(ucs, 0, nuc, cols[pos]);
+      if (u < 0) continue;  // no U row of P reaches this block
+      float4 *C4 = reinterpret_cast<float4 *>(F + (size_t)(rs + pos) * 36);
+      float c[36];
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        const float4 v = C4[q];
+        c[4 * q] = v.x;
+        c[4 * q + 1] = v.y;
+        c[4 * q + 2] = v.z;
+        c[4 * q + 3] = v.w;
+      }
+      int pu_next = tab[(size_t)s_kk[0] * nuc + u];
+#pragma unroll 1
+      for (int kk = 0; kk < nk; kk++) {
+        const int k = s_kk[kk], pu = pu_next;
+        if (kk + 1 < nk) pu_next = tab[(size_t)s_kk[kk + 1] * nuc + u];
+        if (pu < 0) continue;
+        const float4 *U4 = reinterpret_cast<const float4 *>(F + (size_t)pu * 36);
+        float U[36];
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+          const float4 v = __ldg(U4 + q);  // U rows of P: read-only in this launch
+          U[4 * q] = v.x;
+          U[4 * q + 1] = v.y;
+          U[4 * q + 2] = v.z;
+          U[4 * q + 3] = v.w;
+        }
+        const float2 *L2 = reinterpret_cast<const float2 *>(&s_L[k][0]);
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+          const float2 l0 = L2[3 * a], l1 = L2[3 * a + 1], l2 = L2[3 * a + 2];
+          const float l[6] = {l0.x, l0.y, l1.x, l1.y, l2.x, l2.y};
+#pragma unroll
+          for (int bb = 0; bb < 6; bb++) {
+            float sacc = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 6; q++) sacc += l[q] * U[6 * q + bb];
+            c[6 * a + bb] = c[6 * a + bb] - sacc;
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 9; q++)
+        C4[q] = make_float4(c[4 * q], c[4 * q + 1], c[4 * q + 2], c[4 * q + 3]);
+    }
+    return;
+  }
 #pragma unroll 1
   for (int pos = lo0 + slot; pos < len; pos += nslots) {
     const int u = find_col(ucs, 0, nuc, cols[pos]);
@@ -680,6 +748,8 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
     A2DS_CUDA_TRY(cudaGetDevice(&dev));
     A2DS_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   }
+  if (std::is_same<T, float>::value && (reinterpret_cast<uintptr_t>(F) & 15))
+    return fail(A2DS_ERR_ARG, "FP32 factor values must be 16-byte aligned");
   long long nl = 0;
   const PanelSchedule &pn = f.pn;
   constexpr int PM = PANEL_MAX_ROWS;
@@ -742,7 +812,8 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
         // U columns), so more CTAs fit on an SM
         const int cols_cap = std::min(FACTOR_CTA_COLS, std::max(1, pn.task_maxlen[pk]));
         const int uc_cap = std::min(PANEL_UC_SMEM, std::max(1, nuc));
-        k_update_panel<T><<<ntk, 384, (cols_cap + uc_cap) * (int)sizeof(int), s>>>(
+        k_update_panel<T><<<ntk, PanelLaunch<T>::threads, (cols_cap + uc_cap) * (int)sizeof(int),
+                            s>>>(
             f.d_pn_task_row.p + a, f.d_pn_task_jpk.p + (size_t)a * PM, ntk,
             f.d_pn_prow.p + (size_t)pk * PM, pn.np[pk], f.d_pn_uc.p + u0, nuc, cols_cap, uc_cap,
             f.d_pn_tab.p + pn.tab_off[pk], f.d_pn_tp.p + (size_t)pk * PM * PM, f.d_frowp.p,
