@@ -566,6 +566,10 @@ template <>
 struct PanelLaunch<float> {
   static constexpr int threads = 256, min_blocks = 2;
 };
+template <>
+struct PanelLaunch<df64> {
+  static constexpr int threads = 384, min_blocks = 2;
+};
 template <typename T>
 __global__ void __launch_bounds__(PanelLaunch<T>::threads, PanelLaunch<T>::min_blocks)
     k_update_panel(
@@ -680,6 +684,69 @@ __global__ void __launch_bounds__(PanelLaunch<T>::threads, PanelLaunch<T>::min_b
     }
     return;
   }
+  if constexpr (std::is_same<T, df64>::value) {
+    // three threads per target block, thread h owning columns 2h and 2h + 1
+    // (16-byte loads of C, U and the L rows; the same operation sequence per
+    // value as blk_col_sub)
+    const int nsl = blockDim.x / 3, sl = tid / 3, h = tid - 3 * (tid / 3);
+    if (sl >= nsl) return;
+#pragma unroll 1
+    for (int pos = lo0 + sl; pos < len; pos += nsl) {
+      const int u = find_col(ucs, 0, nuc, cols[pos]);
+      if (u < 0) continue;  // no U row of P reaches this block
+      float4 *C4 = reinterpret_cast<float4 *>(F + (size_t)(rs + pos) * 36 + 2 * h);
+      float ch[12], cl[12];
+#pragma unroll
+      for (int a = 0; a < 6; a++) {
+        const float4 v = C4[3 * a];  // row a: 6 values of 8 bytes, 3 float4
+        ch[2 * a] = v.x;
+        cl[2 * a] = v.y;
+        ch[2 * a + 1] = v.z;
+        cl[2 * a + 1] = v.w;
+      }
+      int pu_next = tab[(size_t)s_kk[0] * nuc + u];
+#pragma unroll 1
+      for (int kk = 0; kk < nk; kk++) {
+        const int k = s_kk[kk], pu = pu_next;
+        if (kk + 1 < nk) pu_next = tab[(size_t)s_kk[kk + 1] * nuc + u];
+        if (pu < 0) continue;
+        const float4 *U4 = reinterpret_cast<const float4 *>(F + (size_t)pu * 36 + 2 * h);
+        df64 U0[6], U1[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+          const float4 v = __ldg(U4 + 3 * q);  // U rows of P: read-only in this launch
+          U0[q] = df64{v.x, v.y};
+          U1[q] = df64{v.z, v.w};
+        }
+        const float4 *L4 = reinterpret_cast<const float4 *>(&s_L[k][0]);
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+          df64 l[6];
+#pragma unroll
+          for (int q = 0; q < 3; q++) {
+            const float4 v = L4[3 * a + q];
+            l[2 * q] = df64{v.x, v.y};
+            l[2 * q + 1] = df64{v.z, v.w};
+          }
+          float h0 = ch[2 * a], l0 = cl[2 * a], h1 = ch[2 * a + 1], l1 = cl[2 * a + 1];
+#pragma unroll
+          for (int q = 0; q < 6; q++) {
+            df_sub_prod(h0, l0, l[q], U0[q]);
+            df_sub_prod(h1, l1, l[q], U1[q]);
+          }
+          const df64 r0 = df_norm(h0, l0), r1 = df_norm(h1, l1);
+          ch[2 * a] = r0.hi;
+          cl[2 * a] = r0.lo;
+          ch[2 * a + 1] = r1.hi;
+          cl[2 * a + 1] = r1.lo;
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < 6; a++)
+        C4[3 * a] = make_float4(ch[2 * a], cl[2 * a], ch[2 * a + 1], cl[2 * a + 1]);
+    }
+    return;
+  }
 #pragma unroll 1
   for (int pos = lo0 + slot; pos < len; pos += nslots) {
     const int u = find_col(ucs, 0, nuc, cols[pos]);
@@ -748,8 +815,8 @@ static int levels_t(const Factor &f, T *F, int *status, cudaStream_t s, long lon
     A2DS_CUDA_TRY(cudaGetDevice(&dev));
     A2DS_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
   }
-  if (std::is_same<T, float>::value && (reinterpret_cast<uintptr_t>(F) & 15))
-    return fail(A2DS_ERR_ARG, "FP32 factor values must be 16-byte aligned");
+  if (!std::is_same<T, double>::value && (reinterpret_cast<uintptr_t>(F) & 15))
+    return fail(A2DS_ERR_ARG, "FP32 and double-float factor values must be 16-byte aligned");
   long long nl = 0;
   const PanelSchedule &pn = f.pn;
   constexpr int PM = PANEL_MAX_ROWS;
