@@ -23,11 +23,13 @@
 // L_ij = A_ij D_j^{-1} (j in level l) and apply -L_ij U_j* to row i.
 // Pivots of one level never update each other's rows or L entries, and one
 // task owns its target row, so no atomics are needed.  Six threads share
-// each 6x6 block update (one output column each).  Long rows: one 384-thread
-// CTA per task (or several CTAs per single-pivot task when a level has few,
-// with k_factor_lcol forming the L blocks first).  Short rows: a group of 6,
-// 12 or 30 lanes per task within a warp, sized to the level's U-row lengths.
-// Runs of narrow levels are grouped into panels (k_update_panel).
+// each 6x6 block update (one output column each), except where noted: three
+// (two columns each) for double-float long rows and panels, one (the whole
+// block) for FP32 panels.  Long rows: one CTA per task (or several CTAs per
+// single-pivot task when a level has few, with k_factor_lcol forming the L
+// blocks first).  Short rows: a group of 6, 12 or 30 lanes per task within a
+// warp, sized to the level's U-row lengths.  Runs of narrow levels are
+// grouped into panels (k_update_panel).
 #include <type_traits>
 
 #include "a2ds_internal.h"
@@ -424,10 +426,59 @@ __device__ __forceinline__ void blk_col_update(T *C, const T *L, const T *U, int
   for (int a = 0; a < 6; a++) C[6 * a + b] = c[a];
 }
 
-// Long target rows: one 384-thread CTA per task (64 block updates at a
-// time, six threads each); every pivot's U blocks are strided over the
-// slots (a pivot's U columns are distinct, so no two slots touch one target
-// block), one barrier between pivots.  The row's column indices are staged
+// Columns 2h and 2h + 1 of C -= L U (double-float): 16-byte loads of C, U
+// and the L rows (L 16-byte aligned), the same operation sequence per value
+// as blk_col_sub.
+__device__ __forceinline__ void blk_update_pair(df64 *C, const df64 *L, const df64 *U, int h) {
+  float4 *C4 = reinterpret_cast<float4 *>(C + 2 * h);
+  const float4 *U4 = reinterpret_cast<const float4 *>(U + 2 * h);
+  df64 u0[6], u1[6];
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    const float4 v = U4[3 * q];
+    u0[q] = df64{v.x, v.y};
+    u1[q] = df64{v.z, v.w};
+  }
+  const float4 *L4 = reinterpret_cast<const float4 *>(L);
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    const float4 cv = C4[3 * a];
+    float h0 = cv.x, l0 = cv.y, h1 = cv.z, l1 = cv.w;
+    df64 l[6];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const float4 v = L4[3 * a + q];
+      l[2 * q] = df64{v.x, v.y};
+      l[2 * q + 1] = df64{v.z, v.w};
+    }
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+      df_sub_prod(h0, l0, l[q], u0[q]);
+      df_sub_prod(h1, l1, l[q], u1[q]);
+    }
+    const df64 r0 = df_norm(h0, l0), r1 = df_norm(h1, l1);
+    C4[3 * a] = make_float4(r0.hi, r0.lo, r1.hi, r1.lo);
+  }
+}
+
+// Threads per block update in the long-row kernel: three for double-float
+// (two columns each), six for FP64 and FP32 (one column each; one thread
+// per whole FP32 block needs ~140 registers, and the fewer resident warps
+// made the leaf levels' long tasks slower).
+template <typename T>
+struct UpdateLanes {
+  static constexpr int n = 6;
+};
+template <>
+struct UpdateLanes<df64> {
+  static constexpr int n = 3;
+};
+
+// Long target rows: one CTA per task (64 or 32 block updates at a time,
+// six threads each in FP64 and FP32, three in double-float); every pivot's
+// U blocks are strided over the update units (a pivot's U columns are
+// distinct, so no two units touch one target block), one barrier between
+// pivots.  The row's column indices are staged
 // in shared memory.  With nsplit == 1 the CTA also forms its L blocks
 // L_ij = A_ij D_j^{-1} (it owns them: no other task reads them in this
 // level).  With nsplit > 1 (levels whose tasks have one pivot each) nsplit
@@ -443,12 +494,13 @@ __global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ 
                                                         const int *__restrict__ fdiag,
                                                         T *__restrict__ F) {
   extern __shared__ int s_cols[];
-  __shared__ T s_L[36];
+  __shared__ __align__(16) T s_L[36];
   const int t = blockIdx.x / nsplit, sidx = blockIdx.x - nsplit * t;
   if (t >= ntasks) return;
   const int tid = threadIdx.x;
-  const int slot = tid / 6, b = tid - 6 * (tid / 6);
-  const int nslots = blockDim.x / 6;
+  constexpr int NL = UpdateLanes<T>::n;
+  const int slot = tid / NL, b = tid - NL * (tid / NL);
+  const int nslots = blockDim.x / NL;
   const int i = task_row[t];
   const int rs = frowp[i], len = frowp[i + 1] - rs;
   const bool staged = len <= cap;
@@ -473,12 +525,17 @@ __global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ 
     const int ue = frowp[j + 1], lo0 = jp + 1 - rs;
     const int stride = nslots * nsplit;
 #pragma unroll 1
-    for (int pu = fdiag[j] + 1 + sidx * nslots + slot; pu < ue; pu += stride) {
+    for (int pu = fdiag[j] + 1 + sidx * nslots + slot; slot < nslots && pu < ue; pu += stride) {
       // re-read s_L each block (cheap) rather than pinning 36 values in
       // registers for the whole loop, which would halve the resident warps
       asm volatile("" ::: "memory");
       const int pos = find_col(cols, lo0, len, fcols[pu]);
-      if (pos >= 0) blk_col_update(F + (size_t)(rs + pos) * 36, s_L, F + (size_t)pu * 36, b);
+      if (pos < 0) continue;
+      T *C = F + (size_t)(rs + pos) * 36;
+      if constexpr (std::is_same<T, df64>::value)
+        blk_update_pair(C, s_L, F + (size_t)pu * 36, b);
+      else
+        blk_col_update(C, s_L, F + (size_t)pu * 36, b);
     }
     __syncthreads();  // this pivot's updates done before the next pivot's
   }
