@@ -512,16 +512,18 @@ __global__ void __launch_bounds__(384, 2) k_update_long(const int *__restrict__ 
     const int j = fcols[jp];
     if (nsplit == 1) {
       T v{};
-      if (tid < 36) v = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[j] * 36, tid);
-      __syncthreads();  // every read of A_ij done before the in-place write
       if (tid < 36) {
+        v = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[j] * 36, tid);
         s_L[tid] = v;
-        F[(size_t)jp * 36 + tid] = v;
       }
-    } else if (tid < 36) {
-      s_L[tid] = F[(size_t)jp * 36 + tid];
+      __syncthreads();  // s_L (and, first time, s_cols) ready; every read of A_ij done
+      // in place, after every read of A_ij; no update of this pivot touches
+      // position jp (they search from jp + 1)
+      if (tid < 36) F[(size_t)jp * 36 + tid] = v;
+    } else {
+      if (tid < 36) s_L[tid] = F[(size_t)jp * 36 + tid];
+      __syncthreads();  // s_L (and, first time, s_cols) ready
     }
-    __syncthreads();  // s_L (and, first time, s_cols) ready
     const int ue = frowp[j + 1], lo0 = jp + 1 - rs;
     const int stride = nslots * nsplit;
 #pragma unroll 1
@@ -668,13 +670,14 @@ __global__ void __launch_bounds__(PanelLaunch<T>::threads, PanelLaunch<T>::min_b
   for (int kk = 0; kk < nk; kk++) {
     const int k = s_kk[kk], jp = s_jp[k];
     T v{};
-    if (tid < 36) v = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[prow[k]] * 36, tid);
-    __syncthreads();  // every read of A_ik done before the in-place write
     if (tid < 36) {
+      v = blk_mul_entry(F + (size_t)jp * 36, F + (size_t)fdiag[prow[k]] * 36, tid);
       s_L[k][tid] = v;
-      F[(size_t)jp * 36 + tid] = v;
     }
-    __syncthreads();
+    __syncthreads();  // s_L[k] ready; every read of A_ik done
+    // in place, after every read of A_ik; the updates below write only the
+    // blocks of row i's later pivots in P
+    if (tid < 36) F[(size_t)jp * 36 + tid] = v;
     if (slot < nslots)
       for (int q = kk + 1 + slot; q < nk; q += nslots) {
         const int k2 = s_kk[q];
