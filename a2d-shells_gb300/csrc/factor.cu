@@ -610,13 +610,14 @@ __global__ void __launch_bounds__(256) k_update_group(const int *__restrict__ ta
 // blocks are read and written once per panel instead of once per level.
 // FP32: one thread per target block (its 36 values in registers, the U
 // block read as nine 16-byte vectors, 216 multiply-adds per U block read);
-// FP64 and double-float: six threads per target block, one column each.
-// tab[k nuc + u] / tp[k PM + k2] are the U positions of pivot k at column
-// uc[u] / at P's column k2 (-1: none); task_jpk holds row i's L positions in
-// P's columns (-1: none).  Dynamic shared memory: row i's columns
-// (FACTOR_CTA_COLS ints) and uc (PANEL_UC_SMEM ints), each read from global
-// memory instead when longer.  FP32 factor values must be 16-byte aligned
-// (checked by the launcher).
+// double-float: three threads per target block, two columns each (16-byte
+// loads of C, U and the L rows); FP64: six threads per target block, one
+// column each.  tab[k nuc + u] / tp[k PM + k2] are the U positions of pivot
+// k at column uc[u] / at P's column k2 (-1: none); task_jpk holds row i's L
+// positions in P's columns (-1: none).  Dynamic shared memory: row i's
+// columns (FACTOR_CTA_COLS ints) and uc (PANEL_UC_SMEM ints), each read
+// from global memory instead when longer.  FP32 and double-float factor
+// values must be 16-byte aligned (checked by the launcher).
 template <typename T>
 struct PanelLaunch {
   static constexpr int threads = 384, min_blocks = 3;
