@@ -9,7 +9,7 @@ derivatives and the dense CPU restatement of the sensitivity formulas.
 * dlambda/dt_g (a2ds_eig_sens_thickness) against oracle/sens.py's dense
   restatement of the documented formula (src/TACSBuckling.cpp:359-382, the
   load-path adjoint included): 1e-6 of the largest |dlambda/dt_g| (the
-  spec bound), for a one-thickness cylinder and for every one of the
+  stated sensitivity accuracy), for a one-thickness cylinder and for every one of the
   400 groups of the stiffened panel; central differences of whole solves
   (step 1e-6 t_g) on 10 seeded panel groups.
 * dlambda/ds_p for 8 of the 64 radial shape parameters (a2ds_eig_sens_xpts
