@@ -4,7 +4,11 @@ oracle's solve of the same cylinder on the same host threads.  Test
 infrastructure: it calibrates the oracle port, which stands in for the
 reference where the reference's sources cannot travel.
 
-  python oracle/ref/ref_timing.py --nx 128 --ny 256 --threads 8 [--port]
+  python oracle/ref/ref_timing.py --nx 128 --ny 256 --threads 8 [--port] [--save F.npz]
+
+--save writes the reference's loads with the workload and run details to an
+npz fixture (tests/golden/cyl_q4_512x1024_ref_loads.npz came from
+--nx 512 --ny 1024 --threads 8: 2.6 h on 8 x86 cores).
 
 Only a machine with the reference sources builds cpu_ref_bench (the Makefile
 reads them from REF, default the reference checkout beside this repository's
@@ -45,6 +49,15 @@ def write_inputs(d, m, sigma, lev, gm_m, gm_restarts, lanczos, nev, gm_tol, eig_
     np.save(os.path.join(d, "params.npy"), prm)
 
 
+def save_fixture(path, ref, nx, ny, vectors):
+    """The reference run's loads and its set-up, as a test fixture."""
+    np.savez(path, nx=nx, ny=ny, sigma=float(ref["sigma"]),
+             eigvals=np.asarray(ref["eigvals"], np.float64),
+             lanczos_vectors=vectors, threads=int(ref["threads"]),
+             seconds=float(ref["seconds"]), gmres_iterations=int(ref["gmres_iterations"]),
+             gmres_cycles=int(ref["gmres_cycles"]))
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--nx", type=int, default=128)
@@ -61,6 +74,7 @@ def main(argv=None):
     p.add_argument("--eig-tol", type=float, default=1e-8)
     p.add_argument("--port", action="store_true",
                    help="also time the CPU oracle's solve on the same threads")
+    p.add_argument("--save", help="write the reference's loads to this npz fixture")
     args = p.parse_args(argv)
     if not os.path.exists(BIN):
         print(json.dumps({"unavailable": "oracle/_ref/cpu_ref_bench is not built "
@@ -81,6 +95,8 @@ def main(argv=None):
     ref = json.loads(line)
     ref.update(kind="reference", workload=f"cylinder {args.nx}x{args.ny}", sigma=sigma)
     print(json.dumps(ref), flush=True)
+    if args.save:
+        save_fixture(args.save, ref, args.nx, args.ny, args.vectors)
     if args.port:
         os.environ["OMP_NUM_THREADS"] = str(args.threads)
         import oracle

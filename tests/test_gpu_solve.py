@@ -520,3 +520,26 @@ def test_config1_cylinder_32x64_against_reference(precision):
     assert np.all(b.errors < 1e-8), b.errors
     for truth in (f["eigvals_sparse"][:nev], f["eigvals"][:nev]):
         assert np.max(np.abs(lam - truth) / np.abs(truth)) < 1e-8, (lam, truth)
+
+
+@pytest.mark.gpu
+def test_bench_workload_against_reference():
+    """The benchmark's workload (512 x 1024 Quad4 cylinder, 3,151,872 DOF,
+    sigma = 0.35 x the classical load) against the reference's own
+    TACSLinearBuckling::solve of the same mesh, run once on the host with its
+    sources (complete LU, GMRES to 1e-12, 76 Lanczos vectors, eig_tol 1e-8;
+    cyl_q4_512x1024_ref_loads.npz, written by oracle/ref/ref_timing.py
+    --save): the FP32-factor GMRES-IR solve's 10 lowest loads within 1e-8."""
+    from a2ds import mesh as meshgen
+    f = np.load(os.path.join(GOLDEN, "cyl_q4_512x1024_ref_loads.npz"))
+    m = meshgen.cylinder(int(f["nx"]), int(f["ny"]))
+    a = capi.Assembler(m.X, m.conn)
+    a.set_material(m.E, m.nu)
+    a.set_thickness([m.meta["t"]])
+    a.add_bcs(m.bc_nodes, m.bc_mask, m.bc_vals)
+    a.initialize(capi.A2DS_TACS_AMD_ORDER)
+    b = capi.LinearBuckling(a, float(f["sigma"]), max_lanczos=200, num_eigvals=10, eig_tol=1e-8,
+                            precision=32, block_size=4)
+    lam = np.sort(b.solve(m.rhs, want_vectors=False))
+    truth = np.sort(f["eigvals"])
+    assert np.max(np.abs(lam - truth) / np.abs(truth)) < 1e-8, (lam, truth)
