@@ -53,3 +53,19 @@ def test_reference_arm_other_ranks_do_no_work():
                        timeout=120)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_reference_loads_fixture_is_the_bench_workload():
+    """The 512x1024 reference-loads fixture (the GPU test's truth at the bench
+    size) was made on the benchmark's own workload: the same mesh size and
+    the same shift bench.py uses, and its loads lie above that shift."""
+    import numpy as np
+
+    sys.path.insert(0, REPO)
+    import bench
+    f = np.load(os.path.join(REPO, "tests", "golden", "cyl_q4_512x1024_ref_loads.npz"))
+    m = bench.build_workload(int(f["nx"]), int(f["ny"]))
+    assert (int(f["nx"]), int(f["ny"])) == (512, 1024)
+    assert float(f["sigma"]) == pytest.approx(bench.workload_sigma(m), rel=1e-15)
+    lam = np.asarray(f["eigvals"])
+    assert lam.size == 10 and np.all(np.diff(lam) >= 0) and lam[0] > float(f["sigma"])
